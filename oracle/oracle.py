@@ -1,0 +1,136 @@
+"""ctypes wrapper for the CPU oracle (test infrastructure, see clbm_oracle.c).
+
+``Oracle`` mirrors the reference objects: ``compute_force`` is
+``DroneMovingIBM.compute_force`` (airfoil_moving.py:230-255) and ``lbm_step`` is
+``CLBMSolver.step`` (clbm_moving.py:326-343); arrays come back in the reference layout,
+(Nx, Ny, Nz) and (Nx, Ny, Nz, 19), z fastest.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIBS = {}
+
+
+def load(real="f32"):
+    if real not in _LIBS:
+        path = _build.lib_path(real)
+        if not os.path.exists(path):
+            _build.build()
+        lib = ctypes.CDLL(path)
+        vp, d, i, ll = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_longlong
+        P = ctypes.c_void_p
+        lib.oracle_create.restype = vp
+        lib.oracle_create.argtypes = [i, i, i, d, d, d, d, i, P, P, P]
+        lib.oracle_destroy.argtypes = [vp]
+        lib.oracle_compute_force.argtypes = [vp] + [d] * 6
+        lib.oracle_lbm_step.argtypes = [vp]
+        lib.oracle_motion_state.argtypes = [ll] + [d] * 7 + [P]
+        lib.oracle_body_force.argtypes = [vp, P]
+        lib.oracle_run.argtypes = [vp, ll, i] + [d] * 7 + [P]
+        for name in ("oracle_get_f", "oracle_set_f", "oracle_minv", "oracle_get_markers"):
+            getattr(lib, name).argtypes = [vp, P]
+        lib.oracle_get_macro.argtypes = [vp, P, P, P, P]
+        lib.oracle_get_forces.argtypes = [vp, P, P, P]
+        lib.oracle_set_forces.argtypes = [vp, P, P, P]
+        lib.oracle_set_threads.argtypes = [i]
+        lib.oracle_max_threads.restype = i
+        lib.oracle_real_size.restype = i
+        _LIBS[real] = lib
+    return _LIBS[real]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def motion_state(step, m):
+    """_motion_state(step) (main_moving.py:62-74) for a motion dict with keys
+    x0, y0, a_heave, a_pitch, phi_pitch, aoa0, omega."""
+    out = np.zeros(6, np.float64)
+    load().oracle_motion_state(int(step), m["x0"], m["y0"], m["a_heave"], m["a_pitch"],
+                               m["phi_pitch"], m["aoa0"], m["omega"], _ptr(out))
+    return out
+
+
+class Oracle:
+    def __init__(self, nx, ny, nz, s_v, s_e, ux_in, uy_in, X0, Y0, Z0, real="f32",
+                 threads=None):
+        self.lib = load(real)
+        self.dtype = np.float32 if real == "f32" else np.float64
+        self.shape = (nx, ny, nz)
+        self.X0 = np.ascontiguousarray(X0, np.float32)
+        self.Y0 = np.ascontiguousarray(Y0, np.float32)
+        self.Z0 = np.ascontiguousarray(Z0, np.float32)
+        self.n = len(self.X0)
+        if threads:
+            self.lib.oracle_set_threads(int(threads))
+        self.h = self.lib.oracle_create(nx, ny, nz, s_v, s_e, ux_in, uy_in, self.n,
+                                        _ptr(self.X0), _ptr(self.Y0), _ptr(self.Z0))
+        if not self.h:
+            raise ValueError("oracle_create rejected the configuration")
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def compute_force(self, xc, yc, theta, vx, vy, omega):
+        self.lib.oracle_compute_force(self.h, xc, yc, theta, vx, vy, omega)
+
+    def lbm_step(self):
+        self.lib.oracle_lbm_step(self.h)
+
+    def run(self, step0, nsteps, m, record=True):
+        hist = np.zeros((nsteps, 4), np.float64) if record else None
+        self.lib.oracle_run(self.h, int(step0), int(nsteps), m["x0"], m["y0"], m["a_heave"],
+                            m["a_pitch"], m["phi_pitch"], m["aoa0"], m["omega"],
+                            _ptr(hist) if record else None)
+        return hist
+
+    def body_force(self):
+        out = np.zeros(4, np.float64)
+        self.lib.oracle_body_force(self.h, _ptr(out))
+        return out
+
+    def f(self):
+        out = np.empty(self.shape + (19,), self.dtype)
+        self.lib.oracle_get_f(self.h, _ptr(out))
+        return out
+
+    def set_f(self, f):
+        f = np.ascontiguousarray(f, self.dtype)
+        assert f.shape == self.shape + (19,)
+        self.lib.oracle_set_f(self.h, _ptr(f))
+
+    def macro(self):
+        outs = [np.empty(self.shape, self.dtype) for _ in range(4)]
+        self.lib.oracle_get_macro(self.h, *[_ptr(a) for a in outs])
+        return outs
+
+    def forces(self):
+        outs = [np.empty(self.shape, self.dtype) for _ in range(3)]
+        self.lib.oracle_get_forces(self.h, *[_ptr(a) for a in outs])
+        return outs
+
+    def set_forces(self, fx, fy, fz):
+        ins = [np.ascontiguousarray(a, self.dtype) for a in (fx, fy, fz)]
+        self.lib.oracle_set_forces(self.h, *[_ptr(a) for a in ins])
+
+    def markers(self):
+        out = np.empty((9, max(self.n, 1)), self.dtype)
+        self.lib.oracle_get_markers(self.h, _ptr(out))
+        names = ("X", "Y", "Z", "VX", "VY", "Uk", "Vk", "FXk", "FYk")
+        return {k: out[t, :self.n] for t, k in enumerate(names)}
+
+    def minv(self):
+        out = np.empty((19, 19), self.dtype)
+        self.lib.oracle_minv(self.h, _ptr(out))
+        return out
