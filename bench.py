@@ -1,0 +1,302 @@
+"""Benchmark: MLUPS of the D3Q19 cascaded-LBM + IBM time step on the 600x200x50 moving-wing
+case (chord 80, Re 200, 12,600 markers), plain float32 populations.
+
+A step is one full time step of the reference driver loop (main_moving.py:116-122):
+compute_force (marker kinematics, band macro, interpolation + spreading, force sums) and
+the fused stream-collide pass. MLUPS = Nx*Ny*Nz*steps / seconds / 1e6.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--storage f32|f16|bf16]
+
+--impl reference times the reference's arithmetic on the host cores instead: Taichi is not
+available, so that arm runs the C/OpenMP restatement of the reference's unfused 12-kernel
+step (oracle/clbm_oracle.c) with all host threads on the same case.
+Multi-GPU (torchrun): every rank runs an independent replica of the case ("replicas
+only": the single-case step has no data-parallel split); value aggregates all ranks.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL = {"f32": 152, "f16": 76, "bf16": 76}   # 19 loads + 19 stores
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--warmup", type=int, default=20)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=200)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        return False
+
+    def summary(self):
+        if not getattr(self, "lines", None):
+            return None
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(storage):
+    """DRAM bytes per fused launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", f"stream_collide_{storage}_600x200x50.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["dram_bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_baseline(cfg, steps=3):
+    """The oracle (reference arithmetic, unfused, OpenMP) on a bounded sample of the case."""
+    from oracle.oracle import Oracle, load
+    threads = load().oracle_max_threads()
+    o = Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+               cfg.X0, cfg.Y0, cfg.Z0)
+    o.run(0, 1, cfg.motion(), record=False)      # warm-up (first touch of the arrays)
+    t0 = time.perf_counter()
+    o.run(1, steps, cfg.motion(), record=False)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": cfg.cells * steps / dt / 1e6, "unit": "MLUPS", "cores": threads,
+            "kind": "port",
+            "sample": f"{steps} full steps of {cfg.nx}x{cfg.ny}x{cfg.nz} "
+                      f"({cfg.n_markers} markers) after 1 warm-up step, "
+                      "C/OpenMP restatement of the reference's unfused step"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import importlib
+    pkg = importlib.import_module("clbm_ibm-moving-airfoil_gb300")
+    cfg = pkg.full_case(storage="f32")
+    from oracle.oracle import Oracle, load
+    threads = load().oracle_max_threads()
+    # bounded sample: the oracle needs ~0.5-2 s per full step of this case
+    k = max(1, min(args.steps, 8))
+    w = max(0, min(args.warmup, 1))
+    o = Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+               cfg.X0, cfg.Y0, cfg.Z0)
+    if w:
+        o.run(0, w, cfg.motion(), record=False)
+    t0 = time.perf_counter()
+    o.run(w, k, cfg.motion(), record=False)
+    dt = time.perf_counter() - t0
+    o.close()
+    v = cfg.cells * k / dt / 1e6
+    return {
+        "metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": world, "steps": k,
+        "warmup": w, "ms_per_step": dt / k * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": "moving NACA0012 wing, D3Q19 CLBM + IBM, 600x200x50, chord 80, Re 200",
+                   "lattice": [cfg.nx, cfg.ny, cfg.nz], "markers": cfg.n_markers,
+                   "storage": "f32"},
+        "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"{k} of the requested {args.steps} steps after {w} warm-up; "
+                                   "Taichi is not installed, so the reference arm is the "
+                                   "C/OpenMP restatement of its unfused step"},
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_gpu(args, rank, world, local):
+    import importlib
+
+    import torch
+    pkg = importlib.import_module("clbm_ibm-moving-airfoil_gb300")
+    if world == 1:
+        pkg.build()   # no-op when the library is current; ranks of a multi-GPU run expect it built
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    cfg = pkg.full_case(storage=args.storage)
+    sim = pkg.Simulation(cfg, device=local)
+    solver, ibm = sim.solver, sim.ibm
+    stream = torch.cuda.ExternalStream(solver.stream_handle(), device=torch.device("cuda", local))
+
+    # ---- device-timed region: inputs resident in HBM, direct launches, fused kernel timed
+    sim.run(args.warmup, graph=False)
+    solver.synchronize()
+    launches0 = solver.profile_read()["total_launches"]
+    solver.profile(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        sim.run(args.steps, graph=False)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    prof = solver.profile_read()
+    solver.profile(False)
+    gpu_launches = prof["total_launches"] - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cfg.cells * args.steps * world / (ms / 1e3) / 1e6
+    st = solver.check()
+
+    # ---- graph-replayed loop (same work, one graph launch per two steps)
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.run(4, graph=True)
+    solver.synchronize()
+    g0.record(stream)
+    sim.run(args.steps, graph=True)
+    g1.record(stream)
+    g1.synchronize()
+    graph_ms = g0.elapsed_time(g1)
+
+    # ---- end to end through the public API: host motion per step (6 float32 kernel
+    # arguments) and the step's lift/drag sums read back (4 doubles) every step
+    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    step0 = ibm.step_count()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(1, e2e_steps + 1):
+        ibm.compute_force(*cfg.motion_state(step0 + k))
+        solver.step(ibm)
+        ibm.force_history(1)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = cfg.cells * e2e_steps * world / e2e_s / 1e6
+
+    fused_ms = prof["fused_ms"] / max(prof["fused_launches"], 1)
+    alg_bytes = BYTES_PER_CELL[args.storage] * cfg.cells
+    achieved = alg_bytes / (fused_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = traffic_from_profile(args.storage)
+    result = None
+    if rank == 0:
+        result = {
+            "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.storage, "data": "synthetic",
+            "config": {
+                "workload": "moving NACA0012 wing, D3Q19 CLBM + IBM, 600x200x50, chord 80, Re 200",
+                "lattice": [cfg.nx, cfg.ny, cfg.nz], "markers": cfg.n_markers,
+                "storage": args.storage, "parallelism": f"replicas x{world}",
+                "l2": "inputs larger than L2: 2 x %.0f MB population buffers" %
+                      (cfg.cells * 19 * (4 if args.storage == "f32" else 2) / 1e6),
+                "timed_region": "direct launches, per-step IBM + fused stream-collide",
+            },
+            "graph_value": cfg.cells * args.steps * world / (graph_ms / 1e3) / 1e6,
+            "gpu_launches": gpu_launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_stream_collide", "fused_ms_per_launch": fused_ms,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+            "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": 24,
+                    "d2h_bytes_per_step": 32,
+                    "how": "Python public API per step: IBM.compute_force(host motion) + "
+                           "Solver.step + read of the step's force sums"},
+            "check": {"rho_min": st["rho_min"], "rho_max": st["rho_max"], "u_max": st["u_max"]},
+            "clocks": clk.summary(),
+        }
+    sim.close()
+    if result is not None and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(pkg.full_case())
+    if dist is not None:
+        dist.destroy_process_group()
+    return result
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_gpu(args, rank, world, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,24 @@
+"""GB300-native D3Q19 cascaded-LBM + immersed-boundary time step.
+
+The package is loaded by path (its directory name is not a Python identifier):
+
+    import importlib, sys
+    sys.path.insert(0, "<repo root>")
+    clbm = importlib.import_module("clbm_ibm-moving-airfoil_gb300")
+
+Drop-in modules for the reference driver (``clbm_moving``, ``airfoil_moving`` and a
+``taichi`` import shim) live in ``compat/``; put that directory first on PYTHONPATH.
+"""
+
+from . import config
+from ._lib import CLBMError, DivergedError, EXPORTED, lib, lib_path
+from .build import build
+from .config import (SimConfig, force_coefficients, full_case, reference_airplane_case,
+                     small_case, wing_case)
+from .solver import IBM, PinnedBuffer, Simulation, Solver
+
+__all__ = [
+    "CLBMError", "DivergedError", "EXPORTED", "IBM", "PinnedBuffer", "SimConfig", "Simulation",
+    "Solver", "build", "config", "force_coefficients", "full_case", "lib", "lib_path",
+    "reference_airplane_case", "small_case", "wing_case",
+]

@@ -1,0 +1,642 @@
+// capi.cu -- extern "C" entry points (include/clbm_gb300.h): object lifetimes, host-side
+// sequencing of the kernels on the solver's stream, CUDA-graph capture of the time loop,
+// transfers in the reference layout and error reporting.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "clbm_internal.cuh"
+
+using namespace clbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(CLBM_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CK_LAUNCH()                                                                   \
+    do {                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                          \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(CLBM_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr double kWd[19] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
+                            1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
+                            1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
+constexpr int kHistCap = 1 << 16;
+// kernels one graph-captured step launches: markers, band-prepare, interp/spread, finish,
+// fused stream-collide
+constexpr int kKernelsPerIbmStep = 5;
+
+}  // namespace
+
+struct clbm_ibm;
+
+struct clbm_solver {
+    clbm_config cfg{};
+    Grid g{};
+    Coef c{};
+    void* f[2] = {nullptr, nullptr};
+    int cur = 0;
+    bool local = true;        // f[cur] holds a post-stream state (no pull on the next read)
+    bool macro_full = false;  // rho/ux/uy/uz hold the macro fields of the current state
+    float *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
+    float *dfx = nullptr, *dfy = nullptr, *dfz = nullptr;  // dense force, padded layout
+    float* stage = nullptr;
+    size_t stage_bytes = 0;
+    unsigned long long* stats = nullptr;
+    cudaStream_t st = nullptr;
+    long long launches = 0;
+    // profiling of the fused kernel
+    bool prof = false;
+    std::vector<cudaEvent_t> ev;
+    size_t ev_used = 0;
+    // cached two-step graph of the time loop
+    cudaGraphExec_t gexec = nullptr;
+    const clbm_ibm* g_ibm = nullptr;
+    clbm_motion g_m{};
+    int g_cur = -1;
+};
+
+struct clbm_ibm {
+    clbm_solver* s = nullptr;
+    IbmArrays a{};
+    long long calls = 0;   // host mirror of the device call counter
+};
+
+namespace {
+
+int ensure_stage(clbm_solver* s, size_t bytes) {
+    if (s->stage_bytes >= bytes) return CLBM_OK;
+    if (s->stage) CK(cudaFree(s->stage));
+    s->stage = nullptr;
+    s->stage_bytes = 0;
+    CK(cudaMalloc(&s->stage, bytes));
+    s->stage_bytes = bytes;
+    return CLBM_OK;
+}
+
+size_t cells(const clbm_solver* s) { return (size_t)s->g.nx * s->g.ny * s->g.nz; }
+
+int record_event(clbm_solver* s) {
+    if (s->ev_used == s->ev.size()) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        s->ev.push_back(e);
+    }
+    CK(cudaEventRecord(s->ev[s->ev_used++], s->st));
+    return CLBM_OK;
+}
+
+int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa) {
+    if (s->prof) {
+        int rc = record_event(s);
+        if (rc) return rc;
+    }
+    launch_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur], s->g,
+                          s->c, fa, s->st);
+    CK_LAUNCH();
+    if (s->prof) {
+        int rc = record_event(s);
+        if (rc) return rc;
+    }
+    s->launches += 1;
+    s->cur = 1 - s->cur;
+    s->local = false;
+    s->macro_full = false;
+    return CLBM_OK;
+}
+
+int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motion& m) {
+    clbm_solver* s = ibm->s;
+    launch_ibm_markers(ibm->a, s->g, devm, mf, m, s->st);
+    launch_band_prepare(s->cfg.storage, !s->local, s->f[s->cur], s->g, s->c, ibm->a.dev,
+                        ibm->a.fx, ibm->a.fy, s->rho, s->ux, s->uy, s->uz, ibm->a.max_bx,
+                        ibm->a.max_by, ibm->a.max_bz, !s->macro_full, s->st);
+    launch_ibm_interp_spread(ibm->a, s->g, s->st);
+    launch_ibm_finish(ibm->a, s->g, s->st);
+    CK_LAUNCH();
+    s->launches += (ibm->a.n > 0) ? 4 : 2;
+    ibm->calls += 1;
+    return CLBM_OK;
+}
+
+void free_graph(clbm_solver* s) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    s->gexec = nullptr;
+    s->g_ibm = nullptr;
+    s->g_cur = -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* clbm_last_error(void) { return g_err.c_str(); }
+
+int clbm_create(const clbm_config* cfg, clbm_solver** out) {
+    if (!cfg || !out) return fail(CLBM_ERR_ARG, "clbm_create: null argument");
+    *out = nullptr;
+    if (cfg->nx < 3 || cfg->ny < 1 || cfg->nz < 1)
+        return fail(CLBM_ERR_ARG, "clbm_create: lattice %dx%dx%d invalid (nx >= 3, ny, nz >= 1)",
+                    cfg->nx, cfg->ny, cfg->nz);
+    if (cfg->storage < CLBM_STORE_F32 || cfg->storage > CLBM_STORE_BF16S)
+        return fail(CLBM_ERR_ARG, "clbm_create: unknown storage %d", cfg->storage);
+    if (!(cfg->s_v > 0.0 && cfg->s_v < 2.0))
+        return fail(CLBM_ERR_ARG, "clbm_create: s_v = %g outside (0, 2)", cfg->s_v);
+    const long long pitch = ((long long)cfg->nx + 31) / 32 * 32;
+    const long long plane = pitch * cfg->ny * cfg->nz;
+    if (plane * 19 >= (1LL << 40))
+        return fail(CLBM_ERR_ARG, "clbm_create: lattice too large");
+    if (cudaSetDevice(cfg->device) != cudaSuccess)
+        return fail(CLBM_ERR_CUDA, "clbm_create: cannot use CUDA device %d: %s", cfg->device,
+                    cudaGetErrorString(cudaGetLastError()));
+    clbm_solver* s = new clbm_solver();
+    s->cfg = *cfg;
+    s->g.nx = cfg->nx; s->g.ny = cfg->ny; s->g.nz = cfg->nz;
+    s->g.pitch = (int)pitch; s->g.plane = plane;
+    s->c.one_m_sv = (float)(1.0 - cfg->s_v);
+    s->c.s_e = (float)cfg->s_e;
+    s->c.ux_in = (float)cfg->ux_in;
+    s->c.uy_in = (float)cfg->uy_in;
+    s->c.c23 = (float)(2.0 / 3.0);
+    s->c.c16 = (float)(1.0 / 6.0);
+    for (int q = 0; q < 19; ++q) s->c.wc[q] = (float)(kWd[q] * (1.0 - cfg->s_v * 0.5));
+    auto bail = [&](int rc) { clbm_destroy(s); return rc; };
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "clbm_create: no CUDA device or stream creation failed: %s",
+                         cudaGetErrorString(cudaGetLastError())));
+    const size_t fbytes = (size_t)plane * 19 * store_bytes(cfg->storage);
+    for (int b = 0; b < 2; ++b) {
+        if (cudaMalloc(&s->f[b], fbytes) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "clbm_create: cudaMalloc of %zu bytes failed", fbytes));
+        cudaMemsetAsync(s->f[b], 0, fbytes, s->st);
+    }
+    float** fields[] = {&s->rho, &s->ux, &s->uy, &s->uz};
+    for (float** p : fields) {
+        if (cudaMalloc(p, (size_t)plane * sizeof(float)) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "clbm_create: cudaMalloc of macro field failed"));
+        cudaMemsetAsync(*p, 0, (size_t)plane * sizeof(float), s->st);
+    }
+    if (cudaMalloc(&s->stats, 4 * sizeof(unsigned long long)) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "clbm_create: cudaMalloc failed"));
+    launch_init(cfg->storage, s->f[0], s->g, s->c, s->st);
+    launch_fill_macro(s->g, s->c, s->rho, s->ux, s->uy, s->uz, s->st);
+    s->launches += 2;
+    s->cur = 0;
+    s->local = true;
+    s->macro_full = true;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "clbm_create: %s", cudaGetErrorString(e)));
+    *out = s;
+    return CLBM_OK;
+}
+
+int clbm_destroy(clbm_solver* s) {
+    if (!s) return CLBM_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    free_graph(s);
+    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+    void* ptrs[] = {s->f[0], s->f[1], s->rho, s->ux, s->uy, s->uz, s->dfx, s->dfy, s->dfz,
+                    s->stage, s->stats};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return CLBM_OK;
+}
+
+int clbm_step(clbm_solver* s, const clbm_ibm* ibm) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_step: null solver");
+    if (ibm && ibm->s != s) return fail(CLBM_ERR_ARG, "clbm_step: IBM bound to another solver");
+    ForceArgs fa{};
+    if (ibm) {
+        fa.fx = ibm->a.fx;
+        fa.fy = ibm->a.fy;
+        fa.dev = ibm->a.dev;
+    }
+    return step_impl(s, ibm ? kForceBand : kForceNone, fa);
+}
+
+int clbm_step_dense_force(clbm_solver* s, const float* fx, const float* fy, const float* fz) {
+    if (!s || !fx || !fy) return fail(CLBM_ERR_ARG, "clbm_step_dense_force: null argument");
+    const size_t pb = (size_t)s->g.plane * sizeof(float);
+    float** bufs[] = {&s->dfx, &s->dfy, &s->dfz};
+    for (float** p : bufs)
+        if (!*p) {
+            CK(cudaMalloc(p, pb));
+            CK(cudaMemsetAsync(*p, 0, pb, s->st));
+        }
+    launch_import_field(fx, s->dfx, s->g, s->st);
+    launch_import_field(fy, s->dfy, s->g, s->st);
+    if (fz) launch_import_field(fz, s->dfz, s->g, s->st);
+    else CK(cudaMemsetAsync(s->dfz, 0, pb, s->st));
+    CK_LAUNCH();
+    s->launches += fz ? 3 : 2;
+    ForceArgs fa{s->dfx, s->dfy, s->dfz, nullptr};
+    return step_impl(s, kForceDense, fa);
+}
+
+int clbm_step_host_force(clbm_solver* s, const float* fx, const float* fy, const float* fz) {
+    if (!s || !fx || !fy) return fail(CLBM_ERR_ARG, "clbm_step_host_force: null argument");
+    const size_t n = cells(s);
+    int rc = ensure_stage(s, 3 * n * sizeof(float));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->stage, fx, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(s->stage + n, fy, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    if (fz) CK(cudaMemcpyAsync(s->stage + 2 * n, fz, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    rc = clbm_step_dense_force(s, s->stage, s->stage + n, fz ? s->stage + 2 * n : nullptr);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->st));  // the host arrays may be released after return
+    return CLBM_OK;
+}
+
+static int materialize(clbm_solver* s, bool with_stats) {
+    if (with_stats) {
+        unsigned long long init[4] = {~0ull, 0ull, 0ull, 0ull};
+        CK(cudaMemcpyAsync(s->stats, init, sizeof(init), cudaMemcpyHostToDevice, s->st));
+    }
+    if (!s->macro_full || with_stats) {
+        launch_macro_full(s->cfg.storage, !s->local, s->f[s->cur], s->g, s->c, s->rho, s->ux,
+                          s->uy, s->uz, with_stats ? s->stats : nullptr, s->st);
+        CK_LAUNCH();
+        s->launches += 1;
+        s->macro_full = true;
+    }
+    return CLBM_OK;
+}
+
+int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_read_macro: null solver");
+    int rc = materialize(s, false);
+    if (rc) return rc;
+    const size_t n = cells(s);
+    rc = ensure_stage(s, 4 * n * sizeof(float));
+    if (rc) return rc;
+    const float* src[4] = {s->rho, s->ux, s->uy, s->uz};
+    float* dst[4] = {rho, ux, uy, uz};
+    for (int k = 0; k < 4; ++k) {
+        if (!dst[k]) continue;
+        launch_export_field(src[k], s->stage + k * n, s->g, 0.0f, s->st);
+        CK_LAUNCH();
+        s->launches += 1;
+        CK(cudaMemcpyAsync(dst[k], s->stage + k * n, n * sizeof(float), cudaMemcpyDeviceToHost,
+                           s->st));
+    }
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
+int clbm_read_populations(clbm_solver* s, float* f_host) {
+    if (!s || !f_host) return fail(CLBM_ERR_ARG, "clbm_read_populations: null argument");
+    const size_t n = cells(s) * 19;
+    int rc = ensure_stage(s, n * sizeof(float));
+    if (rc) return rc;
+    launch_export_populations(s->cfg.storage, !s->local, s->f[s->cur], s->stage, s->g, s->c,
+                              s->st);
+    CK_LAUNCH();
+    s->launches += 1;
+    CK(cudaMemcpyAsync(f_host, s->stage, n * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
+int clbm_write_populations(clbm_solver* s, const float* f_host) {
+    if (!s || !f_host) return fail(CLBM_ERR_ARG, "clbm_write_populations: null argument");
+    const size_t n = cells(s) * 19;
+    int rc = ensure_stage(s, n * sizeof(float));
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->stage, f_host, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
+    launch_import_populations(s->cfg.storage, s->stage, s->f[s->cur], s->g, s->st);
+    CK_LAUNCH();
+    s->launches += 1;
+    s->local = true;
+    s->macro_full = false;
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
+static double from_ordered(unsigned long long v) {
+    unsigned int u = (unsigned int)v;
+    u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return (double)f;
+}
+
+int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_max,
+               double* u_max, int64_t* nonfinite) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_check: null solver");
+    int rc = materialize(s, true);
+    if (rc) return rc;
+    unsigned long long h[4];
+    CK(cudaMemcpyAsync(h, s->stats, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    const bool any = h[0] != ~0ull;
+    const double rmin = any ? from_ordered(h[0]) : NAN;
+    const double rmax = any ? from_ordered(h[1]) : NAN;
+    const double u2 = any ? from_ordered(h[2]) : NAN;
+    if (rho_min) *rho_min = rmin;
+    if (rho_max) *rho_max = rmax;
+    if (u_max) *u_max = std::sqrt(u2);
+    if (nonfinite) *nonfinite = (int64_t)h[3];
+    if (h[3] > 0 || !any || rmin < rho_floor)
+        return fail(CLBM_ERR_DIVERGED, "clbm_check: diverged (rho_min=%g, nonfinite=%llu)", rmin,
+                    (unsigned long long)h[3]);
+    return CLBM_OK;
+}
+
+int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0, int32_t n,
+               clbm_ibm** out) {
+    if (!s || !out || n < 0 || (n > 0 && (!X0 || !Y0 || !Z0)))
+        return fail(CLBM_ERR_ARG, "ibm_create: invalid argument");
+    *out = nullptr;
+    clbm_ibm* ibm = new clbm_ibm();
+    ibm->s = s;
+    IbmArrays& a = ibm->a;
+    a.n = n;
+    a.hist_cap = kHistCap;
+    auto bail = [&](int rc) { ibm_destroy(ibm); return rc; };
+    const size_t nb = (size_t)(n > 0 ? n : 1) * sizeof(float);
+    float** marr[] = {(float**)&a.X0, (float**)&a.Y0, (float**)&a.Z0, &a.X, &a.Y, &a.Z,
+                      &a.VX, &a.VY, &a.Uk, &a.Vk, &a.FXk, &a.FYk};
+    for (float** p : marr) {
+        if (cudaMalloc(p, nb) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc failed"));
+        cudaMemsetAsync(*p, 0, nb, s->st);
+    }
+    const size_t pb = (size_t)s->g.plane * sizeof(float);
+    if (cudaMalloc(&a.fx, pb) != cudaSuccess || cudaMalloc(&a.fy, pb) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc of force fields failed"));
+    cudaMemsetAsync(a.fx, 0, pb, s->st);
+    cudaMemsetAsync(a.fy, 0, pb, s->st);
+    if (cudaMalloc(&a.dev, sizeof(IbmDev)) != cudaSuccess ||
+        cudaMalloc(&a.hist, (size_t)kHistCap * 4 * sizeof(double)) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc failed"));
+    cudaMemsetAsync(a.hist, 0, (size_t)kHistCap * 4 * sizeof(double), s->st);
+    IbmDev init{};
+    init.step = 0;
+    for (int sl = 0; sl < 2; ++sl)
+        for (int e = 0; e < 6; ++e) init.box[sl][e] = kBoxEmpty;
+    if (n > 0) {
+        cudaMemcpyAsync((void*)a.X0, X0, n * sizeof(float), cudaMemcpyHostToDevice, s->st);
+        cudaMemcpyAsync((void*)a.Y0, Y0, n * sizeof(float), cudaMemcpyHostToDevice, s->st);
+        cudaMemcpyAsync((void*)a.Z0, Z0, n * sizeof(float), cudaMemcpyHostToDevice, s->st);
+    }
+    cudaMemcpyAsync(a.dev, &init, sizeof(init), cudaMemcpyHostToDevice, s->st);
+    // Upper bound of the stencil box for any rigid motion: the template radius about the
+    // pivot bounds x and y; z is fixed.
+    double r2 = 0.0, zmin = 0.0, zmax = 0.0;
+    for (int m = 0; m < n; ++m) {
+        const double rr = (double)X0[m] * X0[m] + (double)Y0[m] * Y0[m];
+        if (!std::isfinite(rr) || !std::isfinite((double)Z0[m]))
+            return bail(fail(CLBM_ERR_ARG, "ibm_create: non-finite marker %d", m));
+        r2 = rr > r2 ? rr : r2;
+        zmin = (m == 0 || Z0[m] < zmin) ? Z0[m] : zmin;
+        zmax = (m == 0 || Z0[m] > zmax) ? Z0[m] : zmax;
+    }
+    const int span = (int)std::ceil(2.0 * std::sqrt(r2)) + 6;
+    a.max_bx = std::min(s->g.nx, span);
+    a.max_by = std::min(s->g.ny, span);
+    a.max_bz = n > 0 ? std::min(s->g.nz, (int)(std::floor(zmax) - std::floor(zmin)) + 5) : 1;
+    a.ux = s->ux;
+    a.uy = s->uy;
+    cudaError_t e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return bail(fail(CLBM_ERR_CUDA, "ibm_create: %s", cudaGetErrorString(e)));
+    *out = ibm;
+    return CLBM_OK;
+}
+
+int ibm_destroy(clbm_ibm* ibm) {
+    if (!ibm) return CLBM_OK;
+    if (ibm->s) {
+        cudaStreamSynchronize(ibm->s->st);
+        if (ibm->s->g_ibm == ibm) free_graph(ibm->s);
+    }
+    IbmArrays& a = ibm->a;
+    void* ptrs[] = {(void*)a.X0, (void*)a.Y0, (void*)a.Z0, a.X, a.Y, a.Z, a.VX, a.VY, a.Uk,
+                    a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete ibm;
+    return CLBM_OK;
+}
+
+int ibm_compute_force(clbm_ibm* ibm, double xc, double yc, double theta, double vx, double vy,
+                      double omega) {
+    if (!ibm) return fail(CLBM_ERR_ARG, "ibm_compute_force: null IBM");
+    MotionF mf{(float)xc, (float)yc, (float)theta, (float)vx, (float)vy, (float)omega};
+    return ibm_force_impl(ibm, false, mf, clbm_motion{});
+}
+
+int ibm_compute_force_motion(clbm_ibm* ibm, const clbm_motion* m) {
+    if (!ibm || !m) return fail(CLBM_ERR_ARG, "ibm_compute_force_motion: null argument");
+    return ibm_force_impl(ibm, true, MotionF{}, *m);
+}
+
+int ibm_read_forces(const clbm_ibm* ibm, float* fx, float* fy, float* fz) {
+    if (!ibm) return fail(CLBM_ERR_ARG, "ibm_read_forces: null IBM");
+    clbm_solver* s = ibm->s;
+    const size_t n = cells(s);
+    int rc = ensure_stage(s, 2 * n * sizeof(float));
+    if (rc) return rc;
+    const float* src[2] = {ibm->a.fx, ibm->a.fy};
+    float* dst[2] = {fx, fy};
+    for (int k = 0; k < 2; ++k) {
+        if (!dst[k]) continue;
+        launch_export_field(src[k], s->stage + k * n, s->g, 0.05f, s->st);
+        CK_LAUNCH();
+        s->launches += 1;
+        CK(cudaMemcpyAsync(dst[k], s->stage + k * n, n * sizeof(float), cudaMemcpyDeviceToHost,
+                           s->st));
+    }
+    CK(cudaStreamSynchronize(s->st));
+    if (fz) std::memset(fz, 0, n * sizeof(float));
+    return CLBM_OK;
+}
+
+int ibm_read_markers(const clbm_ibm* ibm, float* out) {
+    if (!ibm || !out) return fail(CLBM_ERR_ARG, "ibm_read_markers: null argument");
+    const IbmArrays& a = ibm->a;
+    const float* src[9] = {a.X, a.Y, a.Z, a.VX, a.VY, a.Uk, a.Vk, a.FXk, a.FYk};
+    for (int k = 0; k < 9; ++k)
+        if (a.n > 0)
+            CK(cudaMemcpyAsync(out + (size_t)k * a.n, src[k], a.n * sizeof(float),
+                               cudaMemcpyDeviceToHost, ibm->s->st));
+    CK(cudaStreamSynchronize(ibm->s->st));
+    return CLBM_OK;
+}
+
+int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out) {
+    if (!ibm || !out || count < 0) return fail(CLBM_ERR_ARG, "ibm_read_force_history: bad argument");
+    const long long avail = std::min<long long>(ibm->calls, kHistCap);
+    if (count > avail)
+        return fail(CLBM_ERR_ARG, "ibm_read_force_history: %d entries requested, %lld available",
+                    count, avail);
+    // entries calls-count .. calls-1 occupy at most two contiguous runs of the ring
+    int done = 0;
+    while (done < count) {
+        const long long slot = (ibm->calls - count + done) % kHistCap;
+        const int run = (int)std::min<long long>(count - done, kHistCap - slot);
+        CK(cudaMemcpyAsync(out + 4 * (size_t)done, ibm->a.hist + 4 * slot,
+                           (size_t)run * 4 * sizeof(double), cudaMemcpyDeviceToHost, ibm->s->st));
+        done += run;
+    }
+    CK(cudaStreamSynchronize(ibm->s->st));
+    return CLBM_OK;
+}
+
+int ibm_step_count(const clbm_ibm* ibm, int64_t* out) {
+    if (!ibm || !out) return fail(CLBM_ERR_ARG, "ibm_step_count: null argument");
+    *out = ibm->calls;
+    return CLBM_OK;
+}
+
+int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps,
+             int32_t use_graph) {
+    if (!s || nsteps < 0 || (ibm && !m)) return fail(CLBM_ERR_ARG, "clbm_run: invalid argument");
+    if (ibm && ibm->s != s) return fail(CLBM_ERR_ARG, "clbm_run: IBM bound to another solver");
+    int done = 0;
+    auto one = [&]() -> int {
+        if (ibm) {
+            int rc = ibm_compute_force_motion(ibm, m);
+            if (rc) return rc;
+        }
+        return clbm_step(s, ibm);
+    };
+    const bool graph = use_graph && !s->prof;
+    // steps that change the kernel variants (first pull, macro already materialised) or
+    // leave an odd remainder run as plain launches
+    while (done < nsteps && graph && (s->local || s->macro_full)) {
+        int rc = one();
+        if (rc) return rc;
+        ++done;
+    }
+    if (graph && nsteps - done >= 2) {
+        const bool same = s->gexec && s->g_ibm == ibm && s->g_cur == s->cur &&
+                          (!ibm || std::memcmp(&s->g_m, m, sizeof(clbm_motion)) == 0);
+        if (!same) {
+            free_graph(s);
+            const int cur0 = s->cur;
+            const long long launches0 = s->launches;
+            const long long calls0 = ibm ? ibm->calls : 0;
+            CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+            int rc = one();
+            if (!rc) rc = one();
+            cudaGraph_t graph_obj = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s->st, &graph_obj);
+            // capture only recorded the work: restore the host mirrors
+            s->cur = cur0;
+            s->launches = launches0;
+            if (ibm) ibm->calls = calls0;
+            if (rc) {
+                if (graph_obj) cudaGraphDestroy(graph_obj);
+                return rc;
+            }
+            if (e != cudaSuccess)
+                return fail(CLBM_ERR_CUDA, "clbm_run: graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&s->gexec, graph_obj, 0);
+            cudaGraphDestroy(graph_obj);
+            if (e != cudaSuccess)
+                return fail(CLBM_ERR_CUDA, "clbm_run: graph instantiate failed: %s", cudaGetErrorString(e));
+            s->g_ibm = ibm;
+            if (ibm) s->g_m = *m;
+            s->g_cur = cur0;
+        }
+        const int per = ibm ? (ibm->a.n > 0 ? kKernelsPerIbmStep : kKernelsPerIbmStep - 2) : 1;
+        while (nsteps - done >= 2) {
+            CK(cudaGraphLaunch(s->gexec, s->st));
+            done += 2;
+            s->launches += 2 * per;
+            if (ibm) ibm->calls += 2;
+        }
+        s->local = false;
+        s->macro_full = false;
+    }
+    while (done < nsteps) {
+        int rc = one();
+        if (rc) return rc;
+        ++done;
+    }
+    return CLBM_OK;
+}
+
+int clbm_synchronize(clbm_solver* s) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_synchronize: null solver");
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
+int clbm_stream(const clbm_solver* s, void** out) {
+    if (!s || !out) return fail(CLBM_ERR_ARG, "clbm_stream: null argument");
+    *out = (void*)s->st;
+    return CLBM_OK;
+}
+
+int clbm_profile_enable(clbm_solver* s, int32_t on) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_profile_enable: null solver");
+    CK(cudaStreamSynchronize(s->st));
+    s->prof = on != 0;
+    s->ev_used = 0;
+    return CLBM_OK;
+}
+
+int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
+                      int64_t* total_launches) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_profile_read: null solver");
+    CK(cudaStreamSynchronize(s->st));
+    double ms = 0.0;
+    for (size_t i = 0; i + 1 < s->ev_used; i += 2) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, s->ev[i], s->ev[i + 1]));
+        ms += t;
+    }
+    if (fused_ms) *fused_ms = ms;
+    if (fused_launches) *fused_launches = (int64_t)(s->ev_used / 2);
+    if (total_launches) *total_launches = s->launches;
+    return CLBM_OK;
+}
+
+int clbm_device_bytes(const clbm_solver* s, int64_t* out) {
+    if (!s || !out) return fail(CLBM_ERR_ARG, "clbm_device_bytes: null argument");
+    const size_t pb = (size_t)s->g.plane * sizeof(float);
+    size_t b = 2 * (size_t)s->g.plane * 19 * store_bytes(s->cfg.storage) + 4 * pb;
+    if (s->dfx) b += 3 * pb;
+    b += s->stage_bytes;
+    *out = (int64_t)b;
+    return CLBM_OK;
+}
+
+int clbm_host_alloc(int64_t bytes, void** out) {
+    if (!out || bytes <= 0) return fail(CLBM_ERR_ARG, "clbm_host_alloc: invalid argument");
+    CK(cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault));
+    return CLBM_OK;
+}
+
+int clbm_host_free(void* p) {
+    if (p) CK(cudaFreeHost(p));
+    return CLBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+// clbm_internal.cuh -- device data layout, shared device helpers and kernel launchers.
+//
+// Layout in HBM (all grids): structure of arrays, x fastest, rows padded to `pitch`
+// elements (a multiple of 32, so every row starts on a 128-byte boundary for float32):
+//   population q of cell (x, y, z):  f[q * plane + (z * ny + y) * pitch + x]
+//   scalar field of cell (x, y, z):  a[(z * ny + y) * pitch + x]
+// with plane = pitch * ny * nz. The solver stores the post-collision, pre-stream state
+// (f_post) and pulls from it, so one fused pass per step reads 19 and writes 19 values
+// per cell. Host-visible arrays use the reference layout (x, y, z) with z fastest and are
+// produced by transposing export kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "../../include/clbm_gb300.h"
+
+namespace clbm {
+
+// D3Q19 velocity set of the reference (clbm_moving.py:21-30); the order fixes which
+// populations the Zou-He inlet reconstructs.
+__host__ __device__ constexpr int ex(int q) {
+    return (q == 1 || q == 7 || q == 9 || q == 11 || q == 13) ? 1
+         : (q == 2 || q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int ey(int q) {
+    return (q == 3 || q == 7 || q == 8 || q == 15 || q == 17) ? 1
+         : (q == 4 || q == 9 || q == 10 || q == 16 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int ez(int q) {
+    return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
+         : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr float wq(int q) {
+    return q == 0 ? 1.0f / 3.0f : (q <= 6 ? 1.0f / 18.0f : 1.0f / 36.0f);
+}
+
+struct Grid {
+    int nx, ny, nz, pitch;
+    long long plane;  // pitch * ny * nz
+};
+
+// Collision and boundary constants, rounded to float once on the host.
+struct Coef {
+    float one_m_sv;   // 1 - s_v
+    float s_e;        // trace relaxation rate
+    float ux_in, uy_in;
+    float c23, c16;   // 2/3 and 1/6 of the Zou-He inlet
+    float wc[19];     // w_q * (1 - s_v / 2), Guo forcing weight
+};
+
+// Band box of the IBM stencils: all six entries are reduced with atomicMin, maxima stored
+// negated. The reset value 0x7f7f7f7f marks an empty box.
+constexpr int kBoxEmpty = 0x7f7f7f7f;
+
+struct IbmDev {
+    long long step;        // number of completed compute_force calls
+    int box[2][6];         // slot (call index & 1): imin, -imax, jmin, -jmax, kmin, -kmax
+    double acc[4];         // sum fx, sum fy (clipped Eulerian), sum FX_k, sum FY_k
+    unsigned int ticket;   // last-block detection of the force-sum kernel
+    int pad;
+};
+
+// Box in lattice coordinates with periodic y/z: x in [i0, i0 + ilen), y in
+// (j0 + [0, jlen)) mod ny, z in (k0 + [0, klen)) mod nz.
+struct Band {
+    int i0, ilen, j0, jlen, k0, klen;
+};
+
+__host__ __device__ inline int pmod(int a, int m) {
+    int r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+__host__ __device__ inline Band band_from_box(const int* b, int nx, int ny, int nz) {
+    Band r;
+    if (b[0] == kBoxEmpty || b[2] == kBoxEmpty || b[4] == kBoxEmpty) {
+        r.i0 = r.j0 = r.k0 = 0;
+        r.ilen = r.jlen = r.klen = 0;
+        return r;
+    }
+    long long imin = b[0], imax = -(long long)b[1];
+    long long jmin = b[2], jmax = -(long long)b[3];
+    long long kmin = b[4], kmax = -(long long)b[5];
+    r.i0 = (int)imin;
+    r.ilen = (int)(imax - imin + 1);
+    long long jl = jmax - jmin + 1, kl = kmax - kmin + 1;
+    if (jl >= ny) { r.j0 = 0; r.jlen = ny; } else { r.j0 = pmod((int)jmin, ny); r.jlen = (int)jl; }
+    if (kl >= nz) { r.k0 = 0; r.klen = nz; } else { r.k0 = pmod((int)kmin, nz); r.klen = (int)kl; }
+    if (r.ilen <= 0 || r.jlen <= 0 || r.klen <= 0) r.ilen = r.jlen = r.klen = 0;
+    return r;
+}
+
+__device__ inline bool in_band(const Band& b, int x, int y, int z, int ny, int nz) {
+    int oy = y - b.j0; if (oy < 0) oy += ny;
+    int oz = z - b.k0; if (oz < 0) oz += nz;
+    return (unsigned)(x - b.i0) < (unsigned)b.ilen && oy < b.jlen && oz < b.klen;
+}
+
+// Peskin 4-point regularised delta, airfoil_moving.py:27-38, same operation order.
+__device__ inline float phi1d(float r) {
+    float s = fabsf(r);
+    float result = 0.0f;
+    if (s < 1.0f) {
+        float a = 1.0f + 4.0f * s - 4.0f * s * s;
+        result = (3.0f - 2.0f * s + sqrtf(fmaxf(a, 0.0f))) / 8.0f;
+    } else if (s < 2.0f) {
+        float a = -7.0f + 12.0f * s - 4.0f * s * s;
+        result = (5.0f - 2.0f * s - sqrtf(fmaxf(a, 0.0f))) / 8.0f;
+    }
+    return result;
+}
+
+// ---------------------------------------------------------------- population storage
+template <int S> struct Pop;
+template <> struct Pop<CLBM_STORE_F32> {
+    using T = float;
+    static __device__ __forceinline__ float ld(const T* p, int q) { (void)q; return __ldg(p); }
+    static __device__ __forceinline__ void st(T* p, int q, float v) { (void)q; __stcs(p, v); }
+};
+template <> struct Pop<CLBM_STORE_F16S> {
+    using T = __half;
+    static __device__ __forceinline__ float ld(const T* p, int q) {
+        return __half2float(__ldg(p)) + wq(q);
+    }
+    static __device__ __forceinline__ void st(T* p, int q, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p),
+               __half_as_ushort(__float2half_rn(v - wq(q))));
+    }
+};
+template <> struct Pop<CLBM_STORE_BF16S> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ float ld(const T* p, int q) {
+        return __bfloat162float(__ldg(p)) + wq(q);
+    }
+    static __device__ __forceinline__ void st(T* p, int q, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p),
+               __bfloat16_as_ushort(__float2bfloat16_rn(v - wq(q))));
+    }
+};
+
+inline size_t store_bytes(int storage) { return storage == CLBM_STORE_F32 ? 4 : 2; }
+
+// ---------------------------------------------------------------- launchers
+// Force source of the fused step.
+enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2 };
+
+struct ForceArgs {
+    const float* fx;       // padded layout
+    const float* fy;
+    const float* fz;       // dense mode only
+    const IbmDev* dev;     // band mode: box of the last compute_force
+};
+
+void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
+void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
+                           const Grid& g, const Coef& c, const ForceArgs& fa, cudaStream_t st);
+// Macro (rho, u without force) of the current state for every cell of the grid; optional
+// statistics into stats[0..3] (ordered-int min rho, max rho, max |u|^2, nonfinite count).
+void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
+                       float* rho, float* ux, float* uy, float* uz,
+                       unsigned long long* stats, cudaStream_t st);
+void launch_fill_macro(const Grid& g, const Coef& c, float* rho, float* ux, float* uy,
+                       float* uz, cudaStream_t st);
+// Padded-layout field -> reference layout (x, y, z), optional clip to +-clipv.
+void launch_export_field(const float* a, float* out, const Grid& g, float clipv,
+                         cudaStream_t st);
+// Reference layout (x, y, z) -> padded layout.
+void launch_import_field(const float* in, float* a, const Grid& g, cudaStream_t st);
+void launch_export_populations(int storage, bool pull, const void* f, float* out,
+                               const Grid& g, const Coef& c, cudaStream_t st);
+void launch_import_populations(int storage, const float* in, void* f, const Grid& g,
+                               cudaStream_t st);
+
+// IBM
+struct IbmArrays {
+    int n;
+    const float *X0, *Y0, *Z0;
+    float *X, *Y, *Z, *VX, *VY, *Uk, *Vk, *FXk, *FYk;
+    float *fx, *fy;   // padded full grid
+    float *ux, *uy;   // padded full grid (macro of the solver)
+    IbmDev* dev;
+    double* hist;
+    int hist_cap;
+    int max_bx, max_by, max_bz;   // upper bound of the band box dimensions
+};
+
+struct MotionF { float xc, yc, theta, vx, vy, omega; };
+
+// Marker kinematics + band box of this call. device_motion: evaluate the motion law of
+// `m` on the device for t = dev->step + 1; otherwise use the float32 values `mf`.
+void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
+                        const MotionF& mf, const clbm_motion& m, cudaStream_t st);
+// Zero the previous call's force band and compute the macro fields on this call's band.
+void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
+                         IbmDev* dev, float* fx, float* fy, float* rho, float* ux, float* uy,
+                         float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
+                         cudaStream_t st);
+void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st);
+// Force sums of this call into the history ring, then advance the device call counter.
+void launch_ibm_finish(const IbmArrays& a, const Grid& g, cudaStream_t st);
+
+}  // namespace clbm

@@ -1,0 +1,215 @@
+// ibm_kernels.cu -- direct-forcing immersed boundary on the GPU.
+//
+// One compute_force call (airfoil_moving.py:230-255) is four launches:
+//   k_ibm_markers        marker kinematics (airfoil_moving.py:100-127) and the box that
+//                        bounds every 4x4x4 Peskin stencil of this call (block min/max,
+//                        one atomicMin per block and entry)
+//   k_band_prepare       (lbm_kernels.cu) zero the previous call's force box
+//                        (_zero_forces, airfoil_moving.py:132-137, restricted to where
+//                        forces can be non-zero) and compute _macro_post velocities of the
+//                        current state inside this call's box
+//   k_ibm_interp_spread  one warp per marker: 64 stencil taps, two per lane, interpolation
+//                        reduced with warp shuffles (airfoil_moving.py:142-170), marker
+//                        force clip (airfoil_moving.py:175-183), spreading with float
+//                        atomics into the Eulerian fields (airfoil_moving.py:188-214)
+//   k_ibm_finish         double sums of the clipped Eulerian force over the box and of the
+//                        marker forces into the history ring (lift/drag), then advance the
+//                        device call counter. The clip itself (_clip_forces,
+//                        airfoil_moving.py:219-225) is applied where the fields are read.
+#include <algorithm>
+
+#include "clbm_internal.cuh"
+
+namespace clbm {
+
+constexpr int kMarkerBlock = 256;
+
+template <bool DEVM>
+__global__ void __launch_bounds__(kMarkerBlock) k_ibm_markers(IbmArrays a, Grid g, MotionF mf,
+                                                              clbm_motion m) {
+    __shared__ int sbox[kMarkerBlock / 32][6];
+    const long long s = a.dev->step + 1;
+    float xc, yc, theta, vx, vy, omega;
+    if (DEVM) {
+        // _motion_state(step), main_moving.py:65-74, in double, then the float32
+        // truncation of the kernel arguments (airfoil_moving.py:101-103).
+        const double t = (double)s, w = m.w;
+        xc = (float)m.x0;
+        yc = (float)(m.y0 + m.a_heave * sin(w * t));
+        theta = (float)(m.aoa0 + m.a_pitch * sin(w * t + m.phi_pitch));
+        vx = 0.0f;
+        vy = (float)(m.a_heave * w * cos(w * t));
+        omega = (float)(m.a_pitch * w * cos(w * t + m.phi_pitch));
+    } else {
+        xc = mf.xc; yc = mf.yc; theta = mf.theta; vx = mf.vx; vy = mf.vy; omega = mf.omega;
+    }
+    const float cos_t = cosf(theta), sin_t = sinf(theta);
+    int b[6] = {kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty};
+    const int i = blockIdx.x * kMarkerBlock + threadIdx.x;
+    if (i < a.n) {
+        const float x0m = a.X0[i], y0m = a.Y0[i], zk = a.Z0[i];
+        const float xk = xc + x0m * cos_t - y0m * sin_t;
+        const float yk = yc + x0m * sin_t + y0m * cos_t;
+        a.X[i] = xk;
+        a.Y[i] = yk;
+        a.Z[i] = zk;
+        const float rx = xk - xc, ry = yk - yc;
+        a.VX[i] = vx - omega * ry;
+        a.VY[i] = vy + omega * rx;
+        const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
+        b[0] = min(max(ib, 0), g.nx - 1);
+        b[1] = -min(max(ib + 3, 0), g.nx - 1);
+        b[2] = jb;
+        b[3] = -(jb + 3);
+        b[4] = kb;
+        b[5] = -(kb + 3);
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) b[e] = __reduce_min_sync(0xffffffffu, b[e]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int e = 0; e < 6; ++e) sbox[warp][e] = b[e];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int v = sbox[0][threadIdx.x];
+        for (int w = 1; w < kMarkerBlock / 32; ++w) v = min(v, sbox[w][threadIdx.x]);
+        if (v != kBoxEmpty) atomicMin(&a.dev->box[s & 1][threadIdx.x], v);
+    }
+}
+
+constexpr int kSpreadBlock = 256;
+
+__global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a, Grid g) {
+    const int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (m >= a.n) return;  // whole warp leaves together
+    const float xk = a.X[m], yk = a.Y[m], zk = a.Z[m];
+    const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
+    float wt[2];
+    long long cell[2];
+    float us = 0.f, vs = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        // tap t: di fastest, so four neighbouring lanes read four consecutive x
+        const int t = lane + 32 * h;
+        const int di = t & 3, dj = (t >> 2) & 3, dk = t >> 4;
+        const int ii = min(max(ib + di, 0), g.nx - 1);   // x clamped (airfoil_moving.py:158)
+        const int jj = pmod(jb + dj, g.ny);              // y, z periodic indices; the weight
+        const int kk = pmod(kb + dk, g.nz);              // uses the wrapped index, as there
+        const float w = phi1d((float)ii - xk) * phi1d((float)jj - yk) * phi1d((float)kk - zk);
+        const long long c = ((long long)kk * g.ny + jj) * g.pitch + ii;
+        wt[h] = w;
+        cell[h] = c;
+        if (w != 0.0f) {
+            us += a.ux[c] * w;
+            vs += a.uy[c] * w;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        us += __shfl_xor_sync(0xffffffffu, us, o);
+        vs += __shfl_xor_sync(0xffffffffu, vs, o);
+    }
+    const float fxk = fmaxf(-0.05f, fminf(0.05f, -(us - a.VX[m])));
+    const float fyk = fmaxf(-0.05f, fminf(0.05f, -(vs - a.VY[m])));
+    if (lane == 0) {
+        a.Uk[m] = us;
+        a.Vk[m] = vs;
+        a.FXk[m] = fxk;
+        a.FYk[m] = fyk;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (wt[h] != 0.0f) {
+            atomicAdd(a.fx + cell[h], fxk * wt[h]);
+            atomicAdd(a.fy + cell[h], fyk * wt[h]);
+        }
+    }
+}
+
+constexpr int kFinishBlock = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g) {
+    __shared__ double red[kFinishBlock / 32][4];
+    __shared__ bool last;
+    IbmDev* dev = a.dev;
+    const long long s = dev->step + 1;
+    const Band b = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
+    const long long cells = (long long)b.ilen * b.jlen * b.klen;
+    const long long stride = (long long)gridDim.x * kFinishBlock;
+    double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;
+    for (long long t = (long long)blockIdx.x * kFinishBlock + threadIdx.x; t < cells; t += stride) {
+        const int ox = (int)(t % b.ilen);
+        const long long r = t / b.ilen;
+        const int oy = (int)(r % b.jlen), oz = (int)(r / b.jlen);
+        const int x = b.i0 + ox, y = pmod(b.j0 + oy, g.ny), z = pmod(b.k0 + oz, g.nz);
+        const long long c = ((long long)z * g.ny + y) * g.pitch + x;
+        sx += (double)fminf(fmaxf(a.fx[c], -0.05f), 0.05f);
+        sy += (double)fminf(fmaxf(a.fy[c], -0.05f), 0.05f);
+    }
+    for (long long t = (long long)blockIdx.x * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
+        mx += (double)a.FXk[t];
+        my += (double)a.FYk[t];
+    }
+    sx = warp_sum(sx); sy = warp_sum(sy); mx = warp_sum(mx); my = warp_sum(my);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[warp][0] = sx; red[warp][1] = sy; red[warp][2] = mx; red[warp][3] = my; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int w = 0; w < kFinishBlock / 32; ++w) v += red[w][threadIdx.x];
+        atomicAdd(&dev->acc[threadIdx.x], v);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int tk = atomicAdd(&dev->ticket, 1u);
+        last = (tk == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double* h = a.hist + 4 * ((s - 1) % a.hist_cap);
+        for (int e = 0; e < 4; ++e) {
+            unsigned long long bits = atomicExch(
+                reinterpret_cast<unsigned long long*>(&dev->acc[e]), 0ull);
+            h[e] = __longlong_as_double((long long)bits);
+        }
+        dev->ticket = 0u;
+        // the previous call's box was consumed by this call's band-prepare
+        for (int e = 0; e < 6; ++e) dev->box[(s + 1) & 1][e] = kBoxEmpty;
+        __threadfence();
+        dev->step = s;
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
+                        const MotionF& mf, const clbm_motion& m, cudaStream_t st) {
+    const int blocks = (a.n + kMarkerBlock - 1) / kMarkerBlock;
+    if (blocks == 0) return;
+    if (device_motion) k_ibm_markers<true><<<blocks, kMarkerBlock, 0, st>>>(a, g, mf, m);
+    else k_ibm_markers<false><<<blocks, kMarkerBlock, 0, st>>>(a, g, mf, m);
+}
+
+void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st) {
+    const long long threads = (long long)a.n * 32;
+    const int blocks = (int)((threads + kSpreadBlock - 1) / kSpreadBlock);
+    if (blocks == 0) return;
+    k_ibm_interp_spread<<<blocks, kSpreadBlock, 0, st>>>(a, g);
+}
+
+void launch_ibm_finish(const IbmArrays& a, const Grid& g, cudaStream_t st) {
+    const long long work = std::max<long long>((long long)a.max_bx * a.max_by * a.max_bz, a.n);
+    int blocks = (int)std::min<long long>((work + kFinishBlock - 1) / kFinishBlock, 304);
+    if (blocks < 1) blocks = 1;
+    k_ibm_finish<<<blocks, kFinishBlock, 0, st>>>(a, g);
+}
+
+}  // namespace clbm

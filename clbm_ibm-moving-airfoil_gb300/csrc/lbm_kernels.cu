@@ -1,0 +1,493 @@
+// lbm_kernels.cu -- fused pull-stream + cascaded central-moment collision for D3Q19.
+//
+// One pass per time step. Each thread owns one cell (x fastest, so a warp covers 32
+// consecutive x of one row) and
+//   1. pulls its 19 post-stream populations from the post-collision state of the
+//      previous step, f(x) = f_post(x - e_q) with y/z periodic wrap (clbm_moving.py:254-261),
+//      the zero-gradient outlet folded in as "cell Nx-1 pulls like cell Nx-2"
+//      (clbm_moving.py:296-300) and the Zou-He velocity inlet applied in registers at
+//      x = 0 (clbm_moving.py:266-294);
+//   2. takes rho and the half-force-shifted velocity (clbm_moving.py:96-115);
+//   3. relaxes the second-order central moments and rebuilds the raw moments with the
+//      reference's fixed choices s_q = s_pi = 1 (clbm_moving.py:170-231);
+//   4. maps raw moments back to populations with the closed form of M_raw^-1 (entries
+//      0, +-1/4, +-1/2, +-1; clbm_moving.py:233-238) and adds Guo forcing
+//      (clbm_moving.py:240-249) where the force is non-zero;
+//   5. stores f_post for the next step, coalesced and with streaming stores.
+// Algorithmic traffic: 19 loads + 19 stores per cell (152 B/cell float32, 76 B/cell for
+// the 16-bit shifted forms); the force fields add 8 B per cell inside the IBM band only.
+#include "clbm_internal.cuh"
+
+namespace clbm {
+
+// Gather the post-stream, post-boundary populations S(x, y, z) of the stored state.
+// pull = false: the stored array already is a post-stream state (after initialisation or
+// an import), read in place.
+template <int S, bool PULL>
+__device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f, const Grid& g,
+                                       const Coef& c, int x, int y, int z, float (&v)[19]) {
+    using P = Pop<S>;
+    if (!PULL) {
+        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) v[q] = P::ld(f + q * g.plane + cell, q);
+        return;
+    }
+    const int xe = (x == g.nx - 1) ? g.nx - 2 : x;  // outlet: copy of column Nx-2
+    const int ym = (y == 0) ? g.ny - 1 : y - 1;
+    const int yp = (y == g.ny - 1) ? 0 : y + 1;
+    const int zm = (z == 0) ? g.nz - 1 : z - 1;
+    const int zp = (z == g.nz - 1) ? 0 : z + 1;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+        const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+        const int sx = xe - ex(q);
+        if (ex(q) == 1 && xe == 0) {
+            v[q] = 0.0f;  // inlet unknown, rebuilt by Zou-He below
+        } else {
+            v[q] = P::ld(f + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + sx, q);
+        }
+    }
+    if (xe == 0) {
+        // 3D Zou-He velocity inlet, clbm_moving.py:266-294 (same operation order)
+        const float ux_in = c.ux_in, uy_in = c.uy_in;
+        float S_known = v[0] + v[3] + v[4] + v[5] + v[6] + v[15] + v[16] + v[17] + v[18];
+        float S_out = v[2] + v[8] + v[10] + v[12] + v[14];
+        float rho_in = (S_known + 2.0f * S_out) / (1.0f - ux_in);
+        float diff_y = v[3] - v[4];
+        float diff_z = v[5] - v[6];
+        v[1] = v[2] + c.c23 * rho_in * ux_in;
+        v[7] = v[10] + c.c16 * rho_in * ux_in + 0.5f * rho_in * uy_in - 0.5f * diff_y;
+        v[9] = v[8] + c.c16 * rho_in * ux_in - 0.5f * rho_in * uy_in + 0.5f * diff_y;
+        v[11] = v[14] + c.c16 * rho_in * ux_in - 0.5f * diff_z;
+        v[13] = v[12] + c.c16 * rho_in * ux_in + 0.5f * diff_z;
+    }
+}
+
+// Zeroth, first and second raw moments of a population vector.
+struct Moments {
+    float rho, mx, my, mz, pxx, pyy, pzz, pxy, pxz, pyz;
+};
+
+__device__ __forceinline__ Moments moments(const float (&f)[19]) {
+    Moments m;
+    const float sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+    const float a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
+    const float e = f[15] + f[16], h = f[17] + f[18];
+    m.rho = f[0] + (sx + sy + sz) + (a + b) + (cc + d) + (e + h);
+    m.mx = (f[1] - f[2]) + (f[7] - f[8]) + (f[9] - f[10]) + (f[11] - f[12]) + (f[13] - f[14]);
+    m.my = (f[3] - f[4]) + (a - b) + (f[15] - f[16]) + (f[17] - f[18]);
+    m.mz = (f[5] - f[6]) + (cc - d) + (e - h);
+    m.pxx = sx + (a + b) + (cc + d);
+    m.pyy = sy + (a + b) + (e + h);
+    m.pzz = sz + (cc + d) + (e + h);
+    m.pxy = (f[7] + f[10]) - (f[8] + f[9]);
+    m.pxz = (f[11] + f[14]) - (f[12] + f[13]);
+    m.pyz = (f[15] + f[18]) - (f[16] + f[17]);
+    return m;
+}
+
+// Cascaded collision in central-moment space followed by the raw-moment back transform,
+// in place on f. (Fx, Fy, Fz) is the body-force density at the cell.
+template <bool FORCE>
+__device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx, float Fy,
+                                        float Fz) {
+    const Moments m = moments(f);
+    const float r = m.rho;
+    const float inv = 1.0f / r;
+    float u = m.mx * inv, v = m.my * inv, w = m.mz * inv;
+    if (FORCE) {
+        u += 0.5f * Fx * inv;
+        v += 0.5f * Fy * inv;
+        w += 0.5f * Fz * inv;
+    }
+    // second-order central moments about the shifted velocity
+    const float k200 = m.pxx - 2.0f * u * m.mx + u * u * r;
+    const float k020 = m.pyy - 2.0f * v * m.my + v * v * r;
+    const float k002 = m.pzz - 2.0f * w * m.mz + w * w * r;
+    const float k110 = m.pxy - u * m.my - v * m.mx + u * v * r;
+    const float k101 = m.pxz - u * m.mz - w * m.mx + u * w * r;
+    const float k011 = m.pyz - v * m.mz - w * m.my + v * w * r;
+    // relaxation (clbm_moving.py:170-196)
+    const float k110s = k110 * c.one_m_sv, k101s = k101 * c.one_m_sv, k011s = k011 * c.one_m_sv;
+    const float kA = k200 + k020 + k002;
+    const float kAs = kA - c.s_e * (kA - r);
+    const float kDs = (k200 - k020) * c.one_m_sv, kEs = (k200 - k002) * c.one_m_sv;
+    const float k200s = (kAs + kDs + kEs) * (1.0f / 3.0f);
+    const float k020s = (kAs - 2.0f * kDs + kEs) * (1.0f / 3.0f);
+    const float k002s = (kAs + kDs - 2.0f * kEs) * (1.0f / 3.0f);
+    const float r9 = r * (1.0f / 9.0f);
+    // raw post-collision moments (third-order central moments relax to 0, fourth to r/9)
+    const float ur = u * r, vr = v * r, wr = w * r;
+    const float uu = u * u, vv = v * v, ww = w * w;
+    const float T110 = k110s + u * vr, T101 = k101s + u * wr, T011 = k011s + v * wr;
+    const float T200 = k200s + u * ur, T020 = k020s + v * vr, T002 = k002s + w * wr;
+    const float T210 = 2.0f * u * k110s + v * k200s + uu * vr;
+    const float T120 = 2.0f * v * k110s + u * k020s + vv * ur;
+    const float T201 = 2.0f * u * k101s + w * k200s + uu * wr;
+    const float T021 = 2.0f * v * k011s + w * k020s + vv * wr;
+    const float T102 = 2.0f * w * k101s + u * k002s + ww * ur;
+    const float T012 = 2.0f * w * k011s + v * k002s + ww * vr;
+    const float T220 = r9 + 4.0f * u * v * k110s + vv * k200s + uu * k020s + uu * vv * r;
+    const float T202 = r9 + 4.0f * u * w * k101s + ww * k200s + uu * k002s + uu * ww * r;
+    const float T022 = r9 + 4.0f * v * w * k011s + ww * k020s + vv * k002s + vv * ww * r;
+    // closed form of M_raw^-1 (config_moving.py:62-73)
+    f[0] = r - (T200 + T020 + T002) + (T220 + T202 + T022);
+    const float A1 = 0.5f * (T200 - T220 - T202), B1 = 0.5f * (ur - T120 - T102);
+    const float A2 = 0.5f * (T020 - T220 - T022), B2 = 0.5f * (vr - T210 - T012);
+    const float A3 = 0.5f * (T002 - T202 - T022), B3 = 0.5f * (wr - T201 - T021);
+    f[1] = A1 + B1; f[2] = A1 - B1;
+    f[3] = A2 + B2; f[4] = A2 - B2;
+    f[5] = A3 + B3; f[6] = A3 - B3;
+    // plane diagonals: f = (T_aabb + e_a e_b T_ab + e_b T_aab + e_a T_abb) / 4
+    {
+        const float s = 0.25f * T220, p = 0.25f * T110, a = 0.25f * T210, b = 0.25f * T120;
+        f[7] = s + p + a + b;   // (+1,+1)
+        f[8] = s - p + a - b;   // (-1,+1)
+        f[9] = s - p - a + b;   // (+1,-1)
+        f[10] = s + p - a - b;  // (-1,-1)
+    }
+    {
+        const float s = 0.25f * T202, p = 0.25f * T101, a = 0.25f * T201, b = 0.25f * T102;
+        f[11] = s + p + a + b;
+        f[12] = s - p + a - b;
+        f[13] = s - p - a + b;
+        f[14] = s + p - a - b;
+    }
+    {
+        const float s = 0.25f * T022, p = 0.25f * T011, a = 0.25f * T021, b = 0.25f * T012;
+        f[15] = s + p + a + b;
+        f[16] = s - p + a - b;
+        f[17] = s - p - a + b;
+        f[18] = s + p - a - b;
+    }
+    if (FORCE) {
+        // Guo forcing: w_q (1 - s_v/2) [ (e - u)/cs2 + (e.u) e / cs2^2 ] . F
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const float eu = ex(q) * u + ey(q) * v + ez(q) * w;
+            const float cx = (ex(q) - u) * 3.0f + eu * ex(q) * 9.0f;
+            const float cy = (ey(q) - v) * 3.0f + eu * ey(q) * 9.0f;
+            const float cz = (ez(q) - w) * 3.0f + eu * ez(q) * 9.0f;
+            f[q] += c.wc[q] * (cx * Fx + cy * Fy + cz * Fz);
+        }
+    }
+}
+
+constexpr int kBX = 128;  // threads per block along x
+
+template <int S, bool PULL, int FMODE>
+__global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T* __restrict__ fin,
+                                                        typename Pop<S>::T* __restrict__ fout,
+                                                        Grid g, Coef c, ForceArgs fa) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    float f[19];
+    gather<S, PULL>(fin, g, c, x, y, z, f);
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    if (FMODE == kForceNone) {
+        collide<false>(f, c, 0.f, 0.f, 0.f);
+    } else if (FMODE == kForceDense) {
+        const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
+        collide<true>(f, c, fa.fx[cell], fa.fy[cell], Fz);
+    } else {
+        const long long step = fa.dev->step;
+        const Band b = band_from_box(fa.dev->box[step & 1], g.nx, g.ny, g.nz);
+        if (in_band(b, x, y, z, g.ny, g.nz)) {
+            // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
+            // fz is always zero there.
+            const float Fx = fminf(fmaxf(fa.fx[cell], -0.05f), 0.05f);
+            const float Fy = fminf(fmaxf(fa.fy[cell], -0.05f), 0.05f);
+            collide<true>(f, c, Fx, Fy, 0.0f);
+        } else {
+            collide<false>(f, c, 0.f, 0.f, 0.f);
+        }
+    }
+    using P = Pop<S>;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) P::st(fout + q * g.plane + cell, q, f[q]);
+}
+
+template <int S>
+__global__ void k_init(typename Pop<S>::T* __restrict__ f, Grid g, Coef c) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    // _init_feq, clbm_moving.py:75-91 (same operation order)
+    const float ux0 = c.ux_in, uy0 = c.uy_in;
+    const float cs2 = 1.0f / 3.0f, cs4 = (float)((1.0 / 3.0) * (1.0 / 3.0));
+    const float u2 = ux0 * ux0 + uy0 * uy0;
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const float eu = (float)ex(q) * ux0 + (float)ey(q) * uy0;
+        const float v = wq(q) * (1.0f + eu / cs2 + 0.5f * eu * eu / cs4 - 0.5f * u2 / cs2);
+        Pop<S>::st(f + q * g.plane + cell, q, v);
+    }
+}
+
+__device__ __forceinline__ unsigned int ordered(float v) {
+    unsigned int u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// _macro_post (clbm_moving.py:305-321) over the whole grid, plus divergence statistics.
+template <int S, bool PULL>
+__global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
+                             float* rho, float* ux, float* uy, float* uz,
+                             unsigned long long* stats) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    unsigned int rmin = 0xffffffffu, rmax = 0u, u2max = 0u;
+    unsigned int bad = 0;
+    if (x < g.nx) {
+        float f[19];
+        gather<S, PULL>(fin, g, c, x, y, z, f);
+        float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            r += f[q];
+            mx += (float)ex(q) * f[q];
+            my += (float)ey(q) * f[q];
+            mz += (float)ez(q) * f[q];
+        }
+        const float u = mx / r, v = my / r, w = mz / r;
+        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        rho[cell] = r;
+        ux[cell] = u;
+        uy[cell] = v;
+        uz[cell] = w;
+        if (stats) {
+            const float u2 = u * u + v * v + w * w;
+            if (!isfinite(r) || !isfinite(u2)) {
+                bad = 1;
+            } else {
+                rmin = rmax = ordered(r);
+                u2max = ordered(u2);
+            }
+        }
+    }
+    if (!stats) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+        rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        u2max = max(u2max, __shfl_xor_sync(0xffffffffu, u2max, o));
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (rmin != 0xffffffffu) {
+            atomicMin(stats + 0, (unsigned long long)rmin);
+            atomicMax(stats + 1, (unsigned long long)rmax);
+            atomicMax(stats + 2, (unsigned long long)u2max);
+        }
+        if (bad) atomicAdd(stats + 3, (unsigned long long)bad);
+    }
+}
+
+// Tiled transpose between the padded (z, y, x) layout and the reference (x, y, z) layout.
+constexpr int kT = 32;
+
+__global__ void k_export_field(const float* __restrict__ a, float* __restrict__ out, Grid g,
+                               float clipv) {
+    __shared__ float tile[kT][kT + 1];
+    const int x0 = blockIdx.x * kT, z0 = blockIdx.z * kT, y = blockIdx.y;
+    for (int r = threadIdx.y; r < kT; r += blockDim.y) {
+        const int z = z0 + r, x = x0 + threadIdx.x;
+        float v = 0.f;
+        if (z < g.nz && x < g.nx) v = a[((long long)z * g.ny + y) * g.pitch + x];
+        if (clipv > 0.f) v = fminf(fmaxf(v, -clipv), clipv);
+        tile[r][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < kT; r += blockDim.y) {
+        const int x = x0 + r, z = z0 + threadIdx.x;
+        if (x < g.nx && z < g.nz) out[((long long)x * g.ny + y) * g.nz + z] = tile[threadIdx.x][r];
+    }
+}
+
+__global__ void k_import_field(const float* __restrict__ in, float* __restrict__ a, Grid g) {
+    __shared__ float tile[kT][kT + 1];
+    const int x0 = blockIdx.x * kT, z0 = blockIdx.z * kT, y = blockIdx.y;
+    for (int r = threadIdx.y; r < kT; r += blockDim.y) {
+        const int x = x0 + r, z = z0 + threadIdx.x;
+        float v = 0.f;
+        if (x < g.nx && z < g.nz) v = in[((long long)x * g.ny + y) * g.nz + z];
+        tile[threadIdx.x][r] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < kT; r += blockDim.y) {
+        const int z = z0 + r, x = x0 + threadIdx.x;
+        if (z < g.nz && x < g.nx) a[((long long)z * g.ny + y) * g.pitch + x] = tile[r][threadIdx.x];
+    }
+}
+
+template <int S, bool PULL>
+__global__ void k_export_populations(const typename Pop<S>::T* __restrict__ fin, float* out,
+                                     Grid g, Coef c) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    float f[19];
+    gather<S, PULL>(fin, g, c, x, y, z, f);
+    float* o = out + (((long long)x * g.ny + y) * g.nz + z) * 19;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) o[q] = f[q];
+}
+
+template <int S>
+__global__ void k_import_populations(const float* __restrict__ in, typename Pop<S>::T* f,
+                                     Grid g) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const float* i = in + (((long long)x * g.ny + y) * g.nz + z) * 19;
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Pop<S>::st(f + q * g.plane + cell, q, i[q]);
+}
+
+// rho = 1, u = (ux_in, uy_in, 0): the macro fields _init_feq sets (clbm_moving.py:88-91)
+__global__ void k_fill_macro(Grid g, Coef c, float* rho, float* ux, float* uy, float* uz) {
+    const int x = blockIdx.x * kBX + threadIdx.x;
+    if (x >= g.nx) return;
+    const long long cell = ((long long)blockIdx.z * g.ny + blockIdx.y) * g.pitch + x;
+    rho[cell] = 1.0f;
+    ux[cell] = c.ux_in;
+    uy[cell] = c.uy_in;
+    uz[cell] = 0.0f;
+}
+
+// ---------------------------------------------------------------- launchers
+static dim3 cell_grid(const Grid& g) { return dim3((g.nx + kBX - 1) / kBX, g.ny, g.nz); }
+
+#define CLBM_DISPATCH_STORE(storage, ...)                                                  \
+    switch (storage) {                                                                     \
+        case CLBM_STORE_F32: { constexpr int S_ = CLBM_STORE_F32; __VA_ARGS__; } break;   \
+        case CLBM_STORE_F16S: { constexpr int S_ = CLBM_STORE_F16S; __VA_ARGS__; } break; \
+        default: { constexpr int S_ = CLBM_STORE_BF16S; __VA_ARGS__; } break;             \
+    }
+
+void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st) {
+    CLBM_DISPATCH_STORE(storage, (k_init<S_><<<cell_grid(g), kBX, 0, st>>>(
+                                     (typename Pop<S_>::T*)f, g, c)));
+}
+
+template <int S, bool PULL>
+static void sc_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                      const ForceArgs& fa, cudaStream_t st) {
+    using T = typename Pop<S>::T;
+    if (fmode == kForceNone)
+        k_stream_collide<S, PULL, kForceNone><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceBand)
+        k_stream_collide<S, PULL, kForceBand><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else
+        k_stream_collide<S, PULL, kForceDense><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+}
+
+void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
+                           const Grid& g, const Coef& c, const ForceArgs& fa, cudaStream_t st) {
+    CLBM_DISPATCH_STORE(storage, {
+        if (pull) sc_launch<S_, true>(fmode, fin, fout, g, c, fa, st);
+        else sc_launch<S_, false>(fmode, fin, fout, g, c, fa, st);
+    });
+}
+
+void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
+                       float* rho, float* ux, float* uy, float* uz,
+                       unsigned long long* stats, cudaStream_t st) {
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        if (pull) k_macro_full<S_, true><<<cell_grid(g), kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
+        else k_macro_full<S_, false><<<cell_grid(g), kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
+    });
+}
+
+void launch_fill_macro(const Grid& g, const Coef& c, float* rho, float* ux, float* uy,
+                       float* uz, cudaStream_t st) {
+    k_fill_macro<<<cell_grid(g), kBX, 0, st>>>(g, c, rho, ux, uy, uz);
+}
+
+void launch_export_field(const float* a, float* out, const Grid& g, float clipv,
+                         cudaStream_t st) {
+    dim3 grid((g.nx + kT - 1) / kT, g.ny, (g.nz + kT - 1) / kT);
+    k_export_field<<<grid, dim3(kT, 8), 0, st>>>(a, out, g, clipv);
+}
+
+void launch_import_field(const float* in, float* a, const Grid& g, cudaStream_t st) {
+    dim3 grid((g.nx + kT - 1) / kT, g.ny, (g.nz + kT - 1) / kT);
+    k_import_field<<<grid, dim3(kT, 8), 0, st>>>(in, a, g);
+}
+
+void launch_export_populations(int storage, bool pull, const void* f, float* out,
+                               const Grid& g, const Coef& c, cudaStream_t st) {
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        if (pull) k_export_populations<S_, true><<<cell_grid(g), kBX, 0, st>>>((const T*)f, out, g, c);
+        else k_export_populations<S_, false><<<cell_grid(g), kBX, 0, st>>>((const T*)f, out, g, c);
+    });
+}
+
+void launch_import_populations(int storage, const float* in, void* f, const Grid& g,
+                               cudaStream_t st) {
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        k_import_populations<S_><<<cell_grid(g), kBX, 0, st>>>(in, (T*)f, g);
+    });
+}
+
+// Band-prepare needs the same gather; the IBM translation unit calls this launcher.
+template <int S, bool PULL>
+__global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
+                               IbmDev* dev, float* fx, float* fy, float* rho, float* ux,
+                               float* uy, float* uz, bool compute_macro) {
+    // Box of this compute_force call (slot s & 1) and of the previous one (slot (s-1) & 1).
+    const long long s = dev->step + 1;
+    const Band nb = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
+    const Band ob = band_from_box(dev->box[(s - 1) & 1], g.nx, g.ny, g.nz);
+    const int ox = blockIdx.x * blockDim.x + threadIdx.x;
+    const int oy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int oz = blockIdx.z;
+    // _zero_forces (airfoil_moving.py:132-137) restricted to where the previous call spread
+    if (ox < ob.ilen && oy < ob.jlen && oz < ob.klen) {
+        const int x = ob.i0 + ox, y = pmod(ob.j0 + oy, g.ny), z = pmod(ob.k0 + oz, g.nz);
+        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        fx[cell] = 0.f;
+        fy[cell] = 0.f;
+    }
+    // _macro_post of the current state on the cells the stencils of this call touch
+    if (compute_macro && ox < nb.ilen && oy < nb.jlen && oz < nb.klen) {
+        const int x = nb.i0 + ox, y = pmod(nb.j0 + oy, g.ny), z = pmod(nb.k0 + oz, g.nz);
+        float f[19];
+        gather<S, PULL>(fin, g, c, x, y, z, f);
+        float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            r += f[q];
+            mx += (float)ex(q) * f[q];
+            my += (float)ey(q) * f[q];
+            mz += (float)ez(q) * f[q];
+        }
+        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        rho[cell] = r;
+        ux[cell] = mx / r;
+        uy[cell] = my / r;
+        uz[cell] = mz / r;
+    }
+}
+
+void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
+                         IbmDev* dev, float* fx, float* fy, float* rho, float* ux, float* uy,
+                         float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
+                         cudaStream_t st) {
+    dim3 block(32, 4, 1);
+    dim3 grid((max_bx + 31) / 32, (max_by + 3) / 4, max_bz);
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        if (pull) k_band_prepare<S_, true><<<grid, block, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+        else k_band_prepare<S_, false><<<grid, block, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+    });
+}
+
+}  // namespace clbm

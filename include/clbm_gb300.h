@@ -1,0 +1,155 @@
+/*
+ * clbm_gb300.h -- C ABI of the GB300 (sm_103a) D3Q19 cascaded-LBM + immersed-boundary step.
+ *
+ * The library replaces the device side of two reference objects:
+ *   CLBMSolver      clbm_moving.py:41-343    (fluid state, step, rho/ux/uy/uz fields)
+ *   DroneMovingIBM  airfoil_moving.py:44-255 (markers, compute_force, fx/fy/fz fields)
+ * Plain pointers and sizes only. Every call returns CLBM_OK (0) or a CLBM_ERR_* code; the
+ * message of the last failure on the calling thread is clbm_last_error(). All work is
+ * queued on the solver's own CUDA stream; calls that hand results to host memory
+ * synchronise that stream. Host arrays use the reference layout: (Nx, Ny, Nz) C order,
+ * z fastest, and (Nx, Ny, Nz, 19) for populations.
+ */
+#ifndef CLBM_GB300_H
+#define CLBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLBM_OK 0
+#define CLBM_ERR_CUDA 1     /* a CUDA runtime call failed */
+#define CLBM_ERR_ARG 2      /* invalid argument or configuration */
+#define CLBM_ERR_DIVERGED 3 /* non-finite or rho < threshold found by clbm_check */
+#define CLBM_ERR_STATE 4    /* call not valid in the current state */
+
+/* Population storage forms. F32 stores f_q; the shifted forms store f_q - w_q. */
+#define CLBM_STORE_F32 0
+#define CLBM_STORE_F16S 1
+#define CLBM_STORE_BF16S 2
+
+typedef struct clbm_solver clbm_solver;
+typedef struct clbm_ibm clbm_ibm;
+
+/* Lattice and collision parameters (config_moving.py:28-43, clbm_moving.py:32-35). */
+typedef struct clbm_config {
+    int32_t nx, ny, nz;     /* lattice, nx >= 3 */
+    double s_v;             /* shear rate 1/tau */
+    double s_e;             /* trace (bulk) rate; the reference fixes s_q = s_pi = 1 */
+    double ux_in, uy_in;    /* Zou-He inlet velocity; also the initial equilibrium */
+    int32_t storage;        /* CLBM_STORE_* */
+    int32_t device;         /* CUDA device ordinal the solver lives on */
+} clbm_config;
+
+/* Prescribed motion (main_moving.py:62-74; config_moving.py:312-318), double precision:
+ * xc = x0, yc = y0 + a_heave sin(w t), theta = aoa0 + a_pitch sin(w t + phi_pitch),
+ * vx = 0, vy = a_heave w cos(w t), omega = a_pitch w cos(w t + phi_pitch). */
+typedef struct clbm_motion {
+    double x0, y0, a_heave, a_pitch, phi_pitch, aoa0, w;
+} clbm_motion;
+
+/* CLBMSolver.__init__ + _init_feq (clbm_moving.py:54-91): allocate the state and set
+ * f = feq(rho = 1, u = (ux_in, uy_in, 0)). */
+int clbm_create(const clbm_config* cfg, clbm_solver** out);
+int clbm_destroy(clbm_solver* s);
+
+/* CLBMSolver.step(fx, fy, fz) (clbm_moving.py:326-343) with the force fields that the
+ * last ibm_compute_force on `ibm` produced (DroneMovingIBM.fx/fy/fz after _clip_forces).
+ * ibm == NULL steps with zero force. */
+int clbm_step(clbm_solver* s, const clbm_ibm* ibm);
+
+/* CLBMSolver.step with caller-supplied force density fields in device memory, reference
+ * layout (Nx, Ny, Nz) float32, used as given (no clip), fz may be NULL. */
+int clbm_step_dense_force(clbm_solver* s, const float* fx_dev, const float* fy_dev,
+                          const float* fz_dev);
+
+/* Same as clbm_step_dense_force with the three fields in host memory (fz may be NULL);
+ * the copies to the device are part of the call. */
+int clbm_step_host_force(clbm_solver* s, const float* fx, const float* fy, const float* fz);
+
+/* lbm.rho/ux/uy/uz.to_numpy() (main_moving.py:125-128): macroscopic fields of the
+ * current post-stream state without force correction (_macro_post,
+ * clbm_moving.py:305-321) copied to host arrays (any may be NULL). */
+int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz);
+
+/* lbm.f.to_numpy(): post-stream, post-boundary populations (Nx, Ny, Nz, 19) float32. */
+int clbm_read_populations(clbm_solver* s, float* f_host);
+/* lbm.f.from_numpy(): replace the state by host populations (Nx, Ny, Nz, 19). */
+int clbm_write_populations(clbm_solver* s, const float* f_host);
+
+/* Divergence statistics of the current state (main_moving.py:130-145): rho min/max,
+ * max |u| and the count of non-finite rho/u values. Returns CLBM_ERR_DIVERGED when
+ * nonfinite > 0 or rho_min < rho_floor. */
+int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_max,
+               double* u_max, int64_t* nonfinite);
+
+/* DroneMovingIBM.__init__ (airfoil_moving.py:64-95): marker template, X0/Y0 in the body
+ * frame, Z0 absolute; n >= 0. The IBM is bound to one solver's lattice and stream. */
+int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0, int32_t n,
+               clbm_ibm** out);
+int ibm_destroy(clbm_ibm* ibm);
+
+/* DroneMovingIBM.compute_force(lbm.ux, lbm.uy, xc, yc, theta, vx, vy, omega)
+ * (airfoil_moving.py:230-255): marker kinematics, Peskin 4-point interpolation of the
+ * solver's current velocity, marker force clip, spreading and Eulerian clip. The six
+ * motion values are truncated to float32 as the reference's kernel arguments are. */
+int ibm_compute_force(clbm_ibm* ibm, double xc, double yc, double theta, double vx,
+                      double vy, double omega);
+
+/* Same as ibm_compute_force with the motion state of main_moving.py:_motion_state(t)
+ * evaluated on the device in double for t = (number of compute_force calls so far) + 1. */
+int ibm_compute_force_motion(clbm_ibm* ibm, const clbm_motion* m);
+
+/* ibm.fx/fy/fz.to_numpy(): the clipped Eulerian force fields (Nx, Ny, Nz) (any NULL). */
+int ibm_read_forces(const clbm_ibm* ibm, float* fx, float* fy, float* fz);
+
+/* Marker arrays of the last compute_force: X, Y, Z, VX_body, VY_body, U_k, V_k, FX_k,
+ * FY_k, each n floats, concatenated in that order into out[9 * n]. */
+int ibm_read_markers(const clbm_ibm* ibm, float* out);
+
+/* Lift/drag support (not in the reference): per compute_force call, double sums of the
+ * clipped Eulerian force over all cells (sx, sy) and of the marker forces (mx, my).
+ * Reads the last `count` entries (oldest first) of the device history ring into
+ * out[4 * count]; the force on the body is minus these sums. */
+int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out);
+/* Number of compute_force calls made on this IBM (the device step counter). */
+int ibm_step_count(const clbm_ibm* ibm, int64_t* out);
+
+/* The driver loop of main_moving.py:116-122 for nsteps steps: per step
+ * ibm_compute_force_motion then clbm_step, captured once into a CUDA graph and replayed
+ * when use_graph != 0. ibm may be NULL (zero force). */
+int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps,
+             int32_t use_graph);
+
+/* Wait for all queued work of the solver. */
+int clbm_synchronize(clbm_solver* s);
+
+/* The solver's CUDA stream (cudaStream_t), for callers that record events or order their
+ * own work against the solver. The stream stays owned by the solver. */
+int clbm_stream(const clbm_solver* s, void** out);
+
+/* Kernel timing for roofline reporting: while enabled, each fused stream-collide launch is
+ * bracketed by CUDA events on the solver stream. clbm_profile_read synchronises and
+ * returns the summed device time (ms) and launch count of the fused kernel since the last
+ * enable, and the total number of kernels this solver launched since creation. */
+int clbm_profile_enable(clbm_solver* s, int32_t on);
+int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
+                      int64_t* total_launches);
+
+/* Bytes of device memory owned by the solver (populations, macro fields). */
+int clbm_device_bytes(const clbm_solver* s, int64_t* out);
+
+/* Page-locked host buffers for fast transfers. */
+int clbm_host_alloc(int64_t bytes, void** out);
+int clbm_host_free(void* p);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* clbm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLBM_GB300_H */

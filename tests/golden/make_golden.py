@@ -164,11 +164,44 @@ def run_case(ref_dir, name, p):
     return out
 
 
+def _sha(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_geometry(ref_dir):
+    """Marker geometry and M_raw^-1 of the reference's own config module (the airplane of
+    config_moving.py:196-307 and the section builders it uses)."""
+    cfg = _load("_reference_config_moving", os.path.join(ref_dir, "config_moving.py"))
+    out = {
+        "airplane_n": cfg.N_MARKERS,
+        "airplane_sha": _sha(cfg.X_marker_np, cfg.Y_marker_np, cfg.Z_marker_np),
+        "airplane_sample": np.stack([cfg.X_marker_np[::97], cfg.Y_marker_np[::97],
+                                     cfg.Z_marker_np[::97]]),
+        "M_raw_inv": cfg.M_raw_inv_np,
+        "interior_80_07_sha": _sha(*cfg._naca0012_interior(80, 0.7)),
+        "ellipsoid_sha": _sha(*cfg._ellipsoid_markers(75.0, 10.0, 10.0, 0.7)),
+        "wing_layers": cfg.Nz_layers, "wing_2d": cfg.N_MARKERS_2D,
+    }
+    for chord, ds in ((32, 1.0), (80, 1.0), (160, 1.0), (80, 0.7), (8, 0.7)):
+        X, Y = cfg._naca0012_2d(chord, ds)
+        out[f"naca_{chord}_{str(ds).replace('.', '')}"] = np.stack([X, Y])
+    return out
+
+
 def main(argv):
     ref_dir = argv[1] if len(argv) > 1 else "/root/reference"
     sys.dont_write_bytecode = True
     sys.path.insert(0, HERE)
-    names = argv[2:] or sorted(CASES)
+    names = argv[2:] or sorted(CASES) + ["geometry"]
+    if "geometry" in names:
+        names = [n for n in names if n != "geometry"]
+        path = os.path.join(HERE, "golden_geometry.npz")
+        np.savez_compressed(path, **make_geometry(ref_dir))
+        print(f"wrote {path} ({os.path.getsize(path)} bytes)")
     for name in names:
         out = run_case(ref_dir, name, CASES[name])
         path = os.path.join(HERE, f"golden_{name}.npz")

@@ -1,0 +1,53 @@
+"""The C ABI library builds for sm_103a, loads, exports every entry point declared in
+include/clbm_gb300.h, and fails loudly (no CPU fallback) when no GPU is present."""
+
+import ctypes
+import os
+import re
+
+import pytest
+import torch
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "clbm_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_declares_the_binding_surface(pkg):
+    declared = _declared()
+    assert len(declared) >= 20
+    assert sorted(pkg.EXPORTED) == declared
+
+
+def test_library_exports_every_declared_symbol(built_pkg):
+    L = ctypes.CDLL(built_pkg.lib_path())
+    missing = [name for name in _declared() if not hasattr(L, name)]
+    assert not missing
+
+
+def test_library_is_built_for_sm103a(built_pkg):
+    path = built_pkg.lib_path()
+    data = open(path, "rb").read()
+    assert b"sm_103a" in data or b"sm_103" in data
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")
+def test_no_gpu_is_an_error_not_a_fallback(built_pkg):
+    with pytest.raises(built_pkg.CLBMError) as ei:
+        built_pkg.Solver(16, 8, 4, 1.5)
+    assert ei.value.code == 1
+
+
+def test_invalid_configuration_is_rejected(built_pkg):
+    with pytest.raises(built_pkg.CLBMError) as ei:
+        built_pkg.Solver(2, 8, 4, 1.5)
+    assert ei.value.code == 2
+    with pytest.raises(built_pkg.CLBMError) as ei:
+        built_pkg.Solver(16, 8, 4, 2.5)
+    assert ei.value.code == 2
+    with pytest.raises(ValueError):
+        built_pkg.Solver(16, 8, 4, 1.5, storage="fp8")

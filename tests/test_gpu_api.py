@@ -1,0 +1,123 @@
+"""C ABI behaviour on the GPU: state transfer, caller-supplied forces, divergence
+detection, empty marker sets, profiling counters and the 16-bit storage forms."""
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpkg(built_pkg):
+    return built_pkg
+
+
+def _random_state(shape, seed=0):
+    rng = np.random.default_rng(seed)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, np.float32)
+    return (w * (1.0 + 0.05 * rng.standard_normal(shape + (19,)))).astype(np.float32)
+
+
+def test_population_round_trip_is_exact(gpkg):
+    s = gpkg.Solver(37, 11, 5, 1.6)
+    f = _random_state(s.shape)
+    s.write_populations(f)
+    np.testing.assert_array_equal(s.read_populations(), f)
+    s.close()
+
+
+def test_steps_from_imported_state_match_oracle(gpkg, oracle_mod):
+    shape = (40, 12, 6)
+    f = _random_state(shape, seed=3)
+    s = gpkg.Solver(*shape, 1.55, 1.1, 0.04, -0.006)
+    o = oracle_mod.Oracle(*shape, 1.55, 1.1, 0.04, -0.006, [], [], [])
+    s.write_populations(f)
+    o.set_f(f)
+    for _ in range(7):
+        s.step()
+        o.lbm_step()
+    assert rel_l2(s.read_populations(), o.f()) < 1e-6
+
+
+def test_host_forces_match_oracle(gpkg, oracle_mod):
+    shape = (30, 10, 4)
+    rng = np.random.default_rng(7)
+    F = [(1e-3 * rng.standard_normal(shape)).astype(np.float32) for _ in range(3)]
+    s = gpkg.Solver(*shape, 1.3, 1.0, 0.05, 0.0)
+    o = oracle_mod.Oracle(*shape, 1.3, 1.0, 0.05, 0.0, [], [], [])
+    o.set_forces(*F)
+    for _ in range(3):
+        s.step_host_force(*F)
+        o.lbm_step()
+    m = s.read_macro()
+    rho, ux, uy, uz = o.macro()
+    assert rel_l2(m["rho"], rho) < 1e-6
+    assert rel_l2(m["ux"], ux) < 1e-5 and rel_l2(m["uy"], uy) < 1e-4 and rel_l2(m["uz"], uz) < 1e-4
+
+
+def test_divergence_is_reported(gpkg):
+    s = gpkg.Solver(20, 8, 4, 1.5)
+    st = s.check()
+    assert st["nonfinite"] == 0 and abs(st["rho_min"] - 1.0) < 1e-6
+    f = s.read_populations()
+    f[3, 2, 1, 5] = np.nan
+    s.write_populations(f)
+    with pytest.raises(gpkg.DivergedError):
+        s.check()
+    f = s.read_populations()
+    f[np.isnan(f)] = 0.0
+    f[5, 3, 2, :] *= 0.2           # rho = 0.2 < 0.3 at one cell
+    s.write_populations(f)
+    with pytest.raises(gpkg.DivergedError):
+        s.check(rho_floor=0.3)
+    s.close()
+
+
+def test_empty_marker_set_and_counters(gpkg):
+    s = gpkg.Solver(24, 10, 4, 1.5)
+    ibm = gpkg.IBM(s, [], [], [])
+    ibm.compute_force(10.0, 5.0, 0.1, 0.0, 0.0, 0.0)
+    s.profile(True)
+    s.step(ibm)
+    s.step(ibm)
+    p = s.profile_read()
+    assert p["fused_launches"] == 2 and p["fused_ms"] > 0
+    fx, fy, fz = ibm.read_forces()
+    assert not fx.any() and not fy.any()
+    assert ibm.step_count() == 1
+    np.testing.assert_array_equal(ibm.force_history(1), np.zeros((1, 4)))
+    s.close()
+
+
+def test_forces_persist_after_step_like_reference(gpkg):
+    cfg = gpkg.wing_case(48, 24, 4, 8.0, re=20.0)
+    sim = gpkg.Simulation(cfg)
+    sim.ibm.compute_force(*cfg.motion_state(1))
+    before = sim.ibm.read_forces()
+    sim.solver.step(sim.ibm)
+    after = sim.ibm.read_forces()
+    np.testing.assert_array_equal(before[0], after[0])
+    assert np.abs(before[0]).max() <= 0.05 and np.abs(before[0]).max() > 0
+    sim.close()
+
+
+@pytest.mark.parametrize("storage,tol", [("f16", 2e-3), ("bf16", 2e-2)])
+def test_shifted_storage_error_against_fp64_oracle(gpkg, oracle_mod, storage, tol):
+    """16-bit shifted populations f - w with float32 collision: field and lift/drag error
+    against the FP64 oracle of the same case (200x80x16, 300 steps)."""
+    cfg = gpkg.small_case(storage=storage)
+    sim = gpkg.Simulation(cfg)
+    sim.run(300)
+    got = sim.solver.read_macro()
+    ref = oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                            cfg.X0, cfg.Y0, cfg.Z0, real="f64")
+    ref_hist = ref.run(0, 300, cfg.motion())
+    rho, ux, uy, _ = ref.macro()
+    e_rho = rel_l2(got["rho"] - 1.0, rho - 1.0)
+    e_u = rel_l2(got["ux"], ux)
+    e_f = rel_l2(sim.ibm.force_history(300), ref_hist)
+    print(f"{storage}: rel L2 (rho-1) {e_rho:.2e}, ux {e_u:.2e}, force history {e_f:.2e}")
+    assert e_u < tol and e_f < 10 * tol
+    sim.close()

@@ -1,0 +1,153 @@
+"""GPU path (through the C ABI) against the reference's golden vectors and the CPU oracle.
+
+Tolerances (float32 path): relative L2 <= 1e-5 on rho and u, <= 1e-4 on the force
+histories (lift/drag), as the plain FP32 target states. The GPU sums in a different order
+than the reference (closed-form moment transform, warp-shuffle interpolation, atomic
+spreading), so agreement is to float32 rounding, not bitwise.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden_inflow, load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_FIELD = 1e-5
+TOL_FORCE = 1e-4
+
+
+@pytest.fixture(scope="module")
+def gpkg(built_pkg):
+    return built_pkg
+
+
+@pytest.mark.parametrize("case", ["A", "B"])
+def test_gpu_matches_reference_golden(gpkg, case):
+    d = load_golden(case)
+    ux_in, uy_in = golden_inflow(d)
+    s = gpkg.Solver(int(d["Nx"]), int(d["Ny"]), int(d["Nz"]), float(d["s_v"]), float(d["s_e"]),
+                    ux_in, uy_in)
+    ibm = gpkg.IBM(s, d["X0"], d["Y0"], d["Z0"])
+    np.testing.assert_array_equal(s.read_populations(), d["f_init"])
+    for step in range(1, int(d["n_steps"]) + 1):
+        ibm.compute_force(*d["motion"][step - 1])
+        if step in d["record"]:
+            mk = ibm.read_markers()
+            for k in ("X", "Y", "VX", "VY"):
+                np.testing.assert_allclose(mk[k], d[f"s{step}_{k}"], rtol=2e-6, atol=2e-6)
+            np.testing.assert_array_equal(mk["Z"], d[f"s{step}_Z"])
+            for k in ("Uk", "Vk", "FXk", "FYk"):
+                assert rel_l2(mk[k], d[f"s{step}_{k}"]) < TOL_FIELD, (step, k)
+            fx, fy, fz = ibm.read_forces()
+            assert rel_l2(fx, d[f"s{step}_fx"]) < TOL_FIELD
+            assert rel_l2(fy, d[f"s{step}_fy"]) < TOL_FIELD
+            assert not fz.any()
+        s.step(ibm)
+        if step in d["record"]:
+            m = s.read_macro()
+            for k in ("rho", "ux", "uy"):
+                assert rel_l2(m[k], d[f"s{step}_{k}"]) < TOL_FIELD, (step, k)
+            assert np.max(np.abs(m["uz"] - d[f"s{step}_uz"])) < 1e-7
+        if step in d["f_record"]:
+            assert rel_l2(s.read_populations(), d[f"s{step}_f"]) < TOL_FIELD
+    s.close()
+
+
+def _oracle_for(oracle_mod, cfg, real="f32"):
+    return oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                             cfg.X0, cfg.Y0, cfg.Z0, real=real)
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_small_case_against_oracle(gpkg, oracle_mod, graph):
+    """200x80x16, chord 32, Re 200: 300 steps of the full driver loop."""
+    cfg = gpkg.small_case()
+    nsteps = 300
+    sim = gpkg.Simulation(cfg)
+    sim.run(nsteps, graph=graph)
+    got = sim.solver.read_macro()
+    hist = sim.ibm.force_history(nsteps)
+    ref = _oracle_for(oracle_mod, cfg)
+    ref_hist = ref.run(0, nsteps, cfg.motion())
+    want = dict(zip(("rho", "ux", "uy", "uz"), ref.macro()))
+    for k in ("rho", "ux", "uy"):
+        assert rel_l2(got[k], want[k]) < TOL_FIELD, k
+    assert rel_l2(hist, ref_hist) < TOL_FORCE
+    cg = gpkg.force_coefficients(hist, cfg)
+    cr = gpkg.force_coefficients(ref_hist, cfg)
+    for k in ("cd", "cl"):
+        assert np.max(np.abs(cg[k] - cr[k])) <= TOL_FORCE * max(1.0, np.max(np.abs(cr[k])))
+    sim.close()
+
+
+def test_host_motion_loop_equals_device_motion(gpkg):
+    cfg = gpkg.small_case()
+    a = gpkg.Simulation(cfg)
+    b = gpkg.Simulation(cfg)
+    for step in range(1, 41):
+        a.step_host_motion(step)
+    b.run(40, graph=True)
+    ma, mb = a.solver.read_macro(), b.solver.read_macro()
+    for k in ("rho", "ux", "uy"):
+        assert rel_l2(ma[k], mb[k]) < 1e-6
+    assert rel_l2(a.ibm.force_history(40), b.ibm.force_history(40)) < 1e-5
+    a.close()
+    b.close()
+
+
+def test_reference_airplane_geometry_short_run(gpkg, oracle_mod):
+    """The reference's airplane marker set (74,201 markers: wing, tip caps, fuselage,
+    tails) on a lattice cut down to 240x120x160, 6 steps, against the oracle."""
+    full = gpkg.reference_airplane_case()
+    from dataclasses import replace
+    cfg = replace(full, nx=240, ny=120, x0=100.0, y0=60.0)
+    sim = gpkg.Simulation(cfg)
+    ref = _oracle_for(oracle_mod, cfg)
+    for step in range(1, 7):
+        ms = cfg.motion_state(step)
+        sim.ibm.compute_force(*ms)
+        sim.solver.step(sim.ibm)
+        ref.compute_force(*ms)
+        ref.lbm_step()
+    got = sim.solver.read_macro()
+    want = dict(zip(("rho", "ux", "uy", "uz"), ref.macro()))
+    for k in ("rho", "ux", "uy"):
+        assert rel_l2(got[k], want[k]) < TOL_FIELD, k
+    mk = sim.ibm.read_markers()
+    ref_mk = ref.markers()
+    assert rel_l2(mk["FXk"], ref_mk["FXk"]) < TOL_FIELD
+    sim.close()
+
+
+def test_full_size_short_parity(gpkg, oracle_mod):
+    """600x200x50, chord 80: the first 4 steps against the oracle at full size."""
+    cfg = gpkg.full_case()
+    sim = gpkg.Simulation(cfg)
+    sim.run(4, graph=False)
+    ref = _oracle_for(oracle_mod, cfg)
+    ref_hist = ref.run(0, 4, cfg.motion())
+    got = sim.solver.read_macro()
+    want = dict(zip(("rho", "ux", "uy", "uz"), ref.macro()))
+    for k in ("rho", "ux", "uy"):
+        assert rel_l2(got[k], want[k]) < TOL_FIELD, k
+    assert rel_l2(sim.ibm.force_history(4), ref_hist) < TOL_FORCE
+    sim.close()
+
+
+def test_full_size_properties(gpkg):
+    """600x200x50 for 400 graph-replayed steps: finite, rho in range, and mirror symmetric
+    in z (the extruded wing, the lattice and the seam treatment of the stencils are all
+    symmetric under z -> Nz-1-z)."""
+    cfg = gpkg.full_case()
+    sim = gpkg.Simulation(cfg)
+    sim.run(400, graph=True)
+    st = sim.solver.check()
+    assert st["nonfinite"] == 0 and 0.9 < st["rho_min"] <= st["rho_max"] < 1.1
+    m = sim.solver.read_macro()
+    for k in ("rho", "ux", "uy"):
+        assert rel_l2(m[k][:, :, ::-1], m[k]) < 1e-5, k
+    assert np.max(np.abs(m["uz"] + m["uz"][:, :, ::-1])) < 1e-5
+    h = sim.ibm.force_history(400)
+    assert np.all(np.isfinite(h)) and np.any(h[:, 0] != 0)
+    sim.close()
