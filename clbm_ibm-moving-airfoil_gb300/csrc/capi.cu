@@ -7,6 +7,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <algorithm>
 
 #include "clbm_internal.cuh"
 
@@ -76,6 +77,7 @@ struct clbm_solver {
     const clbm_ibm* g_ibm = nullptr;
     clbm_motion g_m{};
     int g_cur = -1;
+    std::vector<clbm_ibm*> ibms;  // IBMs bound to this solver (orphaned on destroy)
 };
 
 struct clbm_ibm {
@@ -217,6 +219,8 @@ int clbm_destroy(clbm_solver* s) {
     if (!s) return CLBM_OK;
     if (s->st) cudaStreamSynchronize(s->st);
     free_graph(s);
+    for (clbm_ibm* ibm : s->ibms) ibm->s = nullptr;
+    s->ibms.clear();
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
     void* ptrs[] = {s->f[0], s->f[1], s->rho, s->ux, s->uy, s->uz, s->dfx, s->dfy, s->dfz,
                     s->stage, s->stats};
@@ -232,8 +236,8 @@ int clbm_step(clbm_solver* s, const clbm_ibm* ibm) {
     if (ibm && ibm->s != s) return fail(CLBM_ERR_ARG, "clbm_step: IBM bound to another solver");
     ForceArgs fa{};
     if (ibm) {
-        fa.fx = ibm->a.fx;
-        fa.fy = ibm->a.fy;
+        fa.qx = ibm->a.fx;
+        fa.qy = ibm->a.fy;
         fa.dev = ibm->a.dev;
     }
     return step_impl(s, ibm ? kForceBand : kForceNone, fa);
@@ -254,7 +258,7 @@ int clbm_step_dense_force(clbm_solver* s, const float* fx, const float* fy, cons
     else CK(cudaMemsetAsync(s->dfz, 0, pb, s->st));
     CK_LAUNCH();
     s->launches += fz ? 3 : 2;
-    ForceArgs fa{s->dfx, s->dfy, s->dfz, nullptr};
+    ForceArgs fa{s->dfx, s->dfy, s->dfz, nullptr, nullptr, nullptr};
     return step_impl(s, kForceDense, fa);
 }
 
@@ -386,13 +390,14 @@ int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0
             return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc failed"));
         cudaMemsetAsync(*p, 0, nb, s->st);
     }
-    const size_t pb = (size_t)s->g.plane * sizeof(float);
+    const size_t pb = (size_t)s->g.plane * sizeof(long long);
     if (cudaMalloc(&a.fx, pb) != cudaSuccess || cudaMalloc(&a.fy, pb) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc of force fields failed"));
     cudaMemsetAsync(a.fx, 0, pb, s->st);
     cudaMemsetAsync(a.fy, 0, pb, s->st);
     if (cudaMalloc(&a.dev, sizeof(IbmDev)) != cudaSuccess ||
-        cudaMalloc(&a.hist, (size_t)kHistCap * 4 * sizeof(double)) != cudaSuccess)
+        cudaMalloc(&a.hist, (size_t)kHistCap * 4 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&a.part, (size_t)kFinishBlocks * 4 * sizeof(double)) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc failed"));
     cudaMemsetAsync(a.hist, 0, (size_t)kHistCap * 4 * sizeof(double), s->st);
     IbmDev init{};
@@ -424,48 +429,58 @@ int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0
     a.uy = s->uy;
     cudaError_t e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) return bail(fail(CLBM_ERR_CUDA, "ibm_create: %s", cudaGetErrorString(e)));
+    s->ibms.push_back(ibm);
     *out = ibm;
     return CLBM_OK;
 }
 
 int ibm_destroy(clbm_ibm* ibm) {
     if (!ibm) return CLBM_OK;
-    if (ibm->s) {
-        cudaStreamSynchronize(ibm->s->st);
-        if (ibm->s->g_ibm == ibm) free_graph(ibm->s);
+    if (clbm_solver* s = ibm->s) {
+        cudaStreamSynchronize(s->st);
+        if (s->g_ibm == ibm) free_graph(s);
+        s->ibms.erase(std::remove(s->ibms.begin(), s->ibms.end(), ibm), s->ibms.end());
     }
     IbmArrays& a = ibm->a;
     void* ptrs[] = {(void*)a.X0, (void*)a.Y0, (void*)a.Z0, a.X, a.Y, a.Z, a.VX, a.VY, a.Uk,
-                    a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist};
+                    a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist, a.part};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete ibm;
     return CLBM_OK;
 }
 
+// An IBM whose solver was destroyed first stays a valid handle that can only be destroyed.
+static int check_bound(const clbm_ibm* ibm, const char* fn) {
+    if (!ibm) return fail(CLBM_ERR_ARG, "%s: null IBM", fn);
+    if (!ibm->s) return fail(CLBM_ERR_STATE, "%s: the IBM's solver was destroyed", fn);
+    return CLBM_OK;
+}
+
 int ibm_compute_force(clbm_ibm* ibm, double xc, double yc, double theta, double vx, double vy,
                       double omega) {
-    if (!ibm) return fail(CLBM_ERR_ARG, "ibm_compute_force: null IBM");
+    if (int rc = check_bound(ibm, "ibm_compute_force")) return rc;
     MotionF mf{(float)xc, (float)yc, (float)theta, (float)vx, (float)vy, (float)omega};
     return ibm_force_impl(ibm, false, mf, clbm_motion{});
 }
 
 int ibm_compute_force_motion(clbm_ibm* ibm, const clbm_motion* m) {
-    if (!ibm || !m) return fail(CLBM_ERR_ARG, "ibm_compute_force_motion: null argument");
+    if (int rc = check_bound(ibm, "ibm_compute_force_motion")) return rc;
+    if (!m) return fail(CLBM_ERR_ARG, "ibm_compute_force_motion: null motion");
     return ibm_force_impl(ibm, true, MotionF{}, *m);
 }
 
 int ibm_read_forces(const clbm_ibm* ibm, float* fx, float* fy, float* fz) {
-    if (!ibm) return fail(CLBM_ERR_ARG, "ibm_read_forces: null IBM");
+    if (int rc = check_bound(ibm, "ibm_read_forces")) return rc;
     clbm_solver* s = ibm->s;
     const size_t n = cells(s);
     int rc = ensure_stage(s, 2 * n * sizeof(float));
     if (rc) return rc;
-    const float* src[2] = {ibm->a.fx, ibm->a.fy};
+    const long long* src[2] = {ibm->a.fx, ibm->a.fy};
     float* dst[2] = {fx, fy};
     for (int k = 0; k < 2; ++k) {
         if (!dst[k]) continue;
-        launch_export_field(src[k], s->stage + k * n, s->g, 0.05f, s->st);
+        launch_export_qfield(src[k], s->stage + k * n, s->g, 0.05f, s->st);
         CK_LAUNCH();
         s->launches += 1;
         CK(cudaMemcpyAsync(dst[k], s->stage + k * n, n * sizeof(float), cudaMemcpyDeviceToHost,
@@ -477,7 +492,8 @@ int ibm_read_forces(const clbm_ibm* ibm, float* fx, float* fy, float* fz) {
 }
 
 int ibm_read_markers(const clbm_ibm* ibm, float* out) {
-    if (!ibm || !out) return fail(CLBM_ERR_ARG, "ibm_read_markers: null argument");
+    if (int rc = check_bound(ibm, "ibm_read_markers")) return rc;
+    if (!out) return fail(CLBM_ERR_ARG, "ibm_read_markers: null argument");
     const IbmArrays& a = ibm->a;
     const float* src[9] = {a.X, a.Y, a.Z, a.VX, a.VY, a.Uk, a.Vk, a.FXk, a.FYk};
     for (int k = 0; k < 9; ++k)
@@ -489,7 +505,8 @@ int ibm_read_markers(const clbm_ibm* ibm, float* out) {
 }
 
 int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out) {
-    if (!ibm || !out || count < 0) return fail(CLBM_ERR_ARG, "ibm_read_force_history: bad argument");
+    if (int rc = check_bound(ibm, "ibm_read_force_history")) return rc;
+    if (!out || count < 0) return fail(CLBM_ERR_ARG, "ibm_read_force_history: bad argument");
     const long long avail = std::min<long long>(ibm->calls, kHistCap);
     if (count > avail)
         return fail(CLBM_ERR_ARG, "ibm_read_force_history: %d entries requested, %lld available",

@@ -58,7 +58,6 @@ constexpr int kBoxEmpty = 0x7f7f7f7f;
 struct IbmDev {
     long long step;        // number of completed compute_force calls
     int box[2][6];         // slot (call index & 1): imin, -imax, jmin, -jmax, kmin, -kmax
-    double acc[4];         // sum fx, sum fy (clipped Eulerian), sum FX_k, sum FY_k
     unsigned int ticket;   // last-block detection of the force-sum kernel
     int pad;
 };
@@ -147,10 +146,20 @@ inline size_t store_bytes(int storage) { return storage == CLBM_STORE_F32 ? 4 : 
 // Force source of the fused step.
 enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2 };
 
+// IBM force fields are accumulated in 64-bit fixed point with kForceScale units per unit
+// force: integer atomics are associative, so spreading is deterministic, and a float32
+// contribution scaled by a power of two converts exactly whenever |v| >= 2^-17.
+constexpr float kForceScale = 1099511627776.0f;         // 2^40
+constexpr float kForceInvScale = 1.0f / 1099511627776.0f;
+
+__device__ __forceinline__ float qforce(long long v) { return (float)v * kForceInvScale; }
+
 struct ForceArgs {
-    const float* fx;       // padded layout
+    const float* fx;       // dense mode, padded layout
     const float* fy;
-    const float* fz;       // dense mode only
+    const float* fz;
+    const long long* qx;   // band mode: fixed-point IBM fields, padded layout
+    const long long* qy;
     const IbmDev* dev;     // band mode: box of the last compute_force
 };
 
@@ -167,6 +176,9 @@ void launch_fill_macro(const Grid& g, const Coef& c, float* rho, float* ux, floa
 // Padded-layout field -> reference layout (x, y, z), optional clip to +-clipv.
 void launch_export_field(const float* a, float* out, const Grid& g, float clipv,
                          cudaStream_t st);
+// Same for a fixed-point IBM force field.
+void launch_export_qfield(const long long* a, float* out, const Grid& g, float clipv,
+                          cudaStream_t st);
 // Reference layout (x, y, z) -> padded layout.
 void launch_import_field(const float* in, float* a, const Grid& g, cudaStream_t st);
 void launch_export_populations(int storage, bool pull, const void* f, float* out,
@@ -179,10 +191,11 @@ struct IbmArrays {
     int n;
     const float *X0, *Y0, *Z0;
     float *X, *Y, *Z, *VX, *VY, *Uk, *Vk, *FXk, *FYk;
-    float *fx, *fy;   // padded full grid
-    float *ux, *uy;   // padded full grid (macro of the solver)
+    long long *fx, *fy;   // padded full grid, fixed point (kForceScale)
+    float *ux, *uy;       // padded full grid (macro of the solver)
     IbmDev* dev;
     double* hist;
+    double* part;         // per-block partial sums of the force-sum kernel [kFinishBlocks][4]
     int hist_cap;
     int max_bx, max_by, max_bz;   // upper bound of the band box dimensions
 };
@@ -194,8 +207,9 @@ struct MotionF { float xc, yc, theta, vx, vy, omega; };
 void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
                         const MotionF& mf, const clbm_motion& m, cudaStream_t st);
 // Zero the previous call's force band and compute the macro fields on this call's band.
+constexpr int kFinishBlocks = 304;   // 2 x 152 SMs
 void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
-                         IbmDev* dev, float* fx, float* fy, float* rho, float* ux, float* uy,
+                         IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
                          cudaStream_t st);
 void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st);

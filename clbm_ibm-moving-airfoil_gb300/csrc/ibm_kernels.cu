@@ -118,11 +118,15 @@ __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a,
         a.FXk[m] = fxk;
         a.FYk[m] = fyk;
     }
+    // spreading: the float32 contribution fxk * w (airfoil_moving.py:212-214) is added in
+    // 64-bit fixed point, so the sum does not depend on the order of the atomics
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         if (wt[h] != 0.0f) {
-            atomicAdd(a.fx + cell[h], fxk * wt[h]);
-            atomicAdd(a.fy + cell[h], fyk * wt[h]);
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + cell[h]),
+                      (unsigned long long)__float2ll_rn(fxk * wt[h] * kForceScale));
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + cell[h]),
+                      (unsigned long long)__float2ll_rn(fyk * wt[h] * kForceScale));
         }
     }
 }
@@ -150,8 +154,8 @@ __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g
         const int oy = (int)(r % b.jlen), oz = (int)(r / b.jlen);
         const int x = b.i0 + ox, y = pmod(b.j0 + oy, g.ny), z = pmod(b.k0 + oz, g.nz);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
-        sx += (double)fminf(fmaxf(a.fx[c], -0.05f), 0.05f);
-        sy += (double)fminf(fmaxf(a.fy[c], -0.05f), 0.05f);
+        sx += (double)fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f);
+        sy += (double)fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f);
     }
     for (long long t = (long long)blockIdx.x * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
         mx += (double)a.FXk[t];
@@ -161,10 +165,12 @@ __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) { red[warp][0] = sx; red[warp][1] = sy; red[warp][2] = mx; red[warp][3] = my; }
     __syncthreads();
+    // Per-block partials, summed by the last block in block order: the result does not
+    // depend on which block finishes first.
     if (threadIdx.x < 4) {
         double v = 0.0;
         for (int w = 0; w < kFinishBlock / 32; ++w) v += red[w][threadIdx.x];
-        atomicAdd(&dev->acc[threadIdx.x], v);
+        a.part[4 * blockIdx.x + threadIdx.x] = v;
         __threadfence();
     }
     __syncthreads();
@@ -173,14 +179,15 @@ __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g
         last = (tk == gridDim.x - 1);
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
+    if (last && threadIdx.x < 4) {
         __threadfence();
-        double* h = a.hist + 4 * ((s - 1) % a.hist_cap);
-        for (int e = 0; e < 4; ++e) {
-            unsigned long long bits = atomicExch(
-                reinterpret_cast<unsigned long long*>(&dev->acc[e]), 0ull);
-            h[e] = __longlong_as_double((long long)bits);
-        }
+        const volatile double* p = a.part;
+        double v = 0.0;
+        for (unsigned int blk = 0; blk < gridDim.x; ++blk) v += p[4 * blk + threadIdx.x];
+        a.hist[4 * ((s - 1) % a.hist_cap) + threadIdx.x] = v;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
         dev->ticket = 0u;
         // the previous call's box was consumed by this call's band-prepare
         for (int e = 0; e < 6; ++e) dev->box[(s + 1) & 1][e] = kBoxEmpty;
@@ -207,7 +214,7 @@ void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st
 
 void launch_ibm_finish(const IbmArrays& a, const Grid& g, cudaStream_t st) {
     const long long work = std::max<long long>((long long)a.max_bx * a.max_by * a.max_bz, a.n);
-    int blocks = (int)std::min<long long>((work + kFinishBlock - 1) / kFinishBlock, 304);
+    int blocks = (int)std::min<long long>((work + kFinishBlock - 1) / kFinishBlock, kFinishBlocks);
     if (blocks < 1) blocks = 1;
     k_ibm_finish<<<blocks, kFinishBlock, 0, st>>>(a, g);
 }

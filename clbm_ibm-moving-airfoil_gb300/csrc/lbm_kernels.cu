@@ -198,8 +198,8 @@ __global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T
         if (in_band(b, x, y, z, g.ny, g.nz)) {
             // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
             // fz is always zero there.
-            const float Fx = fminf(fmaxf(fa.fx[cell], -0.05f), 0.05f);
-            const float Fy = fminf(fmaxf(fa.fy[cell], -0.05f), 0.05f);
+            const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
+            const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
             collide<true>(f, c, Fx, Fy, 0.0f);
         } else {
             collide<false>(f, c, 0.f, 0.f, 0.f);
@@ -289,14 +289,18 @@ __global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g,
 // Tiled transpose between the padded (z, y, x) layout and the reference (x, y, z) layout.
 constexpr int kT = 32;
 
-__global__ void k_export_field(const float* __restrict__ a, float* __restrict__ out, Grid g,
+__device__ __forceinline__ float as_force(float v) { return v; }
+__device__ __forceinline__ float as_force(long long v) { return qforce(v); }
+
+template <typename T>
+__global__ void k_export_field(const T* __restrict__ a, float* __restrict__ out, Grid g,
                                float clipv) {
     __shared__ float tile[kT][kT + 1];
     const int x0 = blockIdx.x * kT, z0 = blockIdx.z * kT, y = blockIdx.y;
     for (int r = threadIdx.y; r < kT; r += blockDim.y) {
         const int z = z0 + r, x = x0 + threadIdx.x;
         float v = 0.f;
-        if (z < g.nz && x < g.nx) v = a[((long long)z * g.ny + y) * g.pitch + x];
+        if (z < g.nz && x < g.nx) v = as_force(a[((long long)z * g.ny + y) * g.pitch + x]);
         if (clipv > 0.f) v = fminf(fmaxf(v, -clipv), clipv);
         tile[r][threadIdx.x] = v;
     }
@@ -412,7 +416,13 @@ void launch_fill_macro(const Grid& g, const Coef& c, float* rho, float* ux, floa
 void launch_export_field(const float* a, float* out, const Grid& g, float clipv,
                          cudaStream_t st) {
     dim3 grid((g.nx + kT - 1) / kT, g.ny, (g.nz + kT - 1) / kT);
-    k_export_field<<<grid, dim3(kT, 8), 0, st>>>(a, out, g, clipv);
+    k_export_field<float><<<grid, dim3(kT, 8), 0, st>>>(a, out, g, clipv);
+}
+
+void launch_export_qfield(const long long* a, float* out, const Grid& g, float clipv,
+                          cudaStream_t st) {
+    dim3 grid((g.nx + kT - 1) / kT, g.ny, (g.nz + kT - 1) / kT);
+    k_export_field<long long><<<grid, dim3(kT, 8), 0, st>>>(a, out, g, clipv);
 }
 
 void launch_import_field(const float* in, float* a, const Grid& g, cudaStream_t st) {
@@ -440,7 +450,7 @@ void launch_import_populations(int storage, const float* in, void* f, const Grid
 // Band-prepare needs the same gather; the IBM translation unit calls this launcher.
 template <int S, bool PULL>
 __global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
-                               IbmDev* dev, float* fx, float* fy, float* rho, float* ux,
+                               IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux,
                                float* uy, float* uz, bool compute_macro) {
     // Box of this compute_force call (slot s & 1) and of the previous one (slot (s-1) & 1).
     const long long s = dev->step + 1;
@@ -453,8 +463,8 @@ __global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid 
     if (ox < ob.ilen && oy < ob.jlen && oz < ob.klen) {
         const int x = ob.i0 + ox, y = pmod(ob.j0 + oy, g.ny), z = pmod(ob.k0 + oz, g.nz);
         const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-        fx[cell] = 0.f;
-        fy[cell] = 0.f;
+        fx[cell] = 0;
+        fy[cell] = 0;
     }
     // _macro_post of the current state on the cells the stencils of this call touch
     if (compute_macro && ox < nb.ilen && oy < nb.jlen && oz < nb.klen) {
@@ -478,7 +488,7 @@ __global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid 
 }
 
 void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
-                         IbmDev* dev, float* fx, float* fy, float* rho, float* ux, float* uy,
+                         IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
                          cudaStream_t st) {
     dim3 block(32, 4, 1);

@@ -91,6 +91,19 @@ def test_empty_marker_set_and_counters(gpkg):
     s.close()
 
 
+def test_solver_destroyed_before_ibm(gpkg):
+    """Destroying the solver first orphans its IBM: later calls report CLBM_ERR_STATE and
+    destroying the IBM is still safe (Python finalisers run in arbitrary order)."""
+    s = gpkg.Solver(24, 10, 4, 1.5)
+    ibm = gpkg.IBM(s, [0.0], [0.0], [1.0])
+    gpkg.lib().clbm_destroy(s._h)
+    s._h = None
+    with pytest.raises(gpkg.CLBMError) as ei:
+        ibm.compute_force(10.0, 5.0, 0.0, 0.0, 0.0, 0.0)
+    assert ei.value.code == 4
+    ibm.close()
+
+
 def test_forces_persist_after_step_like_reference(gpkg):
     cfg = gpkg.wing_case(48, 24, 4, 8.0, re=20.0)
     sim = gpkg.Simulation(cfg)

@@ -48,7 +48,9 @@ def test_gpu_matches_reference_golden(gpkg, case):
             m = s.read_macro()
             for k in ("rho", "ux", "uy"):
                 assert rel_l2(m[k], d[f"s{step}_{k}"]) < TOL_FIELD, (step, k)
-            assert np.max(np.abs(m["uz"] - d[f"s{step}_uz"])) < 1e-7
+            # uz is a small secondary component: its error is judged on the velocity scale
+            uscale = np.max(np.abs(d[f"s{step}_ux"]))
+            assert np.max(np.abs(m["uz"] - d[f"s{step}_uz"])) < TOL_FIELD * uscale
         if step in d["f_record"]:
             assert rel_l2(s.read_populations(), d[f"s{step}_f"]) < TOL_FIELD
     s.close()
@@ -81,7 +83,23 @@ def test_small_case_against_oracle(gpkg, oracle_mod, graph):
     sim.close()
 
 
+def test_runs_are_bitwise_repeatable(gpkg):
+    """Spreading accumulates in 64-bit fixed point and the force sums reduce in a fixed
+    order, so two runs of the same case give identical bits."""
+    cfg = gpkg.small_case()
+    out = []
+    for _ in range(2):
+        sim = gpkg.Simulation(cfg)
+        sim.run(60, graph=True)
+        out.append((sim.solver.read_populations(), sim.ibm.force_history(60)))
+        sim.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+
+
 def test_host_motion_loop_equals_device_motion(gpkg):
+    """main_moving.py's loop with _motion_state on the host (double, truncated to float32
+    at the call) against the motion law evaluated on the device inside a CUDA graph."""
     cfg = gpkg.small_case()
     a = gpkg.Simulation(cfg)
     b = gpkg.Simulation(cfg)
@@ -90,7 +108,7 @@ def test_host_motion_loop_equals_device_motion(gpkg):
     b.run(40, graph=True)
     ma, mb = a.solver.read_macro(), b.solver.read_macro()
     for k in ("rho", "ux", "uy"):
-        assert rel_l2(ma[k], mb[k]) < 1e-6
+        assert rel_l2(ma[k], mb[k]) < 1e-6, k
     assert rel_l2(a.ibm.force_history(40), b.ibm.force_history(40)) < 1e-5
     a.close()
     b.close()
