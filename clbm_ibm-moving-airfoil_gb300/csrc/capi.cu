@@ -46,8 +46,8 @@ constexpr double kWd[19] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
 constexpr int kHistCap = 1 << 16;
 // kernels one graph-captured step launches: markers, band-prepare, interp/spread, finish,
-// fused stream-collide
-constexpr int kKernelsPerIbmStep = 5;
+// bulk stream-collide, box stream-collide
+constexpr int kKernelsPerIbmStep = 6;
 
 }  // namespace
 
@@ -66,7 +66,11 @@ struct clbm_solver {
     float* stage = nullptr;
     size_t stage_bytes = 0;
     unsigned long long* stats = nullptr;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;     // high priority: IBM chain, box pass, transfers
+    cudaStream_t st2 = nullptr;    // low priority: bulk stream-collide of IBM steps
+    cudaEvent_t ev_bulk = nullptr; // end of the bulk pass (joined into st)
+    cudaEvent_t ev_fork = nullptr; // fork point of a bulk pass without a fresh box event
+    long long version = 0;         // bumped whenever f[cur] changes
     long long launches = 0;
     // profiling of the fused kernel
     bool prof = false;
@@ -83,7 +87,9 @@ struct clbm_solver {
 struct clbm_ibm {
     clbm_solver* s = nullptr;
     IbmArrays a{};
-    long long calls = 0;   // host mirror of the device call counter
+    long long calls = 0;          // host mirror of the device call counter
+    cudaEvent_t ev_box = nullptr; // recorded on st after the marker kernel of compute_force
+    long long box_version = -1;   // solver state version that ev_box belongs to
 };
 
 namespace {
@@ -100,38 +106,67 @@ int ensure_stage(clbm_solver* s, size_t bytes) {
 
 size_t cells(const clbm_solver* s) { return (size_t)s->g.nx * s->g.ny * s->g.nz; }
 
-int record_event(clbm_solver* s) {
+int record_event(clbm_solver* s, cudaStream_t st) {
     if (s->ev_used == s->ev.size()) {
         cudaEvent_t e;
         CK(cudaEventCreate(&e));
         s->ev.push_back(e);
     }
-    CK(cudaEventRecord(s->ev[s->ev_used++], s->st));
+    CK(cudaEventRecord(s->ev[s->ev_used++], st));
     return CLBM_OK;
 }
 
-int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa) {
-    if (s->prof) {
-        int rc = record_event(s);
-        if (rc) return rc;
-    }
-    launch_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur], s->g,
-                          s->c, fa, s->st);
+// One fused stream-collide launch on stream `st`, bracketed by timing events if profiling.
+int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bool box,
+             long long box_cells) {
+    if (s->prof)
+        if (int rc = record_event(s, st)) return rc;
+    if (box)
+        launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
+                                  s->c, fa, box_cells, st);
+    else
+        launch_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur],
+                              s->g, s->c, fa, st);
     CK_LAUNCH();
-    if (s->prof) {
-        int rc = record_event(s);
-        if (rc) return rc;
-    }
+    if (s->prof)
+        if (int rc = record_event(s, st)) return rc;
     s->launches += 1;
+    return CLBM_OK;
+}
+
+int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ibm) {
+    if (fmode != kForceBand) {
+        if (int rc = sc_timed(s, fmode, fa, s->st, false, 0)) return rc;
+    } else {
+        // IBM step in two passes. The bulk pass (cells outside the force box) needs only the
+        // box, so it forks off after the marker kernel of the last compute_force and runs on
+        // the low-priority stream while the IBM chain still computes the forces; the box
+        // pass follows the IBM chain on the main stream; the main stream then joins the
+        // bulk pass. The fork is valid only while the state is the one compute_force saw.
+        if (ibm->box_version == s->version) {
+            CK(cudaStreamWaitEvent(s->st2, ibm->ev_box, 0));
+        } else {
+            CK(cudaEventRecord(s->ev_fork, s->st));
+            CK(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
+        }
+        if (int rc = sc_timed(s, kForceSkipBand, fa, s->st2, false, 0)) return rc;
+        CK(cudaEventRecord(s->ev_bulk, s->st2));
+        const long long box_cells = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
+        if (int rc = sc_timed(s, kForceBand, fa, s->st, true, box_cells)) return rc;
+        CK(cudaStreamWaitEvent(s->st, s->ev_bulk, 0));
+    }
     s->cur = 1 - s->cur;
     s->local = false;
     s->macro_full = false;
+    s->version += 1;
     return CLBM_OK;
 }
 
 int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motion& m) {
     clbm_solver* s = ibm->s;
     launch_ibm_markers(ibm->a, s->g, devm, mf, m, s->st);
+    CK(cudaEventRecord(ibm->ev_box, s->st));
+    ibm->box_version = s->version;
     launch_band_prepare(s->cfg.storage, !s->local, s->f[s->cur], s->g, s->c, ibm->a.dev,
                         ibm->a.fx, ibm->a.fy, s->rho, s->ux, s->uy, s->uz, ibm->a.max_bx,
                         ibm->a.max_by, ibm->a.max_bz, !s->macro_full, s->st);
@@ -185,7 +220,12 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
     s->c.c16 = (float)(1.0 / 6.0);
     for (int q = 0; q < 19; ++q) s->c.wc[q] = (float)(kWd[q] * (1.0 - cfg->s_v * 0.5));
     auto bail = [&](int rc) { clbm_destroy(s); return rc; };
-    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess)
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s->st2, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_bulk, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "clbm_create: no CUDA device or stream creation failed: %s",
                          cudaGetErrorString(cudaGetLastError())));
     const size_t fbytes = (size_t)plane * 19 * store_bytes(cfg->storage);
@@ -226,6 +266,10 @@ int clbm_destroy(clbm_solver* s) {
                     s->stage, s->stats};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (s->st2) cudaStreamSynchronize(s->st2);
+    if (s->ev_bulk) cudaEventDestroy(s->ev_bulk);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->st2) cudaStreamDestroy(s->st2);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return CLBM_OK;
@@ -240,7 +284,7 @@ int clbm_step(clbm_solver* s, const clbm_ibm* ibm) {
         fa.qy = ibm->a.fy;
         fa.dev = ibm->a.dev;
     }
-    return step_impl(s, ibm ? kForceBand : kForceNone, fa);
+    return step_impl(s, ibm ? kForceBand : kForceNone, fa, ibm);
 }
 
 int clbm_step_dense_force(clbm_solver* s, const float* fx, const float* fy, const float* fz) {
@@ -259,7 +303,7 @@ int clbm_step_dense_force(clbm_solver* s, const float* fx, const float* fy, cons
     CK_LAUNCH();
     s->launches += fz ? 3 : 2;
     ForceArgs fa{s->dfx, s->dfy, s->dfz, nullptr, nullptr, nullptr};
-    return step_impl(s, kForceDense, fa);
+    return step_impl(s, kForceDense, fa, nullptr);
 }
 
 int clbm_step_host_force(clbm_solver* s, const float* fx, const float* fy, const float* fz) {
@@ -337,6 +381,7 @@ int clbm_write_populations(clbm_solver* s, const float* f_host) {
     s->launches += 1;
     s->local = true;
     s->macro_full = false;
+    s->version += 1;
     CK(cudaStreamSynchronize(s->st));
     return CLBM_OK;
 }
@@ -382,6 +427,8 @@ int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0
     a.n = n;
     a.hist_cap = kHistCap;
     auto bail = [&](int rc) { ibm_destroy(ibm); return rc; };
+    if (cudaEventCreateWithFlags(&ibm->ev_box, cudaEventDisableTiming) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "ibm_create: event creation failed"));
     const size_t nb = (size_t)(n > 0 ? n : 1) * sizeof(float);
     float** marr[] = {(float**)&a.X0, (float**)&a.Y0, (float**)&a.Z0, &a.X, &a.Y, &a.Z,
                       &a.VX, &a.VY, &a.Uk, &a.Vk, &a.FXk, &a.FYk};
@@ -446,6 +493,7 @@ int ibm_destroy(clbm_ibm* ibm) {
                     a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist, a.part};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (ibm->ev_box) cudaEventDestroy(ibm->ev_box);
     delete ibm;
     return CLBM_OK;
 }
@@ -585,6 +633,7 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
         while (nsteps - done >= 2) {
             CK(cudaGraphLaunch(s->gexec, s->st));
             done += 2;
+            s->version += 2;
             s->launches += 2 * per;
             if (ibm) ibm->calls += 2;
         }

@@ -57,6 +57,9 @@ constexpr int kBoxEmpty = 0x7f7f7f7f;
 
 struct IbmDev {
     long long step;        // number of completed compute_force calls
+    long long cur;         // index of the call whose box the next fused step uses; written by
+                           // the marker kernel, so a bulk pass that starts before the
+                           // force-sum kernel has advanced `step` still finds the right box
     int box[2][6];         // slot (call index & 1): imin, -imax, jmin, -jmax, kmin, -kmax
     unsigned int ticket;   // last-block detection of the force-sum kernel
     int pad;
@@ -96,6 +99,18 @@ __device__ inline bool in_band(const Band& b, int x, int y, int z, int ny, int n
     int oy = y - b.j0; if (oy < 0) oy += ny;
     int oz = z - b.k0; if (oz < 0) oz += nz;
     return (unsigned)(x - b.i0) < (unsigned)b.ilen && oy < b.jlen && oz < b.klen;
+}
+
+// Cell t (0 <= t < ilen * jlen * klen) of a band box, x fastest.
+__device__ __forceinline__ void box_cell(const Band& b, int ny, int nz, int t, int& x, int& y,
+                                         int& z) {
+    const int ox = t % b.ilen;
+    const int r = t / b.ilen;
+    x = b.i0 + ox;
+    y = b.j0 + r % b.jlen;
+    if (y >= ny) y -= ny;
+    z = b.k0 + r / b.jlen;
+    if (z >= nz) z -= nz;
 }
 
 // Peskin 4-point regularised delta, airfoil_moving.py:27-38, same operation order.
@@ -144,7 +159,9 @@ inline size_t store_bytes(int storage) { return storage == CLBM_STORE_F32 ? 4 : 
 
 // ---------------------------------------------------------------- launchers
 // Force source of the fused step.
-enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2 };
+// kForceSkipBand: bulk pass of an IBM step that leaves the cells of the force box to
+// launch_stream_collide_box, so the bulk can run while the IBM kernels compute the forces.
+enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2, kForceSkipBand = 3 };
 
 // IBM force fields are accumulated in 64-bit fixed point with kForceScale units per unit
 // force: integer atomics are associative, so spreading is deterministic, and a float32
@@ -166,6 +183,11 @@ struct ForceArgs {
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
 void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
                            const Grid& g, const Coef& c, const ForceArgs& fa, cudaStream_t st);
+// Forced stream-collide of the cells of the current IBM force box; max_cells bounds the
+// box size (grid sizing only).
+void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
+                               const Grid& g, const Coef& c, const ForceArgs& fa,
+                               long long max_cells, cudaStream_t st);
 // Macro (rho, u without force) of the current state for every cell of the grid; optional
 // statistics into stats[0..3] (ordered-int min rho, max rho, max |u|^2, nonfinite count).
 void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,

@@ -28,22 +28,31 @@ template <bool DEVM>
 __global__ void __launch_bounds__(kMarkerBlock) k_ibm_markers(IbmArrays a, Grid g, MotionF mf,
                                                               clbm_motion m) {
     __shared__ int sbox[kMarkerBlock / 32][6];
+    __shared__ float smot[8];
     const long long s = a.dev->step + 1;
-    float xc, yc, theta, vx, vy, omega;
-    if (DEVM) {
-        // _motion_state(step), main_moving.py:65-74, in double, then the float32
-        // truncation of the kernel arguments (airfoil_moving.py:101-103).
-        const double t = (double)s, w = m.w;
-        xc = (float)m.x0;
-        yc = (float)(m.y0 + m.a_heave * sin(w * t));
-        theta = (float)(m.aoa0 + m.a_pitch * sin(w * t + m.phi_pitch));
-        vx = 0.0f;
-        vy = (float)(m.a_heave * w * cos(w * t));
-        omega = (float)(m.a_pitch * w * cos(w * t + m.phi_pitch));
-    } else {
-        xc = mf.xc; yc = mf.yc; theta = mf.theta; vx = mf.vx; vy = mf.vy; omega = mf.omega;
+    if (threadIdx.x == 0) {
+        if (blockIdx.x == 0) a.dev->cur = s;
+        MotionF v = mf;
+        if (DEVM) {
+            // _motion_state(step), main_moving.py:65-74, in double, then the float32
+            // truncation of the kernel arguments (airfoil_moving.py:101-103). One thread per
+            // block: double-precision sin/cos are slow on this part.
+            const double t = (double)s, w = m.w;
+            v.xc = (float)m.x0;
+            v.yc = (float)(m.y0 + m.a_heave * sin(w * t));
+            v.theta = (float)(m.aoa0 + m.a_pitch * sin(w * t + m.phi_pitch));
+            v.vx = 0.0f;
+            v.vy = (float)(m.a_heave * w * cos(w * t));
+            v.omega = (float)(m.a_pitch * w * cos(w * t + m.phi_pitch));
+        }
+        smot[0] = v.xc; smot[1] = v.yc; smot[2] = v.theta;
+        smot[3] = v.vx; smot[4] = v.vy; smot[5] = v.omega;
+        smot[6] = cosf(v.theta);
+        smot[7] = sinf(v.theta);
     }
-    const float cos_t = cosf(theta), sin_t = sinf(theta);
+    __syncthreads();
+    const float xc = smot[0], yc = smot[1], vx = smot[3], vy = smot[4], omega = smot[5];
+    const float cos_t = smot[6], sin_t = smot[7];
     int b[6] = {kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty};
     const int i = blockIdx.x * kMarkerBlock + threadIdx.x;
     if (i < a.n) {
@@ -145,19 +154,17 @@ __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g
     IbmDev* dev = a.dev;
     const long long s = dev->step + 1;
     const Band b = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
-    const long long cells = (long long)b.ilen * b.jlen * b.klen;
-    const long long stride = (long long)gridDim.x * kFinishBlock;
+    const int cells = b.ilen * b.jlen * b.klen;
+    const int stride = gridDim.x * kFinishBlock;
     double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;
-    for (long long t = (long long)blockIdx.x * kFinishBlock + threadIdx.x; t < cells; t += stride) {
-        const int ox = (int)(t % b.ilen);
-        const long long r = t / b.ilen;
-        const int oy = (int)(r % b.jlen), oz = (int)(r / b.jlen);
-        const int x = b.i0 + ox, y = pmod(b.j0 + oy, g.ny), z = pmod(b.k0 + oz, g.nz);
+    for (int t = blockIdx.x * kFinishBlock + threadIdx.x; t < cells; t += stride) {
+        int x, y, z;
+        box_cell(b, g.ny, g.nz, t, x, y, z);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
         sx += (double)fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f);
         sy += (double)fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f);
     }
-    for (long long t = (long long)blockIdx.x * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
+    for (int t = blockIdx.x * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
         mx += (double)a.FXk[t];
         my += (double)a.FYk[t];
     }
@@ -179,15 +186,24 @@ __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g
         last = (tk == gridDim.x - 1);
     }
     __syncthreads();
-    if (last && threadIdx.x < 4) {
-        __threadfence();
-        const volatile double* p = a.part;
-        double v = 0.0;
-        for (unsigned int blk = 0; blk < gridDim.x; ++blk) v += p[4 * blk + threadIdx.x];
-        a.hist[4 * ((s - 1) % a.hist_cap) + threadIdx.x] = v;
-    }
+    if (!last) return;
+    // Final sum in a fixed order: thread t takes partial blocks t, t + 256, ... (loads in
+    // parallel), then the same shuffle/shared-memory tree as above.
+    __threadfence();
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (unsigned int blk = threadIdx.x; blk < gridDim.x; blk += kFinishBlock)
+        for (int e = 0; e < 4; ++e) v[e] += __ldcg(a.part + 4 * blk + e);
+    for (int e = 0; e < 4; ++e) v[e] = warp_sum(v[e]);
     __syncthreads();
-    if (last && threadIdx.x == 0) {
+    if (lane == 0)
+        for (int e = 0; e < 4; ++e) red[warp][e] = v[e];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < kFinishBlock / 32; ++w) t += red[w][threadIdx.x];
+        a.hist[4 * ((s - 1) % a.hist_cap) + threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) {
         dev->ticket = 0u;
         // the previous call's box was consumed by this call's band-prepare
         for (int e = 0; e < 6; ++e) dev->box[(s + 1) & 1][e] = kBoxEmpty;

@@ -16,6 +16,8 @@
 //   5. stores f_post for the next step, coalesced and with streaming stores.
 // Algorithmic traffic: 19 loads + 19 stores per cell (152 B/cell float32, 76 B/cell for
 // the 16-bit shifted forms); the force fields add 8 B per cell inside the IBM band only.
+#include <algorithm>
+
 #include "clbm_internal.cuh"
 
 namespace clbm {
@@ -184,17 +186,21 @@ __global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T
     const int x = blockIdx.x * kBX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= g.nx) return;
+    if (FMODE == kForceSkipBand) {
+        // bulk pass of an IBM step: the cells of the force box are done by k_stream_collide_box
+        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        if (in_band(b, x, y, z, g.ny, g.nz)) return;
+    }
     float f[19];
     gather<S, PULL>(fin, g, c, x, y, z, f);
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-    if (FMODE == kForceNone) {
+    if (FMODE == kForceNone || FMODE == kForceSkipBand) {
         collide<false>(f, c, 0.f, 0.f, 0.f);
     } else if (FMODE == kForceDense) {
         const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
         collide<true>(f, c, fa.fx[cell], fa.fy[cell], Fz);
     } else {
-        const long long step = fa.dev->step;
-        const Band b = band_from_box(fa.dev->box[step & 1], g.nx, g.ny, g.nz);
+        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
         if (in_band(b, x, y, z, g.ny, g.nz)) {
             // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
             // fz is always zero there.
@@ -208,6 +214,27 @@ __global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T
     using P = Pop<S>;
 #pragma unroll
     for (int q = 0; q < 19; ++q) P::st(fout + q * g.plane + cell, q, f[q]);
+}
+
+// Forced pass over the cells of the IBM force box (the complement of the bulk pass).
+template <int S, bool PULL>
+__global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S>::T* __restrict__ fin,
+                                                            typename Pop<S>::T* __restrict__ fout,
+                                                            Grid g, Coef c, ForceArgs fa) {
+    const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+    const int cells = b.ilen * b.jlen * b.klen;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells; t += gridDim.x * blockDim.x) {
+        int x, y, z;
+        box_cell(b, g.ny, g.nz, t, x, y, z);
+        float f[19];
+        gather<S, PULL>(fin, g, c, x, y, z, f);
+        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
+        const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+        collide<true>(f, c, Fx, Fy, 0.0f);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) Pop<S>::st(fout + q * g.plane + cell, q, f[q]);
+    }
 }
 
 template <int S>
@@ -386,6 +413,8 @@ static void sc_launch(int fmode, const void* fin, void* fout, const Grid& g, con
         k_stream_collide<S, PULL, kForceNone><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else if (fmode == kForceBand)
         k_stream_collide<S, PULL, kForceBand><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceSkipBand)
+        k_stream_collide<S, PULL, kForceSkipBand><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else
         k_stream_collide<S, PULL, kForceDense><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
 }
@@ -395,6 +424,22 @@ void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, v
     CLBM_DISPATCH_STORE(storage, {
         if (pull) sc_launch<S_, true>(fmode, fin, fout, g, c, fa, st);
         else sc_launch<S_, false>(fmode, fin, fout, g, c, fa, st);
+    });
+}
+
+static int box_blocks(long long max_cells, int block) {
+    const long long b = (max_cells + block - 1) / block;
+    return (int)std::max<long long>(1, std::min<long long>(b, 4 * 152));
+}
+
+void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
+                               const Grid& g, const Coef& c, const ForceArgs& fa,
+                               long long max_cells, cudaStream_t st) {
+    const int blocks = box_blocks(max_cells, 256);
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        if (pull) k_stream_collide_box<S_, true><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        else k_stream_collide_box<S_, false><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     });
 }
 
@@ -456,19 +501,22 @@ __global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid 
     const long long s = dev->step + 1;
     const Band nb = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
     const Band ob = band_from_box(dev->box[(s - 1) & 1], g.nx, g.ny, g.nz);
-    const int ox = blockIdx.x * blockDim.x + threadIdx.x;
-    const int oy = blockIdx.y * blockDim.y + threadIdx.y;
-    const int oz = blockIdx.z;
+    const int stride = gridDim.x * blockDim.x;
     // _zero_forces (airfoil_moving.py:132-137) restricted to where the previous call spread
-    if (ox < ob.ilen && oy < ob.jlen && oz < ob.klen) {
-        const int x = ob.i0 + ox, y = pmod(ob.j0 + oy, g.ny), z = pmod(ob.k0 + oz, g.nz);
+    const int ocells = ob.ilen * ob.jlen * ob.klen;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ocells; t += stride) {
+        int x, y, z;
+        box_cell(ob, g.ny, g.nz, t, x, y, z);
         const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
         fx[cell] = 0;
         fy[cell] = 0;
     }
+    if (!compute_macro) return;
     // _macro_post of the current state on the cells the stencils of this call touch
-    if (compute_macro && ox < nb.ilen && oy < nb.jlen && oz < nb.klen) {
-        const int x = nb.i0 + ox, y = pmod(nb.j0 + oy, g.ny), z = pmod(nb.k0 + oz, g.nz);
+    const int ncells = nb.ilen * nb.jlen * nb.klen;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ncells; t += stride) {
+        int x, y, z;
+        box_cell(nb, g.ny, g.nz, t, x, y, z);
         float f[19];
         gather<S, PULL>(fin, g, c, x, y, z, f);
         float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
@@ -491,12 +539,11 @@ void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, c
                          IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
                          cudaStream_t st) {
-    dim3 block(32, 4, 1);
-    dim3 grid((max_bx + 31) / 32, (max_by + 3) / 4, max_bz);
+    const int blocks = box_blocks((long long)max_bx * max_by * max_bz, 256);
     CLBM_DISPATCH_STORE(storage, {
         using T = typename Pop<S_>::T;
-        if (pull) k_band_prepare<S_, true><<<grid, block, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
-        else k_band_prepare<S_, false><<<grid, block, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+        if (pull) k_band_prepare<S_, true><<<blocks, 256, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+        else k_band_prepare<S_, false><<<blocks, 256, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
     });
 }
 
