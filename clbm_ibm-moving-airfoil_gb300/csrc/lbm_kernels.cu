@@ -22,6 +22,22 @@
 
 namespace clbm {
 
+// 3D Zou-He velocity inlet on the post-stream populations of an x = 0 cell,
+// clbm_moving.py:266-294 (same operation order).
+__device__ __forceinline__ void zou_he(float (&v)[19], const Coef& c) {
+    const float ux_in = c.ux_in, uy_in = c.uy_in;
+    float S_known = v[0] + v[3] + v[4] + v[5] + v[6] + v[15] + v[16] + v[17] + v[18];
+    float S_out = v[2] + v[8] + v[10] + v[12] + v[14];
+    float rho_in = (S_known + 2.0f * S_out) / (1.0f - ux_in);
+    float diff_y = v[3] - v[4];
+    float diff_z = v[5] - v[6];
+    v[1] = v[2] + c.c23 * rho_in * ux_in;
+    v[7] = v[10] + c.c16 * rho_in * ux_in + 0.5f * rho_in * uy_in - 0.5f * diff_y;
+    v[9] = v[8] + c.c16 * rho_in * ux_in - 0.5f * rho_in * uy_in + 0.5f * diff_y;
+    v[11] = v[14] + c.c16 * rho_in * ux_in - 0.5f * diff_z;
+    v[13] = v[12] + c.c16 * rho_in * ux_in + 0.5f * diff_z;
+}
+
 // Gather the post-stream, post-boundary populations S(x, y, z) of the stored state.
 // pull = false: the stored array already is a post-stream state (after initialisation or
 // an import), read in place.
@@ -51,20 +67,7 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
             v[q] = P::ld(f + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + sx, q);
         }
     }
-    if (xe == 0) {
-        // 3D Zou-He velocity inlet, clbm_moving.py:266-294 (same operation order)
-        const float ux_in = c.ux_in, uy_in = c.uy_in;
-        float S_known = v[0] + v[3] + v[4] + v[5] + v[6] + v[15] + v[16] + v[17] + v[18];
-        float S_out = v[2] + v[8] + v[10] + v[12] + v[14];
-        float rho_in = (S_known + 2.0f * S_out) / (1.0f - ux_in);
-        float diff_y = v[3] - v[4];
-        float diff_z = v[5] - v[6];
-        v[1] = v[2] + c.c23 * rho_in * ux_in;
-        v[7] = v[10] + c.c16 * rho_in * ux_in + 0.5f * rho_in * uy_in - 0.5f * diff_y;
-        v[9] = v[8] + c.c16 * rho_in * ux_in - 0.5f * rho_in * uy_in + 0.5f * diff_y;
-        v[11] = v[14] + c.c16 * rho_in * ux_in - 0.5f * diff_z;
-        v[13] = v[12] + c.c16 * rho_in * ux_in + 0.5f * diff_z;
-    }
+    if (xe == 0) zou_he(v, c);
 }
 
 // Zeroth, first and second raw moments of a population vector.
@@ -92,12 +95,24 @@ __device__ __forceinline__ Moments moments(const float (&f)[19]) {
 
 // Cascaded collision in central-moment space followed by the raw-moment back transform,
 // in place on f. (Fx, Fy, Fz) is the body-force density at the cell.
-template <bool FORCE>
+// DEV: f holds deviations h = f - w (shifted storage) on input and output. Moments of the
+// weights are added to the zeroth and second moments (sum w = 1, sum w e_a e_b = d_ab / 3)
+// and subtracted again from the raw post-collision moments before the back transform
+// (sum w = 1, sum w e_a^2 = 1/3, sum w e_a^2 e_b^2 = 1/9; all other moments of w vanish),
+// so no per-population shift is needed.
+template <bool FORCE, bool DEV = false>
 __device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx, float Fy,
                                         float Fz) {
-    const Moments m = moments(f);
+    Moments m = moments(f);
+    const float drho = m.rho;
+    if (DEV) {
+        m.rho += 1.0f;
+        m.pxx += 1.0f / 3.0f;
+        m.pyy += 1.0f / 3.0f;
+        m.pzz += 1.0f / 3.0f;
+    }
     const float r = m.rho;
-    const float inv = 1.0f / r;
+    const float inv = __frcp_rn(r);
     float u = m.mx * inv, v = m.my * inv, w = m.mz * inv;
     if (FORCE) {
         u += 0.5f * Fx * inv;
@@ -119,12 +134,13 @@ __device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx,
     const float k200s = (kAs + kDs + kEs) * (1.0f / 3.0f);
     const float k020s = (kAs - 2.0f * kDs + kEs) * (1.0f / 3.0f);
     const float k002s = (kAs + kDs - 2.0f * kEs) * (1.0f / 3.0f);
-    const float r9 = r * (1.0f / 9.0f);
+    // fourth-order equilibrium r/9; its weight part 1/9 is removed here in the shifted form
+    const float r9 = (DEV ? drho : r) * (1.0f / 9.0f);
     // raw post-collision moments (third-order central moments relax to 0, fourth to r/9)
     const float ur = u * r, vr = v * r, wr = w * r;
     const float uu = u * u, vv = v * v, ww = w * w;
     const float T110 = k110s + u * vr, T101 = k101s + u * wr, T011 = k011s + v * wr;
-    const float T200 = k200s + u * ur, T020 = k020s + v * vr, T002 = k002s + w * wr;
+    float T200 = k200s + u * ur, T020 = k020s + v * vr, T002 = k002s + w * wr;
     const float T210 = 2.0f * u * k110s + v * k200s + uu * vr;
     const float T120 = 2.0f * v * k110s + u * k020s + vv * ur;
     const float T201 = 2.0f * u * k101s + w * k200s + uu * wr;
@@ -134,8 +150,11 @@ __device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx,
     const float T220 = r9 + 4.0f * u * v * k110s + vv * k200s + uu * k020s + uu * vv * r;
     const float T202 = r9 + 4.0f * u * w * k101s + ww * k200s + uu * k002s + uu * ww * r;
     const float T022 = r9 + 4.0f * v * w * k011s + ww * k020s + vv * k002s + vv * ww * r;
+    if (DEV) {
+        T200 -= 1.0f / 3.0f; T020 -= 1.0f / 3.0f; T002 -= 1.0f / 3.0f;
+    }
     // closed form of M_raw^-1 (config_moving.py:62-73)
-    f[0] = r - (T200 + T020 + T002) + (T220 + T202 + T022);
+    f[0] = (DEV ? drho : r) - (T200 + T020 + T002) + (T220 + T202 + T022);
     const float A1 = 0.5f * (T200 - T220 - T202), B1 = 0.5f * (ur - T120 - T102);
     const float A2 = 0.5f * (T020 - T220 - T022), B2 = 0.5f * (vr - T210 - T012);
     const float A3 = 0.5f * (T002 - T202 - T022), B3 = 0.5f * (wr - T201 - T021);
@@ -234,6 +253,171 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
         collide<true>(f, c, Fx, Fy, 0.0f);
 #pragma unroll
         for (int q = 0; q < 19; ++q) Pop<S>::st(fout + q * g.plane + cell, q, f[q]);
+    }
+}
+
+// ------------------------------------------------------------------ 16-bit pair kernel
+// Shifted 16-bit storage moves half the bytes of float32, so the one-cell kernel becomes
+// issue-bound. This variant gives each thread two neighbouring cells (x0, x0 + 1), x0 even:
+// every population is one aligned 32-bit load/store of a half2 (or bf16x2); the x-shifted
+// pulls take the neighbour element from the adjacent lane with a warp shuffle (the lanes at
+// the two warp edges load that one element themselves); the collision works on the
+// deviations directly (collide<.., DEV = true>).
+template <int S> struct Pair;
+template <> struct Pair<CLBM_STORE_F16S> {
+    using T = __half;
+    static __device__ __forceinline__ float2 ld2(const T* p) {
+        return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    }
+    static __device__ __forceinline__ float ld1(const T* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) {
+        const __half2 h = __floats2half2_rn(a, b);
+        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+    }
+    static __device__ __forceinline__ void st1(T* p, float a) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(a)));
+    }
+};
+template <> struct Pair<CLBM_STORE_BF16S> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ float2 ld2(const T* p) {
+        return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)));
+    }
+    static __device__ __forceinline__ float ld1(const T* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+    }
+    static __device__ __forceinline__ void st1(T* p, float a) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __bfloat16_as_ushort(__float2bfloat16_rn(a)));
+    }
+};
+
+constexpr int kPX = 128;  // threads per block of the pair kernel (256 cells along x)
+
+template <int S, bool PULL, int FMODE>
+__global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
+                                                             typename Pair<S>::T* __restrict__ fout,
+                                                             Grid g, Coef c, ForceArgs fa) {
+    using P = Pair<S>;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int x0 = 2 * (blockIdx.x * kPX + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    const int lane = threadIdx.x & 31;
+    const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
+    bool in0 = false, in1 = false;
+    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
+        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
+        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
+    }
+    const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
+    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
+    // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
+    if (__all_sync(kFull, !use0 && !use1)) return;
+    const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
+    const long long row = ((long long)z * g.ny + y) * g.pitch;
+    float h0[19], h1[19];
+    if (!PULL) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const float2 p = P::ld2(fin + q * g.plane + row + x0c);
+            h0[q] = p.x;
+            h1[q] = p.y;
+        }
+    } else {
+        const int ym = (y == 0) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1) ? 0 : z + 1;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+            const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+            const typename P::T* rp = fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch;
+            const float2 p = P::ld2(rp + x0c);
+            if (ex(q) == 0) {
+                h0[q] = p.x;
+                h1[q] = p.y;
+            } else if (ex(q) == 1) {  // pull from x - 1
+                float up = __shfl_up_sync(kFull, p.y, 1);
+                if (lane == 0) up = (x0 >= 1 && x0 - 1 < g.nx) ? P::ld1(rp + (x0 - 1)) : 0.0f;
+                h0[q] = up;   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
+                h1[q] = p.x;
+            } else {                  // pull from x + 1
+                float dn = __shfl_down_sync(kFull, p.x, 1);
+                if (lane == 31) dn = (x0 + 2 < g.nx) ? P::ld1(rp + (x0 + 2)) : 0.0f;
+                h0[q] = p.y;
+                h1[q] = dn;
+            }
+        }
+        if (x0 == 0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h0[q] += wq(q);
+            zou_he(h0, c);
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h0[q] -= wq(q);
+        }
+        if (x0 + 1 == g.nx - 1) {
+            // outlet column Nx-1 is a copy of column Nx-2 = x0 (clbm_moving.py:296-300)
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h1[q] = h0[q];
+        } else if (x0 == g.nx - 1) {
+            // odd Nx: the outlet is the first cell of the last pair; pull like column Nx-2
+            const int xe = g.nx - 2;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+                const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+                h0[q] = P::ld1(fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + (xe - ex(q)));
+            }
+        }
+    }
+    // body force per cell
+    float F0x = 0.f, F0y = 0.f, F0z = 0.f, F1x = 0.f, F1y = 0.f, F1z = 0.f;
+    bool frc0 = false, frc1 = false;
+    if (FMODE == kForceBand) {
+        frc0 = in0;
+        frc1 = in1;
+        if (in0) {
+            F0x = fminf(fmaxf(qforce(fa.qx[row + x0]), -0.05f), 0.05f);
+            F0y = fminf(fmaxf(qforce(fa.qy[row + x0]), -0.05f), 0.05f);
+        }
+        if (in1) {
+            F1x = fminf(fmaxf(qforce(fa.qx[row + x0 + 1]), -0.05f), 0.05f);
+            F1y = fminf(fmaxf(qforce(fa.qy[row + x0 + 1]), -0.05f), 0.05f);
+        }
+    } else if (FMODE == kForceDense) {
+        frc0 = act0;
+        frc1 = act1;
+        if (act0) {
+            F0x = fa.fx[row + x0]; F0y = fa.fy[row + x0]; F0z = fa.fz ? fa.fz[row + x0] : 0.f;
+        }
+        if (act1) {
+            F1x = fa.fx[row + x0 + 1]; F1y = fa.fy[row + x0 + 1];
+            F1z = fa.fz ? fa.fz[row + x0 + 1] : 0.f;
+        }
+    }
+    if (use0) {
+        if (frc0) collide<true, true>(h0, c, F0x, F0y, F0z);
+        else collide<false, true>(h0, c, 0.f, 0.f, 0.f);
+    }
+    if (use1) {
+        if (frc1) collide<true, true>(h1, c, F1x, F1y, F1z);
+        else collide<false, true>(h1, c, 0.f, 0.f, 0.f);
+    }
+    if (use0 && use1) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) P::st2(fout + q * g.plane + row + x0, h0[q], h1[q]);
+    } else {
+        if (use0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0, h0[q]);
+        }
+        if (use1) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0 + 1, h1[q]);
+        }
     }
 }
 
@@ -409,6 +593,18 @@ template <int S, bool PULL>
 static void sc_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
                       const ForceArgs& fa, cudaStream_t st) {
     using T = typename Pop<S>::T;
+    if constexpr (S != CLBM_STORE_F32) {
+        const dim3 grid((g.nx + 2 * kPX - 1) / (2 * kPX), g.ny, g.nz);
+        if (fmode == kForceNone)
+            k_stream_collide_pair<S, PULL, kForceNone><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        else if (fmode == kForceBand)
+            k_stream_collide_pair<S, PULL, kForceBand><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        else if (fmode == kForceSkipBand)
+            k_stream_collide_pair<S, PULL, kForceSkipBand><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        else
+            k_stream_collide_pair<S, PULL, kForceDense><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        return;
+    }
     if (fmode == kForceNone)
         k_stream_collide<S, PULL, kForceNone><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else if (fmode == kForceBand)

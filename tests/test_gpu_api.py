@@ -117,6 +117,37 @@ def test_forces_persist_after_step_like_reference(gpkg):
     sim.close()
 
 
+W19 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+
+
+@pytest.mark.parametrize("storage,tol", [("f16", 5e-3), ("bf16", 4e-2)])
+@pytest.mark.parametrize("shape", [(37, 9, 5), (64, 6, 3), (3, 4, 2), (301, 5, 2), (258, 3, 3)])
+@pytest.mark.parametrize("forced", [False, True])
+def test_shifted_pair_kernel_edges(gpkg, oracle_mod, storage, tol, shape, forced):
+    """16-bit two-cells-per-thread kernel: odd and even Nx, rows shorter than a warp,
+    inlet and outlet columns, lane edges; deviations f - w against the FP64 oracle."""
+    rng = np.random.default_rng(11)
+    f = (W19 * (1.0 + 0.02 * rng.standard_normal(shape + (19,)))).astype(np.float32)
+    F = [(2e-4 * rng.standard_normal(shape)).astype(np.float32) for _ in range(3)]
+    s = gpkg.Solver(*shape, 1.45, 1.1, 0.04, 0.01, storage=storage)
+    o = oracle_mod.Oracle(*shape, 1.45, 1.1, 0.04, 0.01, [], [], [], real="f64")
+    s.write_populations(f)
+    o.set_f(f.astype(np.float64))
+    if forced:
+        o.set_forces(*F)
+    for _ in range(4):
+        if forced:
+            s.step_host_force(*F)
+        else:
+            s.step()
+        o.lbm_step()
+    got = s.read_populations().astype(np.float64) - W19
+    want = o.f() - W19
+    err = rel_l2(got, want)
+    assert err < tol, err
+    s.close()
+
+
 @pytest.mark.parametrize("storage,tol", [("f16", 2e-3), ("bf16", 2e-2)])
 def test_shifted_storage_error_against_fp64_oracle(gpkg, oracle_mod, storage, tol):
     """16-bit shifted populations f - w with float32 collision: field and lift/drag error
