@@ -267,6 +267,26 @@ def from_config_module(mod, storage="f32"):
     return cfg
 
 
+def stencil_box_cells(cfg, state):
+    """Cells of the box that bounds every 4x4x4 Peskin stencil for one motion state
+    (xc, yc, theta, ...), by the rule the marker kernel applies: stencil base floor(x) - 1,
+    x clamped to the lattice, y and z unwrapped and capped at Ny and Nz."""
+    if cfg.n_markers == 0:
+        return 0
+    xc, yc, th = (np.float32(v) for v in state[:3])
+    c, s = np.cos(th), np.sin(th)
+    x = xc + cfg.X0 * c - cfg.Y0 * s
+    y = yc + cfg.X0 * s + cfg.Y0 * c
+    ib = np.floor(x).astype(np.int64) - 1
+    jb = np.floor(y).astype(np.int64) - 1
+    kb = np.floor(cfg.Z0).astype(np.int64) - 1
+    imin = int(np.clip(ib.min(), 0, cfg.nx - 1))
+    imax = int(np.clip(ib.max() + 3, 0, cfg.nx - 1))
+    jl = min(int(jb.max() + 3 - jb.min() + 1), cfg.ny)
+    kl = min(int(kb.max() + 3 - kb.min() + 1), cfg.nz)
+    return (imax - imin + 1) * jl * kl
+
+
 def force_coefficients(sums, cfg):
     """Lift/drag coefficients from per-step force sums (rows: sum fx, sum fy of the clipped
     Eulerian force, sum FX_k, sum FY_k). The force on the body is minus the force injected

@@ -75,6 +75,7 @@ struct clbm_solver {
     // profiling of the fused kernel
     bool prof = false;
     std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_tag;  // per event pair: 0 bulk / plain pass, 1 box pass
     size_t ev_used = 0;
     // cached two-step graph of the time loop
     cudaGraphExec_t gexec = nullptr;
@@ -119,8 +120,11 @@ int record_event(clbm_solver* s, cudaStream_t st) {
 // One fused stream-collide launch on stream `st`, bracketed by timing events if profiling.
 int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bool box,
              long long box_cells) {
-    if (s->prof)
+    if (s->prof) {
         if (int rc = record_event(s, st)) return rc;
+        s->ev_tag.resize(s->ev_used / 2 + 1);
+        s->ev_tag[s->ev_used / 2] = box ? 1 : 0;
+    }
     if (box)
         launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
                                   s->c, fa, box_cells, st);
@@ -681,6 +685,26 @@ int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
     if (fused_ms) *fused_ms = ms;
     if (fused_launches) *fused_launches = (int64_t)(s->ev_used / 2);
     if (total_launches) *total_launches = s->launches;
+    return CLBM_OK;
+}
+
+int clbm_profile_read_split(clbm_solver* s, double* bulk_ms, int64_t* bulk_launches,
+                            double* box_ms, int64_t* box_launches) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_profile_read_split: null solver");
+    CK(cudaStreamSynchronize(s->st));
+    double ms[2] = {0.0, 0.0};
+    int64_t n[2] = {0, 0};
+    for (size_t i = 0; i + 1 < s->ev_used; i += 2) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, s->ev[i], s->ev[i + 1]));
+        const int tag = (i / 2 < s->ev_tag.size()) ? s->ev_tag[i / 2] : 0;
+        ms[tag] += t;
+        n[tag] += 1;
+    }
+    if (bulk_ms) *bulk_ms = ms[0];
+    if (bulk_launches) *bulk_launches = n[0];
+    if (box_ms) *box_ms = ms[1];
+    if (box_launches) *box_launches = n[1];
     return CLBM_OK;
 }
 

@@ -159,7 +159,12 @@ class Solver:
     def profile_read(self):
         ms, n, tot = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
         check(lib().clbm_profile_read(self._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(tot)))
-        return dict(fused_ms=ms.value, fused_launches=n.value, total_launches=tot.value)
+        bms, bn, xms, xn = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        check(lib().clbm_profile_read_split(self._h, ctypes.byref(bms), ctypes.byref(bn),
+                                            ctypes.byref(xms), ctypes.byref(xn)))
+        return dict(fused_ms=ms.value, fused_launches=n.value, total_launches=tot.value,
+                    bulk_ms=bms.value, bulk_launches=bn.value, box_ms=xms.value,
+                    box_launches=xn.value)
 
     def device_bytes(self):
         b = ctypes.c_int64()

@@ -137,6 +137,11 @@ int clbm_stream(const clbm_solver* s, void** out);
 int clbm_profile_enable(clbm_solver* s, int32_t on);
 int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
                       int64_t* total_launches);
+/* The same device time split by pass: an IBM step launches a bulk pass over the cells
+ * outside the force box and a box pass over the cells inside it; other steps count as
+ * bulk. */
+int clbm_profile_read_split(clbm_solver* s, double* bulk_ms, int64_t* bulk_launches,
+                            double* box_ms, int64_t* box_launches);
 
 /* Bytes of device memory owned by the solver (populations, macro fields). */
 int clbm_device_bytes(const clbm_solver* s, int64_t* out);
