@@ -23,7 +23,7 @@ EXPORTED = (
     "clbm_read_populations", "clbm_write_populations", "clbm_check", "ibm_create",
     "ibm_destroy", "ibm_compute_force", "ibm_compute_force_motion", "ibm_read_forces",
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
-    "clbm_synchronize", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
+    "clbm_synchronize", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error",
 )
@@ -95,6 +95,7 @@ def lib():
             "clbm_run": [vp, vp, ctypes.POINTER(Motion), i32, i32],
             "clbm_synchronize": [vp],
             "clbm_stream": [vp, pvp],
+            "clbm_selftest_wait_timeout": [vp, i32],
             "clbm_profile_enable": [vp, i32],
             "clbm_profile_read": [vp, ctypes.POINTER(d), ctypes.POINTER(i64), ctypes.POINTER(i64)],
             "clbm_profile_read_split": [vp, ctypes.POINTER(d), ctypes.POINTER(i64),

@@ -72,6 +72,8 @@ struct clbm_solver {
     cudaEvent_t ev_fork = nullptr; // fork point of a bulk pass without a fresh box event
     long long version = 0;         // bumped whenever f[cur] changes
     long long launches = 0;
+    int variant = kVariantStaged;  // full-grid stream-collide kernel (chosen at create)
+    unsigned int* status = nullptr;
     // profiling of the fused kernel
     bool prof = false;
     std::vector<cudaEvent_t> ev;
@@ -129,8 +131,8 @@ int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bo
         launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
                                   s->c, fa, box_cells, st);
     else
-        launch_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur],
-                              s->g, s->c, fa, st);
+        launch_stream_collide(s->cfg.storage, !s->local, fmode, s->variant, s->f[s->cur],
+                              s->f[1 - s->cur], s->g, s->c, fa, st);
     CK_LAUNCH();
     if (s->prof)
         if (int rc = record_event(s, st)) return rc;
@@ -182,6 +184,47 @@ int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motio
     return CLBM_OK;
 }
 
+// Full-grid kernel variant: CLBM_KERNEL=cell|pair|staged forces one; otherwise lattices of
+// at least 2^20 cells time each candidate (three launches after one warm-up, on the
+// not-yet-initialised buffers) and keep the fastest; smaller lattices use the staged one.
+int pick_variant(clbm_solver* s) {
+    const bool half = s->cfg.storage != CLBM_STORE_F32;
+    if (const char* env = std::getenv("CLBM_KERNEL")) {
+        if (!std::strcmp(env, "cell")) return kVariantCell;
+        if (!std::strcmp(env, "pair") && half) return kVariantPair;
+        if (!std::strcmp(env, "staged")) return kVariantStaged;
+    }
+    const long long n = (long long)s->g.nx * s->g.ny * s->g.nz;
+    if (n < (1LL << 20)) return kVariantStaged;
+    std::vector<int> cand = {kVariantStaged, kVariantCell};
+    if (half) cand.push_back(kVariantPair);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return kVariantStaged;
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return kVariantStaged; }
+    int best = kVariantStaged;
+    float best_ms = 1e30f;
+    for (int v : cand) {
+        ForceArgs fa{};
+        launch_stream_collide(s->cfg.storage, true, kForceNone, v, s->f[0], s->f[1], s->g, s->c, fa, s->st);
+        cudaEventRecord(e0, s->st);
+        for (int k = 0; k < 3; ++k)
+            launch_stream_collide(s->cfg.storage, true, kForceNone, v, s->f[k & 1], s->f[1 - (k & 1)],
+                                  s->g, s->c, fa, s->st);
+        cudaEventRecord(e1, s->st);
+        float ms = 0.f;
+        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+            ms < best_ms) {
+            best_ms = ms;
+            best = v;
+        }
+        s->launches += 4;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+    return best;
+}
+
 void free_graph(clbm_solver* s) {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     s->gexec = nullptr;
@@ -216,6 +259,9 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
     s->cfg = *cfg;
     s->g.nx = cfg->nx; s->g.ny = cfg->ny; s->g.nz = cfg->nz;
     s->g.pitch = (int)pitch; s->g.plane = plane;
+    s->g.seg = staged_segment(cfg->nx);
+    s->g.spin_limit = 1 << 22;
+    s->g.extra_tx = 0;
     s->c.one_m_sv = (float)(1.0 - cfg->s_v);
     s->c.s_e = (float)cfg->s_e;
     s->c.ux_in = (float)cfg->ux_in;
@@ -244,8 +290,12 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
             return bail(fail(CLBM_ERR_CUDA, "clbm_create: cudaMalloc of macro field failed"));
         cudaMemsetAsync(*p, 0, (size_t)plane * sizeof(float), s->st);
     }
-    if (cudaMalloc(&s->stats, 4 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMalloc(&s->stats, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&s->status, sizeof(unsigned int)) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "clbm_create: cudaMalloc failed"));
+    cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st);
+    s->g.status = s->status;
+    s->variant = pick_variant(s);
     launch_init(cfg->storage, s->f[0], s->g, s->c, s->st);
     launch_fill_macro(s->g, s->c, s->rho, s->ux, s->uy, s->uz, s->st);
     s->launches += 2;
@@ -267,7 +317,7 @@ int clbm_destroy(clbm_solver* s) {
     s->ibms.clear();
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
     void* ptrs[] = {s->f[0], s->f[1], s->rho, s->ux, s->uy, s->uz, s->dfx, s->dfy, s->dfz,
-                    s->stage, s->stats};
+                    s->stage, s->stats, s->status};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->st2) cudaStreamSynchronize(s->st2);
@@ -404,8 +454,13 @@ int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_ma
     int rc = materialize(s, true);
     if (rc) return rc;
     unsigned long long h[4];
+    unsigned int status = 0;
     CK(cudaMemcpyAsync(h, s->stats, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
+    if (status)
+        return fail(CLBM_ERR_STATE, "clbm_check: a device wait gave up (status %u); results of "
+                    "the affected steps are invalid", status);
     const bool any = h[0] != ~0ull;
     const double rmin = any ? from_ordered(h[0]) : NAN;
     const double rmax = any ? from_ordered(h[1]) : NAN;
@@ -654,8 +709,35 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
 
 int clbm_synchronize(clbm_solver* s) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_synchronize: null solver");
+    unsigned int status = 0;
+    CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
+    if (status)
+        return fail(CLBM_ERR_STATE, "clbm_synchronize: a device wait gave up (status %u)", status);
     return CLBM_OK;
+}
+
+int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit) {
+    // at least 1024 polls, so every block's copies have landed before it gives up and exits
+    if (!s || spin_limit < 1024)
+        return fail(CLBM_ERR_ARG, "clbm_selftest_wait_timeout: spin_limit must be >= 1024");
+    CK(cudaStreamSynchronize(s->st));
+    Grid g = s->g;
+    g.spin_limit = spin_limit;
+    g.extra_tx = 16;  // one more 16-byte chunk than is ever copied: every wait runs out
+    ForceArgs fa{};
+    launch_stream_collide(s->cfg.storage, !s->local, kForceNone, kVariantStaged, s->f[s->cur],
+                          s->f[1 - s->cur], g, s->c, fa, s->st);
+    CK_LAUNCH();
+    s->launches += 1;
+    unsigned int status = 0;
+    CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (status)
+        return fail(CLBM_ERR_STATE, "clbm_selftest_wait_timeout: bounded wait gave up as intended "
+                    "(status %u)", status);
+    return fail(CLBM_ERR_CUDA, "clbm_selftest_wait_timeout: the wait did not report a timeout");
 }
 
 int clbm_stream(const clbm_solver* s, void** out) {

@@ -39,8 +39,14 @@ __host__ __device__ constexpr float wq(int q) {
 
 struct Grid {
     int nx, ny, nz, pitch;
-    long long plane;  // pitch * ny * nz
+    long long plane;        // pitch * ny * nz
+    unsigned int* status;   // device status word: non-zero after a bounded wait gave up
+    int seg;                // cells per block along x of the staged stream-collide kernel
+    int spin_limit;         // polls of a bounded mbarrier wait before it gives up
+    int extra_tx;           // self test only: bytes a staged block expects beyond its copies
 };
+
+constexpr unsigned int kStatusWaitTimeout = 1u;
 
 // Collision and boundary constants, rounded to float once on the host.
 struct Coef {
@@ -181,8 +187,16 @@ struct ForceArgs {
 };
 
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
-void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
-                           const Grid& g, const Coef& c, const ForceArgs& fa, cudaStream_t st);
+// Stream-collide kernel variants for the full-grid pass:
+//   kVariantCell    one cell per thread, direct loads (float32 parity kernel)
+//   kVariantPair    two cells per thread, half2 loads, warp-shuffle x shifts (16-bit only)
+//   kVariantStaged  two cells per thread, rows staged in shared memory by bulk TMA copies
+enum Variant { kVariantCell = 0, kVariantPair = 1, kVariantStaged = 2 };
+void launch_stream_collide(int storage, bool pull, int fmode, int variant, const void* fin,
+                           void* fout, const Grid& g, const Coef& c, const ForceArgs& fa,
+                           cudaStream_t st);
+// Cells per block of the staged variant for a lattice width.
+int staged_segment(int nx);
 // Forced stream-collide of the cells of the current IBM force box; max_cells bounds the
 // box size (grid sizing only).
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,

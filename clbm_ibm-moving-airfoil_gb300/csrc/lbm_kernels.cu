@@ -421,6 +421,218 @@ __global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair
     }
 }
 
+// ------------------------------------------------------------------ TMA-staged kernel
+// Bulk stream-collide with the pulled rows staged in shared memory by the tensor memory
+// accelerator. A block owns `seg` cells of one (y, z) row. One thread issues, for each of
+// the 19 populations, a 1-D bulk copy (cp.async.bulk) of the source row of that population
+// (the row at y - e_y, z - e_z) over x in [xs - 8, xs + seg + 8), completing on one
+// mbarrier; every address and size is a multiple of 16 bytes (rows are padded to 32
+// elements, segments and halos are multiples of 8 elements). Each thread then computes two
+// neighbouring cells, reading the x-shifted populations from shared memory at constant
+// offsets, and stores its results directly (coalesced), so cells of the IBM force box can
+// be left to the box pass cell by cell.
+template <int S> struct Stg;
+template <> struct Stg<CLBM_STORE_F32> {
+    using T = float;
+    static constexpr bool kDev = false;
+    static __device__ __forceinline__ float2 lds2(const T* p) { return *reinterpret_cast<const float2*>(p); }
+    static __device__ __forceinline__ float lds1(const T* p) { return *p; }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) {
+        __stcs(reinterpret_cast<float2*>(p), make_float2(a, b));
+    }
+    static __device__ __forceinline__ void st1(T* p, float a) { __stcs(p, a); }
+};
+template <> struct Stg<CLBM_STORE_F16S> {
+    using T = __half;
+    static constexpr bool kDev = true;
+    static __device__ __forceinline__ float2 lds2(const T* p) {
+        return __half22float2(*reinterpret_cast<const __half2*>(p));
+    }
+    static __device__ __forceinline__ float lds1(const T* p) { return __half2float(*p); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) { Pair<CLBM_STORE_F16S>::st2(p, a, b); }
+    static __device__ __forceinline__ void st1(T* p, float a) { Pair<CLBM_STORE_F16S>::st1(p, a); }
+};
+template <> struct Stg<CLBM_STORE_BF16S> {
+    using T = __nv_bfloat16;
+    static constexpr bool kDev = true;
+    static __device__ __forceinline__ float2 lds2(const T* p) {
+        return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+    }
+    static __device__ __forceinline__ float lds1(const T* p) { return __bfloat162float(*p); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) { Pair<CLBM_STORE_BF16S>::st2(p, a, b); }
+    static __device__ __forceinline__ void st1(T* p, float a) { Pair<CLBM_STORE_BF16S>::st1(p, a); }
+};
+
+constexpr int kHalo = 8;                 // elements staged on each side of a segment
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+template <int S, bool PULL, int FMODE>
+__global__ void __launch_bounds__(256) k_stream_collide_tma(const typename Stg<S>::T* __restrict__ fin,
+                                                            typename Stg<S>::T* __restrict__ fout,
+                                                            Grid g, Coef c, ForceArgs fa) {
+    using P = Stg<S>;
+    using T = typename P::T;
+    constexpr bool DEV = P::kDev;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long mbar;
+    T* tile = reinterpret_cast<T*>(smem_raw);
+    const int ld = g.seg + 2 * kHalo;               // staged elements per population
+    const int xs = blockIdx.x * g.seg;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const int t = threadIdx.x;
+    const unsigned bar = smem_u32(&mbar);
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        const int xl = max(xs - kHalo, 0);
+        const int xr = min(xs + g.seg + kHalo, g.pitch);
+        const unsigned bytes = (unsigned)(xr - xl) * (unsigned)sizeof(T);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                     ::"r"(bar), "r"(bytes * 19u + (unsigned)g.extra_tx) : "memory");
+        const int ym = (y == 0) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1) ? 0 : z + 1;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const int sy = PULL ? (ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y)) : y;
+            const int sz = PULL ? (ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z)) : z;
+            const T* src = fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + xl;
+            const unsigned dst = smem_u32(tile + q * ld + (xl - (xs - kHalo)));
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+        }
+    }
+    __syncthreads();  // barrier initialised before anyone polls it
+    const int x0 = xs + 2 * t;
+    if (x0 >= g.nx || t * 2 >= g.seg) return;
+    const bool act1 = x0 + 1 < g.nx;
+    bool in0 = false, in1 = false;
+    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
+        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        in0 = in_band(b, x0, y, z, g.ny, g.nz);
+        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
+    }
+    const bool use0 = !(FMODE == kForceSkipBand && in0);
+    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
+    // bounded wait for the staged rows
+    unsigned done = 0;
+    for (int it = 0; it < g.spin_limit && !done; ++it) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done) : "r"(bar) : "memory");
+    }
+    if (!done) {
+        atomicOr(g.status, kStatusWaitTimeout);
+        return;
+    }
+    if (!use0 && !use1) return;
+    const int i0 = kHalo + 2 * t;  // staged index of cell x0
+    float h0[19], h1[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const T* r = tile + q * ld + i0;
+        if (!PULL || ex(q) == 0) {
+            const float2 p = P::lds2(r);
+            h0[q] = p.x;
+            h1[q] = p.y;
+        } else if (ex(q) == 1) {
+            h0[q] = P::lds1(r - 1);   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
+            h1[q] = P::lds1(r);
+        } else {
+            h0[q] = P::lds1(r + 1);
+            h1[q] = P::lds1(r + 2);
+        }
+    }
+    if (PULL) {
+        if (x0 == 0) {
+            if (DEV) {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) h0[q] += wq(q);
+            }
+            zou_he(h0, c);
+            if (DEV) {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) h0[q] -= wq(q);
+            }
+        }
+        if (x0 + 1 == g.nx - 1) {
+            // outlet column Nx-1 is a copy of column Nx-2 = x0 (clbm_moving.py:296-300)
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h1[q] = h0[q];
+        } else if (x0 == g.nx - 1) {
+            // odd Nx: the outlet is the first cell of the last pair; pull like column Nx-2
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h0[q] = P::lds1(tile + q * ld + i0 - 1 - ex(q));
+        }
+    }
+    const long long row = ((long long)z * g.ny + y) * g.pitch;
+    float F0x = 0.f, F0y = 0.f, F0z = 0.f, F1x = 0.f, F1y = 0.f, F1z = 0.f;
+    bool frc0 = false, frc1 = false;
+    if (FMODE == kForceBand) {
+        frc0 = in0;
+        frc1 = in1;
+        if (in0) {
+            F0x = fminf(fmaxf(qforce(fa.qx[row + x0]), -0.05f), 0.05f);
+            F0y = fminf(fmaxf(qforce(fa.qy[row + x0]), -0.05f), 0.05f);
+        }
+        if (in1) {
+            F1x = fminf(fmaxf(qforce(fa.qx[row + x0 + 1]), -0.05f), 0.05f);
+            F1y = fminf(fmaxf(qforce(fa.qy[row + x0 + 1]), -0.05f), 0.05f);
+        }
+    } else if (FMODE == kForceDense) {
+        frc0 = true;
+        frc1 = act1;
+        F0x = fa.fx[row + x0]; F0y = fa.fy[row + x0]; F0z = fa.fz ? fa.fz[row + x0] : 0.f;
+        if (act1) {
+            F1x = fa.fx[row + x0 + 1]; F1y = fa.fy[row + x0 + 1];
+            F1z = fa.fz ? fa.fz[row + x0 + 1] : 0.f;
+        }
+    }
+    if (use0) {
+        if (frc0) collide<true, DEV>(h0, c, F0x, F0y, F0z);
+        else collide<false, DEV>(h0, c, 0.f, 0.f, 0.f);
+    }
+    if (use1) {
+        if (frc1) collide<true, DEV>(h1, c, F1x, F1y, F1z);
+        else collide<false, DEV>(h1, c, 0.f, 0.f, 0.f);
+    }
+    T* o = fout + row + x0;
+    if (use0 && use1) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) P::st2(o + q * g.plane, h0[q], h1[q]);
+    } else {
+        if (use0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(o + q * g.plane, h0[q]);
+        }
+        if (use1) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(o + q * g.plane + 1, h1[q]);
+        }
+    }
+}
+
+// Threads per block (two cells each) of the staged kernel for a lattice width: the widest
+// block whose segments waste at most as many lanes as any narrower choice.
+int staged_segment(int nx) {
+    int best = 64, best_waste = 1 << 30;
+    for (int th = 64; th <= 256; th += 32) {
+        const int seg = 2 * th;
+        const int nseg = (nx + seg - 1) / seg;
+        const int waste = nseg * seg - nx;
+        if (waste <= best_waste) {
+            best_waste = waste;
+            best = seg;
+        }
+    }
+    return best;
+}
+
 template <int S>
 __global__ void k_init(typename Pop<S>::T* __restrict__ f, Grid g, Coef c) {
     const int x = blockIdx.x * kBX + threadIdx.x;
@@ -589,11 +801,27 @@ void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_
                                      (typename Pop<S_>::T*)f, g, c)));
 }
 
+template <int S, bool PULL, int FMODE>
+static void tma_launch(const void* fin, void* fout, const Grid& g, const Coef& c,
+                       const ForceArgs& fa, cudaStream_t st) {
+    using T = typename Stg<S>::T;
+    const dim3 grid((g.nx + g.seg - 1) / g.seg, g.ny, g.nz);
+    const size_t smem = (size_t)19 * (g.seg + 2 * kHalo) * sizeof(T);
+    k_stream_collide_tma<S, PULL, FMODE><<<grid, g.seg / 2, smem, st>>>((const T*)fin, (T*)fout, g, c, fa);
+}
+
 template <int S, bool PULL>
-static void sc_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
-                      const ForceArgs& fa, cudaStream_t st) {
+static void sc_launch(int fmode, int variant, const void* fin, void* fout, const Grid& g,
+                      const Coef& c, const ForceArgs& fa, cudaStream_t st) {
     using T = typename Pop<S>::T;
-    if constexpr (S != CLBM_STORE_F32) {
+    if (variant == kVariantStaged) {
+        if (fmode == kForceNone) tma_launch<S, PULL, kForceNone>(fin, fout, g, c, fa, st);
+        else if (fmode == kForceBand) tma_launch<S, PULL, kForceBand>(fin, fout, g, c, fa, st);
+        else if (fmode == kForceSkipBand) tma_launch<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, st);
+        else tma_launch<S, PULL, kForceDense>(fin, fout, g, c, fa, st);
+        return;
+    }
+    if constexpr (S != CLBM_STORE_F32) if (variant == kVariantPair) {
         const dim3 grid((g.nx + 2 * kPX - 1) / (2 * kPX), g.ny, g.nz);
         if (fmode == kForceNone)
             k_stream_collide_pair<S, PULL, kForceNone><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
@@ -615,11 +843,12 @@ static void sc_launch(int fmode, const void* fin, void* fout, const Grid& g, con
         k_stream_collide<S, PULL, kForceDense><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
 }
 
-void launch_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
-                           const Grid& g, const Coef& c, const ForceArgs& fa, cudaStream_t st) {
+void launch_stream_collide(int storage, bool pull, int fmode, int variant, const void* fin,
+                           void* fout, const Grid& g, const Coef& c, const ForceArgs& fa,
+                           cudaStream_t st) {
     CLBM_DISPATCH_STORE(storage, {
-        if (pull) sc_launch<S_, true>(fmode, fin, fout, g, c, fa, st);
-        else sc_launch<S_, false>(fmode, fin, fout, g, c, fa, st);
+        if (pull) sc_launch<S_, true>(fmode, variant, fin, fout, g, c, fa, st);
+        else sc_launch<S_, false>(fmode, variant, fin, fout, g, c, fa, st);
     });
 }
 

@@ -110,6 +110,16 @@ class Solver:
     def synchronize(self):
         check(lib().clbm_synchronize(self._h))
 
+    def selftest_wait_timeout(self, spin_limit=4096):
+        """Make one staged launch's bounded wait run out on purpose; returns the error the
+        library reports (a CLBMError with code CLBM_ERR_STATE is the expected outcome)."""
+        rc = lib().clbm_selftest_wait_timeout(self._h, int(spin_limit))
+        try:
+            check(rc)
+        except _lib.CLBMError as e:
+            return e
+        return None
+
     def stream_handle(self):
         """cudaStream_t of the solver as an integer (for torch.cuda.ExternalStream)."""
         p = ctypes.c_void_p()

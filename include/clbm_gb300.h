@@ -126,6 +126,14 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
 /* Wait for all queued work of the solver. */
 int clbm_synchronize(clbm_solver* s);
 
+/* Failure-detection self test (no counterpart in the reference, which has no device
+ * waits): runs one launch of the shared-memory-staged stream-collide kernel whose block
+ * barrier expects 16 bytes more than are ever copied, so each block's bounded wait gives
+ * up after `spin_limit` (>= 1024) polls and sets the device status word instead of hanging. Returns
+ * CLBM_ERR_STATE when the timeout was reported (the expected outcome), leaves the state
+ * unchanged (no block writes results) and clears the status word. */
+int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit);
+
 /* The solver's CUDA stream (cudaStream_t), for callers that record events or order their
  * own work against the solver. The stream stays owned by the solver. */
 int clbm_stream(const clbm_solver* s, void** out);

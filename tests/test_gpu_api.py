@@ -120,12 +120,21 @@ def test_forces_persist_after_step_like_reference(gpkg):
 W19 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
 
 
-@pytest.mark.parametrize("storage,tol", [("f16", 5e-3), ("bf16", 4e-2)])
-@pytest.mark.parametrize("shape", [(37, 9, 5), (64, 6, 3), (3, 4, 2), (301, 5, 2), (258, 3, 3)])
+@pytest.fixture
+def kernel_variant(request, monkeypatch):
+    """Force one full-grid stream-collide kernel variant for solvers made in the test."""
+    monkeypatch.setenv("CLBM_KERNEL", request.param)
+    return request.param
+
+
+@pytest.mark.parametrize("kernel_variant", ["cell", "pair", "staged"], indirect=True)
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-5), ("f16", 5e-3), ("bf16", 4e-2)])
+@pytest.mark.parametrize("shape", [(37, 9, 5), (64, 6, 3), (3, 4, 2), (301, 5, 2), (258, 3, 3),
+                                   (515, 3, 2)])
 @pytest.mark.parametrize("forced", [False, True])
-def test_shifted_pair_kernel_edges(gpkg, oracle_mod, storage, tol, shape, forced):
-    """16-bit two-cells-per-thread kernel: odd and even Nx, rows shorter than a warp,
-    inlet and outlet columns, lane edges; deviations f - w against the FP64 oracle."""
+def test_kernel_variants_edges(gpkg, oracle_mod, kernel_variant, storage, tol, shape, forced):
+    """Every stream-collide variant: odd and even Nx, rows shorter than a warp, segment and
+    lane edges, inlet and outlet columns; deviations f - w against the FP64 oracle."""
     rng = np.random.default_rng(11)
     f = (W19 * (1.0 + 0.02 * rng.standard_normal(shape + (19,)))).astype(np.float32)
     F = [(2e-4 * rng.standard_normal(shape)).astype(np.float32) for _ in range(3)]
@@ -145,6 +154,39 @@ def test_shifted_pair_kernel_edges(gpkg, oracle_mod, storage, tol, shape, forced
     want = o.f() - W19
     err = rel_l2(got, want)
     assert err < tol, err
+    s.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_staged_kernel_is_bitwise_equal_to_direct(gpkg, monkeypatch, storage):
+    """The staged (TMA) kernel and the direct-load kernel of the same storage form run the
+    same arithmetic on the same values: identical bits after an IBM run."""
+    cfg = gpkg.small_case(storage=storage)
+    out = {}
+    for v in ("staged", "cell" if storage == "f32" else "pair"):
+        monkeypatch.setenv("CLBM_KERNEL", v)
+        sim = gpkg.Simulation(cfg)
+        sim.run(30, graph=True)
+        out[v] = (sim.solver.read_populations(), sim.ibm.force_history(30))
+        sim.close()
+    a, b = out.values()
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_bounded_wait_reports_timeout(gpkg):
+    """Failure detection on the device: a staged launch whose barrier can never complete
+    gives up after a bounded number of polls, sets the status word and returns; the host
+    reads the error and the solver stays usable."""
+    s = gpkg.Solver(200, 6, 4, 1.5)
+    f0 = s.read_populations()
+    err = s.selftest_wait_timeout(4096)
+    assert err is not None and err.code == 4, err
+    np.testing.assert_array_equal(s.read_populations(), f0)
+    s.step()
+    s.synchronize()
+    st = s.check()
+    assert st["nonfinite"] == 0
     s.close()
 
 
