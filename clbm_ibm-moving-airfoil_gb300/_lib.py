@@ -25,7 +25,7 @@ EXPORTED = (
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
     "clbm_synchronize", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes",
-    "clbm_host_alloc", "clbm_host_free", "clbm_last_error",
+    "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
 )
 
 
@@ -103,6 +103,7 @@ def lib():
             "clbm_device_bytes": [vp, ctypes.POINTER(i64)],
             "clbm_host_alloc": [i64, pvp],
             "clbm_host_free": [vp],
+            "ibm_force_sums_noalloc": [P, P, i32, i32, i32, P, P, i32, vp, P],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

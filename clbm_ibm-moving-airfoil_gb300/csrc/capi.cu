@@ -51,6 +51,8 @@ constexpr int kKernelsPerIbmStep = 6;
 
 }  // namespace
 
+void clbm::set_last_error(const char* msg) { g_err = msg; }
+
 struct clbm_ibm;
 
 struct clbm_solver {

@@ -197,6 +197,9 @@ void launch_stream_collide(int storage, bool pull, int fmode, int variant, const
                            cudaStream_t st);
 // Cells per block of the staged variant for a lattice width.
 int staged_segment(int nx);
+
+// Record the message clbm_last_error() returns on this thread.
+void set_last_error(const char* msg);
 // Forced stream-collide of the cells of the current IBM force box; max_cells bounds the
 // box size (grid sizing only).
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,

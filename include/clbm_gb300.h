@@ -117,6 +117,22 @@ int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out);
 /* Number of compute_force calls made on this IBM (the device step counter). */
 int ibm_step_count(const clbm_ibm* ibm, int64_t* out);
 
+/* No counterpart in the reference. Allocation-free force sums for callers that cannot call
+ * cudaMalloc (code running while another library captures a CUDA graph, real-time loops
+ * with a fixed memory budget, hosts whose device memory belongs to a pool they cannot
+ * reach): the same sums as one entry of ibm_read_force_history -- sum of fx, fy clipped to
+ * +-0.05 over all cells, and sum of FX_k, FY_k -- over caller-owned device arrays fx, fy in
+ * the reference layout (Nx, Ny, Nz) and FXk, FYk (n markers; may be NULL when n == 0),
+ * written to host out[4]. Runs on `stream` (a cudaStream_t; NULL for the default stream)
+ * and waits for it. Its scratch is a fixed file-scope device array that every GPU loading
+ * this library holds until exit; lattices above 67,108,864 cells are rejected with
+ * CLBM_ERR_ARG. The first call on a device looks up that array's device address, a
+ * runtime call that must not happen during stream capture, so make the first call before
+ * capturing. All calls on a device share the array: calls that overlap on the GPU race. */
+int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t nx, int32_t ny, int32_t nz,
+                           const float* FXk, const float* FYk, int32_t n, void* stream,
+                           double* out);
+
 /* The driver loop of main_moving.py:116-122 for nsteps steps: per step
  * ibm_compute_force_motion then clbm_step, captured once into a CUDA graph and replayed
  * when use_graph != 0. ibm may be NULL (zero force). */
