@@ -644,14 +644,27 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
     if (!s || nsteps < 0 || (ibm && !m)) return fail(CLBM_ERR_ARG, "clbm_run: invalid argument");
     if (ibm && ibm->s != s) return fail(CLBM_ERR_ARG, "clbm_run: IBM bound to another solver");
     int done = 0;
+    const bool graph = use_graph && !s->prof;
+    // Captured steps evaluate the motion law on the device (the graph replays with
+    // advancing step numbers); direct launches evaluate it here in double, the arithmetic
+    // of main_moving.py:65-74, and pass the float32 truncation as kernel arguments.
+    bool capturing = false;
     auto one = [&]() -> int {
         if (ibm) {
-            int rc = ibm_compute_force_motion(ibm, m);
+            int rc;
+            if (capturing) {
+                rc = ibm_compute_force_motion(ibm, m);
+            } else {
+                const double t = (double)(ibm->calls + 1), w = m->w;
+                rc = ibm_compute_force(ibm, m->x0, m->y0 + m->a_heave * std::sin(w * t),
+                                       m->aoa0 + m->a_pitch * std::sin(w * t + m->phi_pitch), 0.0,
+                                       m->a_heave * w * std::cos(w * t),
+                                       m->a_pitch * w * std::cos(w * t + m->phi_pitch));
+            }
             if (rc) return rc;
         }
         return clbm_step(s, ibm);
     };
-    const bool graph = use_graph && !s->prof;
     // steps that change the kernel variants (first pull, macro already materialised) or
     // leave an odd remainder run as plain launches
     while (done < nsteps && graph && (s->local || s->macro_full)) {
@@ -668,8 +681,10 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
             const long long launches0 = s->launches;
             const long long calls0 = ibm ? ibm->calls : 0;
             CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+            capturing = true;
             int rc = one();
             if (!rc) rc = one();
+            capturing = false;
             cudaGraph_t graph_obj = nullptr;
             cudaError_t e = cudaStreamEndCapture(s->st, &graph_obj);
             // capture only recorded the work: restore the host mirrors
