@@ -80,6 +80,26 @@ def ellipsoid_markers(ax, ay, az, ds):
             np.array(zs, dtype=np.float32))
 
 
+def ellipse_section(chord, thickness, ds):
+    """Ellipse contour with semi-axes chord/2 (x) and thickness/2 (y), fish/config_fish.py:74-91
+    (perimeter by Ramanujan's first approximation)."""
+    a = chord / 2.0
+    b = thickness / 2.0
+    perim = np.pi * (3 * (a + b) - np.sqrt((3 * a + b) * (a + 3 * b)))
+    n = max(int(np.ceil(perim / ds)), 64)
+    if n % 2 != 0:
+        n += 1
+    ang = np.linspace(0.0, 2.0 * np.pi, n + 1)[:-1]
+    return (a * np.cos(ang)).astype(np.float32), (b * np.sin(ang)).astype(np.float32)
+
+
+def extrude_layers(X2, Y2, nz):
+    """One copy of a 2-D section on every z layer 0..nz-1 (fish/config_fish.py:101-108)."""
+    layers = np.arange(0, nz, 1.0, dtype=np.float32)
+    return (np.tile(X2, len(layers)).astype(np.float32), np.tile(Y2, len(layers)).astype(np.float32),
+            np.repeat(layers, len(X2)).astype(np.float32))
+
+
 def wing_fullspan_markers(chord, nz, ds=1.0, pivot_frac=0.25):
     """NACA 0012 section on every z layer 0..nz-1; body frame origin at the pivot,
     which sits at `pivot_frac` of the chord from the leading edge."""
@@ -155,6 +175,8 @@ class SimConfig:
     storage: str = "f32"
     span: float = 0.0            # spanwise length used for force coefficients
     name: str = "case"
+    templates: dict = field(default=None, repr=False)   # 2-D sections recorded in meta.npz
+    geometry: dict = field(default=None, repr=False)    # body dimensions recorded in grid_meta
     X0: np.ndarray = field(default=None, repr=False)
     Y0: np.ndarray = field(default=None, repr=False)
     Z0: np.ndarray = field(default=None, repr=False)
@@ -221,12 +243,14 @@ def wing_case(nx, ny, nz, chord, re=200.0, u_inf=0.05, k=0.5, name="wing", stora
     h = heave_frac * c * sin(w t), unrotated inflow, pivot at `pivot_frac` chord placed at
     x0 = 2c, y0 = Ny/2 (x0 = 160 for c = 80, as in config_moving.py:84-85)."""
     X, Y, Z = wing_fullspan_markers(chord, nz, ds=ds, pivot_frac=pivot_frac)
+    n2 = len(X) // nz
+    tmpl = dict(X_template=X[:n2].copy(), Y_template=Y[:n2].copy())
     return SimConfig(nx=nx, ny=ny, nz=nz, chord=float(chord), u_inf=u_inf, re=re,
                      inflow_deg=0.0, x0=2.0 * chord, y0=float(ny) / 2.0,
                      a_heave=heave_frac * chord, a_pitch=math.radians(pitch_amp_deg),
                      phi_pitch=math.radians(phase_deg), aoa0=math.radians(aoa0_deg),
                      k_reduced=k, storage=storage, span=float(nz), name=name,
-                     X0=X, Y0=Y, Z0=Z)
+                     templates=tmpl, X0=X, Y0=Y, Z0=Z)
 
 
 def small_case(storage="f32"):
@@ -239,14 +263,60 @@ def full_case(storage="f32"):
     return wing_case(600, 200, 50, 80, name="wing-600x200x50-c80", storage=storage)
 
 
+def _airplane_extras(nz, c, b_half, ds, fuse, x_tail_arm, c_htail, b_half_htail, c_vtail,
+                     h_vtail):
+    z0 = float(nz) / 2.0
+    Xt, Yt = naca0012_section(c, ds)
+    Xh, Yh = naca0012_section(c_htail, ds)
+    templates = dict(X_template=Xt, Y_template=Yt, X_htail_tmpl=Xh, Y_htail_tmpl=Yh)
+    geometry = dict(fuse_ax=fuse[0], fuse_ay=fuse[1], fuse_az=fuse[2], b_half=b_half,
+                    z_wing_start=z0 - b_half, z_wing_end=z0 + b_half, x_tail_arm=x_tail_arm,
+                    c_htail=c_htail, b_half_htail=b_half_htail,
+                    z_htail_start=z0 - b_half_htail, z_htail_end=z0 + b_half_htail,
+                    c_vtail=c_vtail, h_vtail=h_vtail)
+    return templates, geometry
+
+
 def reference_airplane_case(storage="f32"):
     """The reference's own case: 600x200x160 airplane at Re 200 (config_moving.py)."""
     X, Y, Z = airplane_markers()
-    return SimConfig(nx=600, ny=200, nz=160, chord=80.0, u_inf=0.05, re=200.0,
+    cfg = SimConfig(nx=600, ny=200, nz=160, chord=80.0, u_inf=0.05, re=200.0,
                      inflow_deg=8.0, x0=160.0, y0=100.0, a_heave=10.0,
                      a_pitch=float(np.radians(5.0)), phi_pitch=np.pi / 2.0,
                      aoa0=float(np.radians(8.0)), k_reduced=0.5, storage=storage,
                      span=120.0, name="airplane-600x200x160", X0=X, Y0=Y, Z0=Z)
+    cfg.templates, cfg.geometry = _airplane_extras(160, 80, 60, 0.7, (75.0, 10.0, 10.0), 80.0,
+                                                   36.0, 32.0, 36.0, 28.0)
+    return cfg
+
+
+def highre_airplane_case(storage="f32"):
+    """The reference's high-Re variant (config_highRe.py): 800x260x220 airplane, chord 120,
+    Re 1000, heave 15 lu, pitch 5 deg about 8 deg, inflow rotated by 8 deg."""
+    X, Y, Z = airplane_markers(nz=220, c=120, b_half=90, ds=0.7, fuse=(112.5, 15.0, 15.0),
+                               x_tail_arm=120.0, c_htail=54.0, b_half_htail=48.0, c_vtail=54.0,
+                               h_vtail=42.0)
+    cfg = SimConfig(nx=800, ny=260, nz=220, chord=120.0, u_inf=0.05, re=1000.0,
+                     inflow_deg=8.0, x0=200.0, y0=130.0, a_heave=15.0,
+                     a_pitch=float(np.radians(5.0)), phi_pitch=np.pi / 2.0,
+                     aoa0=float(np.radians(8.0)), k_reduced=0.5, storage=storage,
+                     span=180.0, name="airplane-800x260x220-re1000", X0=X, Y0=Y, Z0=Z)
+    cfg.templates, cfg.geometry = _airplane_extras(220, 120, 90, 0.7, (112.5, 15.0, 15.0), 120.0,
+                                                   54.0, 48.0, 54.0, 42.0)
+    return cfg
+
+
+def fish_case(storage="f32"):
+    """The reference's swimmer variant (fish/config_fish.py): 800x250x25, 4:1 ellipse of
+    chord 100, Re 300, heave 0.25c, pitch 15 deg, k = 0.8, no mean incidence."""
+    X2, Y2 = ellipse_section(100, 25, 0.7)
+    X, Y, Z = extrude_layers(X2, Y2, 25)
+    return SimConfig(nx=800, ny=250, nz=25, chord=100.0, u_inf=0.05, re=300.0,
+                     inflow_deg=0.0, x0=200.0, y0=125.0, a_heave=25.0,
+                     a_pitch=float(np.radians(15.0)), phi_pitch=np.pi / 2.0,
+                     aoa0=float(np.radians(0.0)), k_reduced=0.8, storage=storage, span=25.0,
+                     name="fish-800x250x25-re300", templates=dict(X_template=X2, Y_template=Y2),
+                     X0=X, Y0=Y, Z0=Z)
 
 
 def from_config_module(mod, storage="f32"):

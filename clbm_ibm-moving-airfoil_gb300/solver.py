@@ -159,7 +159,11 @@ class Solver:
                               ctypes.byref(umax), ctypes.byref(bad))
         stats = dict(rho_min=rmin.value, rho_max=rmax.value, u_max=umax.value,
                      nonfinite=bad.value)
-        check(rc)
+        try:
+            check(rc)
+        except _lib.CLBMError as e:
+            e.stats = stats
+            raise
         return stats
 
     # --- profiling ----------------------------------------------------------------

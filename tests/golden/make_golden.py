@@ -189,6 +189,12 @@ def make_geometry(ref_dir):
     for chord, ds in ((32, 1.0), (80, 1.0), (160, 1.0), (80, 0.7), (8, 0.7)):
         X, Y = cfg._naca0012_2d(chord, ds)
         out[f"naca_{chord}_{str(ds).replace('.', '')}"] = np.stack([X, Y])
+    hre = _load("_reference_config_highRe", os.path.join(ref_dir, "config_highRe.py"))
+    out["highre_n"] = hre.N_MARKERS
+    out["highre_sha"] = _sha(hre.X_marker_np, hre.Y_marker_np, hre.Z_marker_np)
+    fish = _load("_reference_config_fish", os.path.join(ref_dir, "fish", "config_fish.py"))
+    out["fish_n"] = fish.N_MARKERS
+    out["fish_sha"] = _sha(fish.X_marker_np, fish.Y_marker_np, fish.Z_marker_np)
     return out
 
 
