@@ -19,7 +19,7 @@ STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
 
 EXPORTED = (
     "clbm_create", "clbm_destroy", "clbm_step", "clbm_step_dense_force",
-    "clbm_step_host_force", "clbm_read_macro",
+    "clbm_step_host_force", "clbm_read_macro", "clbm_read_vorticity_slice",
     "clbm_read_populations", "clbm_write_populations", "clbm_check", "ibm_create",
     "ibm_destroy", "ibm_compute_force", "ibm_compute_force_motion", "ibm_read_forces",
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
@@ -80,6 +80,7 @@ def lib():
             "clbm_step_dense_force": [vp, P, P, P],
             "clbm_step_host_force": [vp, P, P, P],
             "clbm_read_macro": [vp, P, P, P, P],
+            "clbm_read_vorticity_slice": [vp, i32, P],
             "clbm_read_populations": [vp, P],
             "clbm_write_populations": [vp, P],
             "clbm_check": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d), ctypes.POINTER(d),

@@ -412,6 +412,22 @@ int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz)
     return CLBM_OK;
 }
 
+int clbm_read_vorticity_slice(clbm_solver* s, int32_t z, float* out) {
+    if (!s || !out || z < 0 || z >= s->g.nz)
+        return fail(CLBM_ERR_ARG, "clbm_read_vorticity_slice: invalid argument");
+    int rc = materialize(s, false);
+    if (rc) return rc;
+    const size_t n = (size_t)s->g.nx * s->g.ny;
+    rc = ensure_stage(s, n * sizeof(float));
+    if (rc) return rc;
+    launch_vorticity_slice(s->ux, s->uy, s->g, z, s->stage, s->st);
+    CK_LAUNCH();
+    s->launches += 1;
+    CK(cudaMemcpyAsync(out, s->stage, n * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
 int clbm_read_populations(clbm_solver* s, float* f_host) {
     if (!s || !f_host) return fail(CLBM_ERR_ARG, "clbm_read_populations: null argument");
     const size_t n = cells(s) * 19;

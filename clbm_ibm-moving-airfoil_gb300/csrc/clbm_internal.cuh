@@ -198,6 +198,10 @@ void launch_stream_collide(int storage, bool pull, int fmode, int variant, const
 // Cells per block of the staged variant for a lattice width.
 int staged_segment(int nx);
 
+// z-vorticity dux/dy - duy/dx of plane z into out (Nx, Ny), NumPy gradient edge rules.
+void launch_vorticity_slice(const float* ux, const float* uy, const Grid& g, int z, float* out,
+                            cudaStream_t st);
+
 // Record the message clbm_last_error() returns on this thread.
 void set_last_error(const char* msg);
 // Forced stream-collide of the cells of the current IBM force box; max_cells bounds the

@@ -775,6 +775,33 @@ __global__ void k_import_populations(const float* __restrict__ in, typename Pop<
     for (int q = 0; q < 19; ++q) Pop<S>::st(f + q * g.plane + cell, q, i[q]);
 }
 
+// z-vorticity of one z plane as the reference's renderers take it (render_2d.py:272-275,
+// fish/main_fish.py:308-309): w = d(ux)/dy - d(uy)/dx with NumPy gradient rules, central
+// differences inside and one-sided first differences on the edges (unit spacing);
+// output (Nx, Ny), y fastest.
+__global__ void k_vorticity_slice(const float* __restrict__ ux, const float* __restrict__ uy,
+                                  Grid g, int z, float* __restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= g.nx) return;
+    const long long row = (long long)z * g.ny * g.pitch;
+    auto at = [&](const float* a, int xx, int yy) { return a[row + (long long)yy * g.pitch + xx]; };
+    float dux_dy, duy_dx;
+    if (g.ny == 1) dux_dy = 0.f;
+    else if (y == 0) dux_dy = at(ux, x, 1) - at(ux, x, 0);
+    else if (y == g.ny - 1) dux_dy = at(ux, x, y) - at(ux, x, y - 1);
+    else dux_dy = 0.5f * (at(ux, x, y + 1) - at(ux, x, y - 1));
+    if (x == 0) duy_dx = at(uy, 1, y) - at(uy, 0, y);
+    else if (x == g.nx - 1) duy_dx = at(uy, x, y) - at(uy, x - 1, y);
+    else duy_dx = 0.5f * (at(uy, x + 1, y) - at(uy, x - 1, y));
+    out[(long long)x * g.ny + y] = dux_dy - duy_dx;
+}
+
+void launch_vorticity_slice(const float* ux, const float* uy, const Grid& g, int z, float* out,
+                            cudaStream_t st) {
+    k_vorticity_slice<<<dim3((g.nx + 127) / 128, g.ny), 128, 0, st>>>(ux, uy, g, z, out);
+}
+
 // rho = 1, u = (ux_in, uy_in, 0): the macro fields _init_feq sets (clbm_moving.py:88-91)
 __global__ void k_fill_macro(Grid g, Coef c, float* rho, float* ux, float* uy, float* uz) {
     const int x = blockIdx.x * kBX + threadIdx.x;

@@ -140,6 +140,14 @@ class Solver:
         check(lib().clbm_read_macro(self._h, *ptrs))
         return {n: buf[i].copy() for i, n in enumerate(names) if n in which}
 
+    def read_vorticity(self, z=None):
+        """z-vorticity d(ux)/dy - d(uy)/dx of plane z (default mid-span), (Nx, Ny) float32,
+        with NumPy gradient edge rules as the reference's renderers use."""
+        z = self.shape[2] // 2 if z is None else int(z)
+        out = np.empty(self.shape[:2], np.float32)
+        check(lib().clbm_read_vorticity_slice(self._h, z, _ptr(out)))
+        return out
+
     def read_populations(self):
         out = np.empty(self.shape + (19,), np.float32)
         check(lib().clbm_read_populations(self._h, _ptr(out)))

@@ -74,6 +74,11 @@ int clbm_step_host_force(clbm_solver* s, const float* fx, const float* fy, const
  * clbm_moving.py:305-321) copied to host arrays (any may be NULL). */
 int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz);
 
+/* z-vorticity of plane z as the reference's renderers compute it from lbm.ux/uy
+ * (render_2d.py:272-275): d(ux)/dy - d(uy)/dx with NumPy gradient rules (central inside,
+ * one-sided at the edges), into host out[Nx * Ny] ((Nx, Ny), y fastest). */
+int clbm_read_vorticity_slice(clbm_solver* s, int32_t z, float* out);
+
 /* lbm.f.to_numpy(): post-stream, post-boundary populations (Nx, Ny, Nz, 19) float32. */
 int clbm_read_populations(clbm_solver* s, float* f_host);
 /* lbm.f.from_numpy(): replace the state by host populations (Nx, Ny, Nz, 19). */

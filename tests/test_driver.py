@@ -36,6 +36,24 @@ def test_grid_meta_order_matches_reference_driver(pkg):
 
 
 @pytest.mark.gpu
+def test_vorticity_slice_matches_numpy_gradient(built_pkg):
+    """Device z-vorticity against render_2d.py's formula applied to the exported fields."""
+    pkg = built_pkg
+    cfg = pkg.wing_case(64, 32, 6, 10.0, re=30.0)
+    sim = pkg.Simulation(cfg)
+    sim.run(25)
+    m = sim.solver.read_macro()
+    for z in (0, 3, 5):
+        want = (np.gradient(m["ux"][:, :, z], 1.0, axis=1)
+                - np.gradient(m["uy"][:, :, z], 1.0, axis=0))
+        got = sim.solver.read_vorticity(z)
+        np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-7)
+    k, p = pkg.analysis.wake_vorticity_spectrum(sim.solver.read_vorticity(), cfg.chord, 30)
+    assert k[0] == 0 and np.all(np.isfinite(p))
+    sim.close()
+
+
+@pytest.mark.gpu
 def test_driver_frames_and_meta_match_oracle(built_pkg, oracle_mod, tmp_path):
     pkg = built_pkg
     cfg = pkg.wing_case(48, 24, 4, 8.0, re=20.0)
