@@ -1,0 +1,201 @@
+// ibm_device.cuh -- block-level bodies of the IBM kernels, shared by the single-lattice
+// kernels (ibm_kernels.cu) and the batched ensemble kernels (ensemble.cu). Each body takes
+// the index of its block within the lattice's launch (`bx`) and the number of such blocks
+// (`nbx`) instead of blockIdx.x / gridDim.x.
+#pragma once
+
+#include "clbm_internal.cuh"
+
+namespace clbm {
+
+constexpr int kMarkerBlock = 256;
+constexpr int kSpreadBlock = 256;
+constexpr int kFinishBlock = 256;
+
+// Marker kinematics (airfoil_moving.py:100-127) of markers [bx * 256, bx * 256 + 256) and
+// the box that bounds their 4x4x4 Peskin stencils (block min, one atomicMin per entry).
+template <bool DEVM>
+__device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid& g,
+                                                 const MotionF& mf, const clbm_motion& m, int bx) {
+    __shared__ int sbox[kMarkerBlock / 32][6];
+    __shared__ float smot[8];
+    const long long s = a.dev->step + 1;
+    if (threadIdx.x == 0) {
+        if (bx == 0) a.dev->cur = s;
+        MotionF v = mf;
+        if (DEVM) {
+            // _motion_state(step), main_moving.py:65-74, in double, then the float32
+            // truncation of the kernel arguments (airfoil_moving.py:101-103). One thread per
+            // block: double-precision sin/cos are slow on this part.
+            const double t = (double)s, w = m.w;
+            v.xc = (float)m.x0;
+            v.yc = (float)(m.y0 + m.a_heave * sin(w * t));
+            v.theta = (float)(m.aoa0 + m.a_pitch * sin(w * t + m.phi_pitch));
+            v.vx = 0.0f;
+            v.vy = (float)(m.a_heave * w * cos(w * t));
+            v.omega = (float)(m.a_pitch * w * cos(w * t + m.phi_pitch));
+        }
+        smot[0] = v.xc; smot[1] = v.yc; smot[2] = v.theta;
+        smot[3] = v.vx; smot[4] = v.vy; smot[5] = v.omega;
+        smot[6] = cosf(v.theta);
+        smot[7] = sinf(v.theta);
+    }
+    __syncthreads();
+    const float xc = smot[0], yc = smot[1], vx = smot[3], vy = smot[4], omega = smot[5];
+    const float cos_t = smot[6], sin_t = smot[7];
+    int b[6] = {kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty};
+    const int i = bx * kMarkerBlock + threadIdx.x;
+    if (i < a.n) {
+        const float x0m = a.X0[i], y0m = a.Y0[i], zk = a.Z0[i];
+        const float xk = xc + x0m * cos_t - y0m * sin_t;
+        const float yk = yc + x0m * sin_t + y0m * cos_t;
+        a.X[i] = xk;
+        a.Y[i] = yk;
+        a.Z[i] = zk;
+        const float rx = xk - xc, ry = yk - yc;
+        a.VX[i] = vx - omega * ry;
+        a.VY[i] = vy + omega * rx;
+        const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
+        b[0] = min(max(ib, 0), g.nx - 1);
+        b[1] = -min(max(ib + 3, 0), g.nx - 1);
+        b[2] = jb;
+        b[3] = -(jb + 3);
+        b[4] = kb;
+        b[5] = -(kb + 3);
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) b[e] = __reduce_min_sync(0xffffffffu, b[e]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+        for (int e = 0; e < 6; ++e) sbox[warp][e] = b[e];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int v = sbox[0][threadIdx.x];
+        for (int w = 1; w < kMarkerBlock / 32; ++w) v = min(v, sbox[w][threadIdx.x]);
+        if (v != kBoxEmpty) atomicMin(&a.dev->box[s & 1][threadIdx.x], v);
+    }
+}
+
+// One warp per marker m: Peskin interpolation of the current velocity (two stencil taps
+// per lane, warp-shuffle sums; airfoil_moving.py:142-170), marker force clip
+// (airfoil_moving.py:175-183) and spreading in 64-bit fixed point (airfoil_moving.py:188-214).
+__device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const Grid& g, int m,
+                                                       int lane) {
+    const float xk = a.X[m], yk = a.Y[m], zk = a.Z[m];
+    const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
+    float wt[2];
+    long long cell[2];
+    float us = 0.f, vs = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        // tap t: di fastest, so four neighbouring lanes read four consecutive x
+        const int t = lane + 32 * h;
+        const int di = t & 3, dj = (t >> 2) & 3, dk = t >> 4;
+        const int ii = min(max(ib + di, 0), g.nx - 1);   // x clamped (airfoil_moving.py:158)
+        const int jj = pmod(jb + dj, g.ny);              // y, z periodic indices; the weight
+        const int kk = pmod(kb + dk, g.nz);              // uses the wrapped index, as there
+        const float w = phi1d((float)ii - xk) * phi1d((float)jj - yk) * phi1d((float)kk - zk);
+        const long long c = ((long long)kk * g.ny + jj) * g.pitch + ii;
+        wt[h] = w;
+        cell[h] = c;
+        if (w != 0.0f) {
+            us += a.ux[c] * w;
+            vs += a.uy[c] * w;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        us += __shfl_xor_sync(0xffffffffu, us, o);
+        vs += __shfl_xor_sync(0xffffffffu, vs, o);
+    }
+    const float fxk = fmaxf(-0.05f, fminf(0.05f, -(us - a.VX[m])));
+    const float fyk = fmaxf(-0.05f, fminf(0.05f, -(vs - a.VY[m])));
+    if (lane == 0) {
+        a.Uk[m] = us;
+        a.Vk[m] = vs;
+        a.FXk[m] = fxk;
+        a.FYk[m] = fyk;
+    }
+    // spreading: the float32 contribution fxk * w (airfoil_moving.py:212-214) is added in
+    // 64-bit fixed point, so the sum does not depend on the order of the atomics
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (wt[h] != 0.0f) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + cell[h]),
+                      (unsigned long long)__float2ll_rn(fxk * wt[h] * kForceScale));
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + cell[h]),
+                      (unsigned long long)__float2ll_rn(fyk * wt[h] * kForceScale));
+        }
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Double sums of the clipped Eulerian force over the box and of the marker forces into the
+// history ring, then the device call counter advances. Block bx of nbx writes its partial;
+// the last block to finish sums the partials in block order (scheduling-independent).
+__device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& g, int bx, int nbx) {
+    __shared__ double red[kFinishBlock / 32][4];
+    __shared__ bool last;
+    IbmDev* dev = a.dev;
+    const long long s = dev->step + 1;
+    const Band b = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
+    const int cells = b.ilen * b.jlen * b.klen;
+    const int stride = nbx * kFinishBlock;
+    double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;
+    for (int t = bx * kFinishBlock + threadIdx.x; t < cells; t += stride) {
+        int x, y, z;
+        box_cell(b, g.ny, g.nz, t, x, y, z);
+        const long long c = ((long long)z * g.ny + y) * g.pitch + x;
+        sx += (double)fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f);
+        sy += (double)fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f);
+    }
+    for (int t = bx * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
+        mx += (double)a.FXk[t];
+        my += (double)a.FYk[t];
+    }
+    sx = warp_sum(sx); sy = warp_sum(sy); mx = warp_sum(mx); my = warp_sum(my);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { red[warp][0] = sx; red[warp][1] = sy; red[warp][2] = mx; red[warp][3] = my; }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int w = 0; w < kFinishBlock / 32; ++w) v += red[w][threadIdx.x];
+        a.part[4 * bx + threadIdx.x] = v;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int tk = atomicAdd(&dev->ticket, 1u);
+        last = (tk == (unsigned int)nbx - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int blk = threadIdx.x; blk < nbx; blk += kFinishBlock)
+        for (int e = 0; e < 4; ++e) v[e] += __ldcg(a.part + 4 * blk + e);
+    for (int e = 0; e < 4; ++e) v[e] = warp_sum(v[e]);
+    __syncthreads();
+    if (lane == 0)
+        for (int e = 0; e < 4; ++e) red[warp][e] = v[e];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < kFinishBlock / 32; ++w) t += red[w][threadIdx.x];
+        a.hist[4 * ((s - 1) % a.hist_cap) + threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) {
+        dev->ticket = 0u;
+        // the previous call's box was consumed by this call's band-prepare
+        for (int e = 0; e < 6; ++e) dev->box[(s + 1) & 1][e] = kBoxEmpty;
+        __threadfence();
+        dev->step = s;
+    }
+}
+
+}  // namespace clbm
