@@ -37,6 +37,7 @@ def parse_args():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=200)
     return p.parse_args()
 
@@ -136,6 +137,29 @@ def cpu_baseline(cfg, steps=3):
             "sample": f"{steps} full steps of {cfg.nx}x{cfg.ny}x{cfg.nz} "
                       f"({cfg.n_markers} markers) after 1 warm-up step, "
                       "C/OpenMP restatement of the reference's unfused step"}
+
+
+def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
+    """Aggregate MLUPS of the batched ensemble: n members drawn with seeds 0..n-1 (lattices
+    150x60x12, 200x80x16, 300x100x24; Re, heave, pitch, phase, k uniform), stepped together
+    as a replayed CUDA graph; CUDA events on the ensemble's stream."""
+    cases = [pkg.config.ensemble_case(seed, storage=storage) for seed in range(n)]
+    ens = pkg.Ensemble(cases, device=device)
+    stream = torch.cuda.ExternalStream(ens.stream_handle(), device=torch.device("cuda", device))
+    ens.run(warmup)
+    ens.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ens.run(steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"instances": n, "cells": ens.cells, "markers": sum(c.n_markers for c in cases),
+           "steps": steps, "ms_per_step": ms / steps,
+           "mlups": ens.cells * steps / (ms / 1e3) / 1e6, "storage": storage,
+           "tuning": ens.tuning()}
+    ens.close()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -292,6 +316,8 @@ def run_gpu(args, rank, world, local):
             "clocks": clk.summary(),
         }
     sim.close()
+    if result is not None and not args.no_ensemble:
+        result["ensemble"] = {s: measure_ensemble(pkg, torch, local, s) for s in ("f32", "f16")}
     if result is not None and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(pkg.full_case())
     if dist is not None:

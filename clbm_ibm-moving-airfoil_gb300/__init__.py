@@ -15,10 +15,10 @@ from ._lib import CLBMError, DivergedError, EXPORTED, lib, lib_path
 from .build import build
 from .config import (SimConfig, fish_case, force_coefficients, full_case,
                      highre_airplane_case, reference_airplane_case, small_case, wing_case)
-from .solver import IBM, PinnedBuffer, Simulation, Solver
+from .solver import IBM, Ensemble, PinnedBuffer, Simulation, Solver
 
 __all__ = [
-    "CLBMError", "DivergedError", "EXPORTED", "IBM", "PinnedBuffer", "SimConfig", "Simulation",
+    "CLBMError", "DivergedError", "EXPORTED", "Ensemble", "IBM", "PinnedBuffer", "SimConfig", "Simulation",
     "Solver", "analysis", "build", "config", "driver", "fish_case", "force_coefficients", "full_case",
     "highre_airplane_case", "lib", "lib_path", "reference_airplane_case", "small_case",
     "wing_case",

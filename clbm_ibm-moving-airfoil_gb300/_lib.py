@@ -26,6 +26,8 @@ EXPORTED = (
     "clbm_synchronize", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
+    "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
+    "clbm_ensemble_tuning", "clbm_ensemble_destroy",
 )
 
 
@@ -105,6 +107,12 @@ def lib():
             "clbm_host_alloc": [i64, pvp],
             "clbm_host_free": [vp],
             "ibm_force_sums_noalloc": [P, P, i32, i32, i32, P, P, i32, vp, P],
+            "clbm_ensemble_create": [P, P, P, i32, pvp],
+            "clbm_ensemble_run": [vp, i32, i32],
+            "clbm_ensemble_stream": [vp, pvp],
+            "clbm_ensemble_tuning": [vp, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                     ctypes.POINTER(i64)],
+            "clbm_ensemble_destroy": [vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

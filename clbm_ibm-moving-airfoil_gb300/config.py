@@ -290,6 +290,26 @@ def reference_airplane_case(storage="f32"):
     return cfg
 
 
+ENSEMBLE_LATTICES = ((150, 60, 12), (200, 80, 16), (300, 100, 24))
+
+
+def ensemble_case(seed, storage="f32", lattices=ENSEMBLE_LATTICES):
+    """One member of the batched ensemble, drawn from numpy's default_rng(seed): a lattice
+    uniformly from `lattices` with chord Nx / 6.25, Re in [100, 400], heave amplitude in
+    [0.1c, 0.4c], pitch amplitude in [0, 20] deg, phase in [0, 180] deg, k in [0.25, 1];
+    the rest as the wing cases (mean pitch 8 deg, quarter-chord pivot, unrotated inflow)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = lattices[int(rng.integers(len(lattices)))]
+    chord = nx / 6.25
+    re = float(rng.uniform(100.0, 400.0))
+    heave = float(rng.uniform(0.1, 0.4))
+    pitch = float(rng.uniform(0.0, 20.0))
+    phase = float(rng.uniform(0.0, 180.0))
+    k = float(rng.uniform(0.25, 1.0))
+    return wing_case(nx, ny, nz, chord, re=re, k=k, heave_frac=heave, pitch_amp_deg=pitch,
+                     phase_deg=phase, storage=storage, name=f"ensemble-{seed}")
+
+
 def highre_airplane_case(storage="f32"):
     """The reference's high-Re variant (config_highRe.py): 800x260x220 airplane, chord 120,
     Re 1000, heave 15 lu, pitch 5 deg about 8 deg, inflow rotated by 8 deg."""

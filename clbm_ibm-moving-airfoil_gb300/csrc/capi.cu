@@ -845,3 +845,286 @@ int clbm_host_free(void* p) {
 }
 
 }  // extern "C"
+
+// ====================================================================== ensemble
+struct clbm_ensemble {
+    std::vector<clbm_solver*> s;
+    std::vector<clbm_ibm*> ibm;
+    std::vector<clbm_motion> m;
+    int n = 0;
+    int storage = 0;
+    EnsDesc* d_desc = nullptr;
+    long long* d_tile0 = nullptr;
+    long long ntiles = 0;
+    int bx = 128;            // bulk tile width (cells)
+    int grid = 0;            // persistent bulk blocks
+    int max_marker_blocks = 0, max_spread_blocks = 0, box_blocks = 0;
+    int cur = 0;
+    bool local = true, macro_full = true;
+    cudaStream_t st = nullptr, st2 = nullptr;
+    cudaEvent_t ev_box = nullptr, ev_bulk = nullptr, ev_sync = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int g_cur = -1;
+    long long launches = 0;
+};
+
+namespace {
+
+// Device descriptors for tile width bx; returns the number of bulk tiles.
+int ens_upload(clbm_ensemble* e, int bx) {
+    std::vector<EnsDesc> h(e->n);
+    std::vector<long long> t0(e->n);
+    long long tiles = 0;
+    for (int i = 0; i < e->n; ++i) {
+        clbm_solver* s = e->s[i];
+        EnsDesc& D = h[i];
+        D = EnsDesc{};
+        D.g = s->g;
+        D.c = s->c;
+        D.f[0] = s->f[0];
+        D.f[1] = s->f[1];
+        D.rho = s->rho; D.ux = s->ux; D.uy = s->uy; D.uz = s->uz;
+        D.has_ibm = e->ibm[i] != nullptr;
+        if (D.has_ibm) D.a = e->ibm[i]->a;
+        D.m = e->m[i];
+        D.tiles_x = (s->g.nx + bx - 1) / bx;
+        D.tile0 = tiles;
+        t0[i] = tiles;
+        tiles += (long long)D.tiles_x * s->g.ny * s->g.nz;
+    }
+    CK(cudaMemcpyAsync(e->d_desc, h.data(), sizeof(EnsDesc) * e->n, cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->d_tile0, t0.data(), sizeof(long long) * e->n, cudaMemcpyHostToDevice, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    e->ntiles = tiles;
+    e->bx = bx;
+    return CLBM_OK;
+}
+
+// The ensemble's bulk-pass schedule: tile width 128 or 256 cells, and persistent blocks
+// (4 or 8 per SM) or one block per tile; each candidate is timed over three launches.
+int ens_tune(clbm_ensemble* e) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_bx = 128, best_grid = 4 * sms;
+    for (int bx : {128, 256}) {
+        if (int rc = ens_upload(e, bx)) return rc;
+        for (int per_sm : {4, 8, 0}) {
+            const long long g = per_sm ? (long long)per_sm * sms : e->ntiles;
+            const int grid = (int)std::min<long long>(g, 1LL << 30);
+            launch_ens_bulk(e->storage, true, bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
+                            grid, e->st);
+            CK(cudaEventRecord(e0, e->st));
+            for (int k = 0; k < 3; ++k)
+                launch_ens_bulk(e->storage, true, bx, e->d_desc, e->d_tile0, e->n, e->ntiles,
+                                e->cur, grid, e->st);
+            CK(cudaEventRecord(e1, e->st));
+            CK(cudaEventSynchronize(e1));
+            CK_LAUNCH();
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            e->launches += 4;
+            if (ms < best) {
+                best = ms;
+                best_bx = bx;
+                best_grid = grid;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    e->grid = best_grid;
+    return ens_upload(e, best_bx);
+}
+
+int ens_step(clbm_ensemble* e) {
+    const bool pull = !e->local;
+    launch_ens_markers(e->d_desc, e->n, e->max_marker_blocks, e->st);
+    CK(cudaEventRecord(e->ev_box, e->st));
+    launch_ens_band_prepare(e->storage, pull, e->d_desc, e->n, e->cur, !e->macro_full,
+                            e->box_blocks, e->st);
+    launch_ens_interp_spread(e->d_desc, e->n, e->max_spread_blocks, e->st);
+    launch_ens_finish(e->d_desc, e->n, e->st);
+    CK(cudaStreamWaitEvent(e->st2, e->ev_box, 0));
+    launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
+                    e->grid, e->st2);
+    CK(cudaEventRecord(e->ev_bulk, e->st2));
+    launch_ens_box(e->storage, pull, e->d_desc, e->n, e->cur, e->box_blocks, e->st);
+    CK(cudaStreamWaitEvent(e->st, e->ev_bulk, 0));
+    CK_LAUNCH();
+    e->launches += 6;
+    e->cur ^= 1;
+    e->local = false;
+    e->macro_full = false;
+    return CLBM_OK;
+}
+
+void ens_free_graph(clbm_ensemble* e) {
+    if (e->gexec) cudaGraphExecDestroy(e->gexec);
+    e->gexec = nullptr;
+    e->g_cur = -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
+                         const clbm_motion* motions, int32_t n, clbm_ensemble** out) {
+    if (!solvers || !motions || !out || n < 1 || n > 4096)
+        return fail(CLBM_ERR_ARG, "clbm_ensemble_create: invalid argument");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        clbm_solver* s = solvers[i];
+        if (!s) return fail(CLBM_ERR_ARG, "clbm_ensemble_create: null solver %d", i);
+        if (s->cfg.storage != solvers[0]->cfg.storage || s->cfg.device != solvers[0]->cfg.device)
+            return fail(CLBM_ERR_ARG, "clbm_ensemble_create: solvers differ in storage or device");
+        if (s->cur != solvers[0]->cur || s->local != solvers[0]->local ||
+            s->macro_full != solvers[0]->macro_full)
+            return fail(CLBM_ERR_STATE, "clbm_ensemble_create: solvers are not at the same step");
+        if (ibms && ibms[i] && ibms[i]->s != s)
+            return fail(CLBM_ERR_ARG, "clbm_ensemble_create: IBM %d bound to another solver", i);
+        for (int j = 0; j < i; ++j)
+            if (solvers[j] == s) return fail(CLBM_ERR_ARG, "clbm_ensemble_create: solver %d repeated", i);
+    }
+    clbm_ensemble* e = new clbm_ensemble();
+    e->n = n;
+    e->storage = solvers[0]->cfg.storage;
+    e->cur = solvers[0]->cur;
+    e->local = solvers[0]->local;
+    e->macro_full = solvers[0]->macro_full;
+    auto bail = [&](int rc) { clbm_ensemble_destroy(e); return rc; };
+    for (int i = 0; i < n; ++i) {
+        e->s.push_back(solvers[i]);
+        e->ibm.push_back(ibms ? ibms[i] : nullptr);
+        e->m.push_back(motions[i]);
+        clbm_ibm* b = e->ibm.back();
+        if (b) {
+            e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + 255) / 256);
+            e->max_spread_blocks = std::max(e->max_spread_blocks, (int)(((long long)b->a.n * 32 + 255) / 256));
+            const long long cells = (long long)b->a.max_bx * b->a.max_by * b->a.max_bz;
+            e->box_blocks = std::max(e->box_blocks, (int)std::min<long long>((cells + 255) / 256, 4 * 152));
+        }
+    }
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&e->st, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&e->st2, cudaStreamNonBlocking, lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ev_box, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ev_bulk, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->ev_sync, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc(&e->d_desc, sizeof(EnsDesc) * n) != cudaSuccess ||
+        cudaMalloc(&e->d_tile0, sizeof(long long) * n) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream/event/allocation failed"));
+    for (clbm_solver* s : e->s) {   // members' queued work (initialisation) comes first
+        if (cudaEventRecord(e->ev_sync, s->st) != cudaSuccess ||
+            cudaStreamWaitEvent(e->st, e->ev_sync, 0) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream ordering failed"));
+    }
+    if (int rc = ens_tune(e)) return bail(rc);
+    *out = e;
+    return CLBM_OK;
+}
+
+int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
+    if (!e || nsteps < 0) return fail(CLBM_ERR_ARG, "clbm_ensemble_run: invalid argument");
+    for (int i = 0; i < e->n; ++i)
+        if (e->s[i]->cur != e->cur || (e->ibm[i] && e->ibm[i]->s != e->s[i]))
+            return fail(CLBM_ERR_STATE, "clbm_ensemble_run: member %d was stepped or destroyed "
+                        "outside the ensemble", i);
+    for (clbm_solver* s : e->s) {
+        CK(cudaEventRecord(e->ev_sync, s->st));
+        CK(cudaStreamWaitEvent(e->st, e->ev_sync, 0));
+    }
+    int done = 0;
+    while (done < nsteps && (!use_graph || e->local || e->macro_full)) {
+        if (int rc = ens_step(e)) return rc;
+        ++done;
+    }
+    if (use_graph && nsteps - done >= 2) {
+        if (!e->gexec || e->g_cur != e->cur) {
+            ens_free_graph(e);
+            const int cur0 = e->cur;
+            const long long l0 = e->launches;
+            CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+            int rc = ens_step(e);
+            if (!rc) rc = ens_step(e);
+            cudaGraph_t g = nullptr;
+            cudaError_t err = cudaStreamEndCapture(e->st, &g);
+            e->cur = cur0;
+            e->launches = l0;
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (err != cudaSuccess)
+                return fail(CLBM_ERR_CUDA, "clbm_ensemble_run: capture failed: %s", cudaGetErrorString(err));
+            err = cudaGraphInstantiate(&e->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (err != cudaSuccess)
+                return fail(CLBM_ERR_CUDA, "clbm_ensemble_run: instantiate failed: %s", cudaGetErrorString(err));
+            e->g_cur = cur0;
+        }
+        while (nsteps - done >= 2) {
+            CK(cudaGraphLaunch(e->gexec, e->st));
+            done += 2;
+            e->launches += 12;
+        }
+    }
+    while (done < nsteps) {
+        if (int rc = ens_step(e)) return rc;
+        ++done;
+    }
+    // members see the new state: host mirrors, and their streams wait for the ensemble
+    CK(cudaEventRecord(e->ev_sync, e->st));
+    for (int i = 0; i < e->n; ++i) {
+        clbm_solver* s = e->s[i];
+        if (nsteps > 0) {
+            s->cur = e->cur;
+            s->local = false;
+            s->macro_full = false;
+            s->version += nsteps;
+        }
+        if (e->ibm[i]) e->ibm[i]->calls += nsteps;
+        CK(cudaStreamWaitEvent(s->st, e->ev_sync, 0));
+    }
+    return CLBM_OK;
+}
+
+int clbm_ensemble_stream(const clbm_ensemble* e, void** out) {
+    if (!e || !out) return fail(CLBM_ERR_ARG, "clbm_ensemble_stream: null argument");
+    *out = (void*)e->st;
+    return CLBM_OK;
+}
+
+int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
+                         int64_t* tiles) {
+    if (!e) return fail(CLBM_ERR_ARG, "clbm_ensemble_tuning: null ensemble");
+    if (tile_width) *tile_width = e->bx;
+    if (blocks) *blocks = e->grid;
+    if (tiles) *tiles = e->ntiles;
+    return CLBM_OK;
+}
+
+int clbm_ensemble_destroy(clbm_ensemble* e) {
+    if (!e) return CLBM_OK;
+    if (e->st) cudaStreamSynchronize(e->st);
+    if (e->st2) cudaStreamSynchronize(e->st2);
+    ens_free_graph(e);
+    if (e->d_desc) cudaFree(e->d_desc);
+    if (e->d_tile0) cudaFree(e->d_tile0);
+    cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};
+    for (cudaEvent_t ev : evs)
+        if (ev) cudaEventDestroy(ev);
+    if (e->st2) cudaStreamDestroy(e->st2);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return CLBM_OK;
+}
+
+}  // extern "C"

@@ -259,4 +259,32 @@ void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st
 // Force sums of this call into the history ring, then advance the device call counter.
 void launch_ibm_finish(const IbmArrays& a, const Grid& g, cudaStream_t st);
 
+// ---------------------------------------------------------------- ensemble
+// Descriptor of one lattice of an ensemble: the batched kernels find everything an
+// instance needs here (device copy, one entry per instance).
+struct EnsDesc {
+    Grid g;
+    Coef c;
+    void* f[2];
+    float *rho, *ux, *uy, *uz;
+    IbmArrays a;
+    clbm_motion m;
+    long long tile0;   // first bulk tile of this instance in the flat tile list
+    int tiles_x;       // bulk tiles per (y, z) row
+    int has_ibm;
+};
+
+// One ensemble step is six batched launches: markers (device motion), band prepare,
+// interpolation + spreading, force sums, box pass on `st`; the bulk pass over the flat
+// tile list of all instances (tile width bx, `grid` persistent blocks) on `st2`.
+void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st);
+void launch_ens_band_prepare(int storage, bool pull, const EnsDesc* d, int n, int parity,
+                             bool compute_macro, int blocks, cudaStream_t st);
+void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st);
+void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st);
+void launch_ens_box(int storage, bool pull, const EnsDesc* d, int n, int parity, int blocks,
+                    cudaStream_t st);
+void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,
+                     int n, long long ntiles, int parity, int grid, cudaStream_t st);
+
 }  // namespace clbm

@@ -280,3 +280,59 @@ class Simulation:
         if self.ibm is not None:
             self.ibm.close()
         self.solver.close()
+
+
+class Ensemble:
+    """Many independent cases stepped together by batched launches (one Simulation per
+    member; members stay readable individually through `sims`)."""
+
+    def __init__(self, cfgs, device=0):
+        self.sims = [Simulation(c, device=device) for c in cfgs]
+        n = len(self.sims)
+        if n == 0:
+            raise ValueError("an ensemble needs at least one case")
+        solvers = (ctypes.c_void_p * n)(*[s.solver.handle.value for s in self.sims])
+        ibms = (ctypes.c_void_p * n)(*[(s.ibm._h.value if s.ibm is not None else None)
+                                       for s in self.sims])
+        motions = (_lib.Motion * n)()
+        for i, s in enumerate(self.sims):
+            m = s.cfg.motion()
+            motions[i] = _lib.Motion(x0=m["x0"], y0=m["y0"], a_heave=m["a_heave"],
+                                     a_pitch=m["a_pitch"], phi_pitch=m["phi_pitch"],
+                                     aoa0=m["aoa0"], w=m["omega"])
+        self._h = ctypes.c_void_p()
+        check(lib().clbm_ensemble_create(solvers, ibms, motions, n, ctypes.byref(self._h)))
+
+    @property
+    def cells(self):
+        return sum(s.cfg.cells for s in self.sims)
+
+    def run(self, nsteps, graph=True):
+        check(lib().clbm_ensemble_run(self._h, int(nsteps), 1 if graph else 0))
+
+    def stream_handle(self):
+        p = ctypes.c_void_p()
+        check(lib().clbm_ensemble_stream(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    def tuning(self):
+        w, b, t = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+        check(lib().clbm_ensemble_tuning(self._h, ctypes.byref(w), ctypes.byref(b), ctypes.byref(t)))
+        return dict(tile_width=w.value, blocks=b.value, tiles=t.value)
+
+    def synchronize(self):
+        for s in self.sims:
+            s.solver.synchronize()
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            lib().clbm_ensemble_destroy(self._h)
+        self._h = None
+        for s in self.sims:
+            s.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

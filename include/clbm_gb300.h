@@ -144,6 +144,26 @@ int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t nx, int32_t
 int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps,
              int32_t use_graph);
 
+/* Batched ensemble (no counterpart in the reference, which runs one case per process):
+ * many independent solvers, each with its own IBM (or NULL) and motion law, stepped
+ * together -- each step is six launches over all members (markers, band macro,
+ * interpolation/spreading, force sums, force-box pass, and one persistent bulk
+ * stream-collide over a flat tile list of every member). Members keep their buffers and
+ * all per-member reads (clbm_read_macro, ibm_read_force_history, ...) keep working; the
+ * members must be fresh or at the same step, share storage form and device, and outlive
+ * the ensemble. clbm_ensemble_create times the bulk-pass tile width and block schedule
+ * and keeps the fastest (clbm_ensemble_tuning reports them). */
+typedef struct clbm_ensemble clbm_ensemble;
+int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
+                         const clbm_motion* motions, int32_t n, clbm_ensemble** out);
+/* nsteps steps of every member (main_moving.py:116-122 with the motion law evaluated on the
+ * device), as a two-step CUDA graph replay when use_graph != 0. */
+int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph);
+int clbm_ensemble_stream(const clbm_ensemble* e, void** out);
+int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
+                         int64_t* tiles);
+int clbm_ensemble_destroy(clbm_ensemble* e);
+
 /* Wait for all queued work of the solver. */
 int clbm_synchronize(clbm_solver* s);
 
