@@ -887,10 +887,10 @@ int ens_upload(clbm_ensemble* e, int bx) {
         D.has_ibm = e->ibm[i] != nullptr;
         if (D.has_ibm) D.a = e->ibm[i]->a;
         D.m = e->m[i];
-        D.tiles_x = (s->g.nx + bx - 1) / bx;
+        D.cells = s->g.nx * s->g.ny * s->g.nz;
         D.tile0 = tiles;
         t0[i] = tiles;
-        tiles += (long long)D.tiles_x * s->g.ny * s->g.nz;
+        tiles += (D.cells + bx - 1) / bx;
     }
     CK(cudaMemcpyAsync(e->d_desc, h.data(), sizeof(EnsDesc) * e->n, cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->d_tile0, t0.data(), sizeof(long long) * e->n, cudaMemcpyHostToDevice, e->st));
@@ -982,6 +982,8 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
     for (int i = 0; i < n; ++i) {
         clbm_solver* s = solvers[i];
         if (!s) return fail(CLBM_ERR_ARG, "clbm_ensemble_create: null solver %d", i);
+        if ((long long)s->g.nx * s->g.ny * s->g.nz > (1LL << 30))
+            return fail(CLBM_ERR_ARG, "clbm_ensemble_create: member %d has more than 2^30 cells", i);
         if (s->cfg.storage != solvers[0]->cfg.storage || s->cfg.device != solvers[0]->cfg.device)
             return fail(CLBM_ERR_ARG, "clbm_ensemble_create: solvers differ in storage or device");
         if (s->cur != solvers[0]->cur || s->local != solvers[0]->local ||

@@ -135,13 +135,20 @@ __device__ inline float phi1d(float r) {
 
 // ---------------------------------------------------------------- population storage
 template <int S> struct Pop;
+// ld/st convert between the stored value and f; ld_raw/st_raw move the stored value
+// itself (f for float32, the deviation f - w for the shifted forms), for the
+// deviation-form collision.
 template <> struct Pop<CLBM_STORE_F32> {
     using T = float;
+    static constexpr bool kShifted = false;
     static __device__ __forceinline__ float ld(const T* p, int q) { (void)q; return __ldg(p); }
     static __device__ __forceinline__ void st(T* p, int q, float v) { (void)q; __stcs(p, v); }
+    static __device__ __forceinline__ float ld_raw(const T* p) { return __ldg(p); }
+    static __device__ __forceinline__ void st_raw(T* p, float v) { __stcs(p, v); }
 };
 template <> struct Pop<CLBM_STORE_F16S> {
     using T = __half;
+    static constexpr bool kShifted = true;
     static __device__ __forceinline__ float ld(const T* p, int q) {
         return __half2float(__ldg(p)) + wq(q);
     }
@@ -149,15 +156,24 @@ template <> struct Pop<CLBM_STORE_F16S> {
         __stcs(reinterpret_cast<unsigned short*>(p),
                __half_as_ushort(__float2half_rn(v - wq(q))));
     }
+    static __device__ __forceinline__ float ld_raw(const T* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void st_raw(T* p, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
+    }
 };
 template <> struct Pop<CLBM_STORE_BF16S> {
     using T = __nv_bfloat16;
+    static constexpr bool kShifted = true;
     static __device__ __forceinline__ float ld(const T* p, int q) {
         return __bfloat162float(__ldg(p)) + wq(q);
     }
     static __device__ __forceinline__ void st(T* p, int q, float v) {
         __stcs(reinterpret_cast<unsigned short*>(p),
                __bfloat16_as_ushort(__float2bfloat16_rn(v - wq(q))));
+    }
+    static __device__ __forceinline__ float ld_raw(const T* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void st_raw(T* p, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __bfloat16_as_ushort(__float2bfloat16_rn(v)));
     }
 };
 
@@ -270,7 +286,7 @@ struct EnsDesc {
     IbmArrays a;
     clbm_motion m;
     long long tile0;   // first bulk tile of this instance in the flat tile list
-    int tiles_x;       // bulk tiles per (y, z) row
+    int cells;         // nx * ny * nz; a tile is a run of consecutive cells in x-fastest order
     int has_ibm;
 };
 

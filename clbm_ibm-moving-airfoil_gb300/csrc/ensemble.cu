@@ -3,8 +3,8 @@
 // Each lattice of an ensemble keeps its own buffers; a device array of descriptors
 // (EnsDesc) tells the batched kernels where they are. The IBM kernels index the instance
 // with blockIdx.y (each instance uses as many x-blocks as it needs, the rest leave). The
-// bulk stream-collide pass runs persistent blocks over one flat list of row-segment tiles
-// of all instances, so lattices of different sizes share the GPU without tail effects;
+// bulk stream-collide pass runs persistent blocks over one flat list of tiles (runs of
+// consecutive cells) of all instances, so lattices of different sizes share the GPU without tail effects;
 // the tile width and the number of persistent blocks are picked by timing at creation.
 // Every per-cell and per-marker computation is the single-lattice code (lbm_device.cuh,
 // ibm_device.cuh), so an instance gives the same bits as when it is stepped alone.
@@ -72,11 +72,13 @@ __global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
         }
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
-        const long long rem = t - D.tile0;
-        const int row = (int)(rem / D.tiles_x);
-        const int x = (int)(rem - (long long)row * D.tiles_x) * BX + threadIdx.x;
-        if (x >= g.nx) continue;
-        const int y = row % g.ny, z = row / g.ny;
+        // tiles run over the instance's cells in x-fastest order across row ends, so no
+        // lane idles at the end of a row that is not a multiple of the tile width
+        const unsigned i = (unsigned)(t - D.tile0) * BX + threadIdx.x;
+        if (i >= (unsigned)D.cells) continue;
+        const unsigned row = i / (unsigned)g.nx;
+        const int x = (int)(i - row * (unsigned)g.nx);
+        const int y = (int)(row % (unsigned)g.ny), z = (int)(row / (unsigned)g.ny);
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
         if (D.has_ibm) {

@@ -25,14 +25,19 @@ __device__ __forceinline__ void zou_he(float (&v)[19], const Coef& c) {
 // Gather the post-stream, post-boundary populations S(x, y, z) of the stored state.
 // pull = false: the stored array already is a post-stream state (after initialisation or
 // an import), read in place.
-template <int S, bool PULL>
+// RAW: return the stored values themselves (the deviations h = f - w of the shifted forms,
+// for collide<.., DEV = true>); the Zou-He inlet is applied to f = h + w and shifted back.
+// For float32 storage RAW changes nothing.
+template <int S, bool PULL, bool RAW = false>
 __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f, const Grid& g,
                                        const Coef& c, int x, int y, int z, float (&v)[19]) {
     using P = Pop<S>;
+    constexpr bool kRaw = RAW && P::kShifted;
     if (!PULL) {
         const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
 #pragma unroll
-        for (int q = 0; q < 19; ++q) v[q] = P::ld(f + q * g.plane + cell, q);
+        for (int q = 0; q < 19; ++q)
+            v[q] = kRaw ? P::ld_raw(f + q * g.plane + cell) : P::ld(f + q * g.plane + cell, q);
         return;
     }
     const int xe = (x == g.nx - 1) ? g.nx - 2 : x;  // outlet: copy of column Nx-2
@@ -48,10 +53,29 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
         if (ex(q) == 1 && xe == 0) {
             v[q] = 0.0f;  // inlet unknown, rebuilt by Zou-He below
         } else {
-            v[q] = P::ld(f + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + sx, q);
+            const typename P::T* p = f + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + sx;
+            v[q] = kRaw ? P::ld_raw(p) : P::ld(p, q);
         }
     }
-    if (xe == 0) zou_he(v, c);
+    if (xe == 0) {
+        if (kRaw) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) v[q] += wq(q);
+        }
+        zou_he(v, c);
+        if (kRaw) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) v[q] -= wq(q);
+        }
+    }
+}
+
+// Store a population vector produced by gather<.., RAW = true> + collide<.., DEV = kShifted>.
+template <int S>
+__device__ __forceinline__ void store_raw(typename Pop<S>::T* __restrict__ f, const Grid& g,
+                                          long long cell, const float (&v)[19]) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Pop<S>::st_raw(f + q * g.plane + cell, v[q]);
 }
 
 // Zeroth, first and second raw moments of a population vector.
@@ -191,14 +215,16 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
         const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
         if (in_band(b, x, y, z, g.ny, g.nz)) return;
     }
+    // shifted storage: the collision works on the deviations (no per-population shift)
+    constexpr bool DEV = Pop<S>::kShifted;
     float f[19];
-    gather<S, PULL>(fin, g, c, x, y, z, f);
+    gather<S, PULL, true>(fin, g, c, x, y, z, f);
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
     if (FMODE == kForceNone || FMODE == kForceSkipBand) {
-        collide<false>(f, c, 0.f, 0.f, 0.f);
+        collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
     } else if (FMODE == kForceDense) {
         const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
-        collide<true>(f, c, fa.fx[cell], fa.fy[cell], Fz);
+        collide<true, DEV>(f, c, fa.fx[cell], fa.fy[cell], Fz);
     } else {
         const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
         if (in_band(b, x, y, z, g.ny, g.nz)) {
@@ -206,13 +232,12 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
             // fz is always zero there.
             const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
             const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
-            collide<true>(f, c, Fx, Fy, 0.0f);
+            collide<true, DEV>(f, c, Fx, Fy, 0.0f);
         } else {
-            collide<false>(f, c, 0.f, 0.f, 0.f);
+            collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
         }
     }
-#pragma unroll
-    for (int q = 0; q < 19; ++q) Pop<S>::st(fout + q * g.plane + cell, q, f[q]);
+    store_raw<S>(fout, g, cell, f);
 }
 
 // Forced stream-collide of the cells of the IBM force box; block bx of nbx (256 threads)
@@ -228,13 +253,12 @@ __device__ __forceinline__ void box_pass_body(const typename Pop<S>::T* __restri
         int x, y, z;
         box_cell(b, g.ny, g.nz, t, x, y, z);
         float f[19];
-        gather<S, PULL>(fin, g, c, x, y, z, f);
+        gather<S, PULL, true>(fin, g, c, x, y, z, f);
         const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
         const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
         const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
-        collide<true>(f, c, Fx, Fy, 0.0f);
-#pragma unroll
-        for (int q = 0; q < 19; ++q) Pop<S>::st(fout + q * g.plane + cell, q, f[q]);
+        collide<true, Pop<S>::kShifted>(f, c, Fx, Fy, 0.0f);
+        store_raw<S>(fout, g, cell, f);
     }
 }
 

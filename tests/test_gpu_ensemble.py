@@ -17,9 +17,11 @@ def _cases(pkg, storage, n=5):
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 @pytest.mark.parametrize("graph", [True, False])
-def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph):
+@pytest.mark.parametrize("variant", ["cell", "pair"])
+def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant):
+    """The single runs use either full-grid kernel; all variants give the same bits."""
     pkg = built_pkg
-    monkeypatch.setenv("CLBM_KERNEL", "cell")   # the ensemble's bulk pass is the cell kernel
+    monkeypatch.setenv("CLBM_KERNEL", variant)
     cases = _cases(pkg, storage)
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
