@@ -282,6 +282,7 @@ def run_gpu(args, rank, world, local):
     achieved = alg_bytes / (bulk_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = traffic_from_profile(args.storage)
+    variant = solver.kernel_variant()
     result = None
     if rank == 0:
         result = {
@@ -301,7 +302,9 @@ def run_gpu(args, rank, world, local):
             "gpu_launches": gpu_launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_stream_collide bulk pass (cells outside the force box)",
+                         "kernel": "bulk stream-collide pass (cells outside the force box), "
+                                   f"{variant['variant']} variant",
+                         "variant_autotune_us": variant["us_per_launch"],
                          "ms_per_launch": bulk_ms, "launches": prof["bulk_launches"],
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "cells_per_launch": bulk_cells,

@@ -57,6 +57,30 @@ struct Coef {
     float wc[19];     // w_q * (1 - s_v / 2), Guo forcing weight
 };
 
+// Learned sub-grid closure: a 19 -> 32 -> 32 -> 1 network (GELU, BF16 weights, FP32
+// accumulation) maps the 19 normalised non-equilibrium central moments of a cell to the
+// relaxation rate s_h of its third- and fourth-order central moments (the reference fixes
+// s_q = s_pi = 1, clbm_moving.py:186-194). Parameters are one float32 array:
+namespace closure {
+constexpr int kIn = 19;                        // input features (moment order of M_raw)
+constexpr int kHid = 32;                       // hidden width; inputs are padded to 32
+constexpr int kMu = 0;                         // [19] feature means
+constexpr int kSinv = 19;                      // [19] inverse feature scales
+constexpr int kW1 = 40;                        // [32 out][32 in], in >= 19 zero
+constexpr int kB1 = kW1 + kHid * kHid;         // [32]
+constexpr int kW2 = kB1 + kHid;                // [32 out][32 in]
+constexpr int kB2 = kW2 + kHid * kHid;         // [32]
+constexpr int kW3 = kB2 + kHid;                // [32]
+constexpr int kB3 = kW3 + kHid;                // [1]
+constexpr int kSpan = kB3 + 1;                 // [1] s_h = 1 + span * tanh(z3)
+constexpr int kParams = kSpan + 1;
+constexpr int kTrainable = kSpan - kW1;        // W1 .. b3
+// BF16 images of W1, W2 and W2^T in the K-major core-matrix layout of the MMAs.
+constexpr int kImgElems = 3 * kHid * kHid;
+constexpr int kTargets = 9;                    // third- and fourth-order moments per sample
+constexpr int kSampleFloats = kIn + 2 * kTargets;
+}  // namespace closure
+
 // Band box of the IBM stencils: all six entries are reduced with atomicMin, maxima stored
 // negated. The reset value 0x7f7f7f7f marks an empty box.
 constexpr int kBoxEmpty = 0x7f7f7f7f;
@@ -302,5 +326,50 @@ void launch_ens_box(int storage, bool pull, const EnsDesc* d, int n, int parity,
                     cudaStream_t st);
 void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,
                      int n, long long ntiles, int parity, int grid, cudaStream_t st);
+
+// ---- learned closure (closure.cu)
+struct ClosureArgs {
+    const float* params;      // closure parameter array (closure::kParams floats)
+    const uint16_t* img;      // BF16 weight images (closure::kImgElems)
+    long long cells;          // nx * ny * nz
+    long long tiles;          // ceil(cells / 128)
+};
+
+struct TrainArgs {
+    const float* samples;     // samples[i * stride + j]: 19 features, then 9 targets
+    long long stride;
+    long long off, count;     // sample range
+    long long batch;          // samples per call (random: drawn from the range with a hash)
+    unsigned long long seed;
+    int random;
+    int spin_limit;
+    const float* params;
+    const uint16_t* img;
+    float wscale;             // loss scale
+    float* part;              // per-block partials (closure_part_floats() each)
+    unsigned int* status;
+};
+
+void launch_closure_images(const float* params, uint16_t* img, cudaStream_t st);
+int closure_grid(int storage);
+void launch_closure_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
+                                   const Grid& g, const Coef& c, const ForceArgs& fa,
+                                   const ClosureArgs& ca, int grid, cudaStream_t st);
+void launch_filter2(bool pull, const float* ff, const Grid& gf, const Coef& cf, float* out,
+                    const Grid& gc, cudaStream_t st);
+void launch_closure_samples(const float* f0, const float* f1, const Grid& gc, const long long* cells,
+                            long long n, float* samples, long long stride, long long offset,
+                            cudaStream_t st);
+void launch_sample_stats(const float* s, long long stride, long long n, double* part, int blocks,
+                         double* out, cudaStream_t st);
+int closure_train_smem();
+int closure_part_floats();
+void launch_closure_train(const TrainArgs& a, bool grad, int grid, cudaStream_t st);
+void launch_closure_reduce(const float* part, int blocks, float inv_batch, float* grad, double* loss,
+                           cudaStream_t st);
+void launch_closure_adam(float* params, const float* grad, float* m1, float* m2, float lr, float b1,
+                         float b2, float eps, int t, cudaStream_t st);
+void launch_tc_selftest(const float* A, const float* B, float* D, int kdim, int n, unsigned int* status,
+                        int spin, cudaStream_t st);
 
 }  // namespace clbm

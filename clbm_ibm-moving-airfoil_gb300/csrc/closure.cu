@@ -1,0 +1,609 @@
+// closure.cu -- learned sub-grid closure: fused stream-collide with the network evaluated
+// on the tensor cores, training-sample extraction from box-filtered fine-lattice fields,
+// and the training kernels (forward, backward and weight gradients on the tensor cores,
+// deterministic reductions, Adam).
+//
+// The network maps the 19 normalised non-equilibrium central moments of a cell to the
+// rate s_h of its third- and fourth-order central moments, which the reference relaxes
+// fully (s_q = s_pi = 1, clbm_moving.py:186-194):
+//   k3* = (1 - s_h) k3,  k4* = r/9 + (1 - s_h)(k4 - r/9),  s_h = 1 + span tanh(z3).
+// Dense layers run as tcgen05 MMAs (BF16 operands from shared memory, FP32 accumulators in
+// tensor memory, M = 128 rows = one cell or sample per thread of a 128-thread block).
+#include <algorithm>
+#include <cstdint>
+
+#include "closure_device.cuh"
+
+namespace clbm {
+using namespace closure;
+
+// ------------------------------------------------------------------ weight images
+// BF16 images of W1 [out][in], W2 [out][in] and W2^T [in][out], each 32 x 32 in the
+// K-major core-matrix layout (the B operands of the forward and input-gradient MMAs).
+__global__ void k_closure_images(const float* __restrict__ p, uint16_t* __restrict__ img) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= kImgElems) return;
+    const int which = t >> 10, e = t & 1023, n = e >> 5, k = e & 31;
+    const float v = which == 0 ? p[kW1 + n * 32 + k] : which == 1 ? p[kW2 + n * 32 + k] : p[kW2 + k * 32 + n];
+    img[which * 1024 + (tc::kmajor_offset(n, k, 32) >> 1)] = bf16_bits(v);
+}
+
+void launch_closure_images(const float* params, uint16_t* img, cudaStream_t st) {
+    k_closure_images<<<(kImgElems + 255) / 256, 256, 0, st>>>(params, img);
+}
+
+namespace {
+
+constexpr uint32_t kIdescFwd = tc::idesc_bf16(128, 32);
+
+// Issue D = A (128 x 32, K-major) * B^T (32 x 32) as two K = 16 MMAs and commit.
+__device__ __forceinline__ void mma_k32(uint32_t tmem, uint32_t a, uint32_t b, uint64_t* bar) {
+    tc::mma(tmem, tc::smem_desc(a, 128, 512), tc::smem_desc(b, 128, 512), kIdescFwd, false);
+    tc::mma(tmem, tc::smem_desc(a + 256, 128, 512), tc::smem_desc(b + 256, 128, 512), kIdescFwd, true);
+    tc::commit(bar);
+}
+
+// Block-wide barrier that also orders tensor-core work around it.
+__device__ __forceinline__ void tc_sync() {
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ fused inference
+// Persistent stream-collide pass with the closure: 128 threads, one cell each; a block
+// takes tiles of 128 consecutive cells (x fastest across row ends). Per tile: gather,
+// moments and features (row of the A tile), layer 1 MMA, GELU, layer 2 MMA, GELU, output
+// layer on the CUDA cores, collision with s_h, store. Cells of the IBM force box (SkipBand)
+// are left to the box pass, which uses the plain collision with forcing.
+template <int S, bool PULL, int FMODE>
+__global__ void __launch_bounds__(128) k_closure_stream_collide(const typename Pop<S>::T* __restrict__ fin,
+                                                                typename Pop<S>::T* __restrict__ fout,
+                                                                Grid g, Coef c, ForceArgs fa,
+                                                                ClosureArgs ca) {
+    constexpr bool DEV = Pop<S>::kShifted;
+    __shared__ __align__(1024) unsigned char sA[128 * 32 * 2];
+    __shared__ __align__(1024) unsigned char sW[2 * 32 * 32 * 2];
+    __shared__ NetSmem net;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < (2 * 32 * 32 * 2) / 16; i += 128)
+        reinterpret_cast<uint4*>(sW)[i] = reinterpret_cast<const uint4*>(ca.img)[i];
+    load_net(ca.params, net, tid, 128);
+    if (warp == 0) tc::alloc(&tbase, 32);
+    if (tid == 0) tc::bar_init(&bar, 1);
+    tc_sync();
+    const uint32_t tm = tbase;
+    const uint32_t aA = tc::smem_addr(sA), aW1 = tc::smem_addr(sW), aW2 = aW1 + 2048;
+    uint32_t phase = 0;
+    bool ok = true;
+    const Band band = (FMODE == kForceSkipBand) ? band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz)
+                                                : Band{};
+    for (long long tile = blockIdx.x; tile < ca.tiles; tile += gridDim.x) {
+        const long long i = tile * 128 + tid;
+        bool use = i < ca.cells;
+        int x = 0, y = 0, z = 0;
+        if (use) {
+            const long long row = i / g.nx;
+            x = (int)(i - row * g.nx);
+            y = (int)(row % g.ny);
+            z = (int)(row / g.ny);
+            if (FMODE == kForceSkipBand && in_band(band, x, y, z, g.ny, g.nz)) use = false;
+        }
+        float f[19];
+        CMom m;
+        float v[32];
+        if (use) {
+            gather<S, PULL, true>(fin, g, c, x, y, z, f);
+            moments_full<DEV>(f, m);
+            standardise(m, net, v);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+        }
+        put_row32(sA, tid, v);
+        tc_sync();
+        if (tid == 0) mma_k32(tm, aA, aW1, &bar);
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, g.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+        tc::ld32(tc::lane_addr(tm, warp, 0), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = gelu(v[j] + net.b1[j]);
+        put_row32(sA, tid, v);
+        tc_sync();
+        if (tid == 0) mma_k32(tm, aA, aW2, &bar);
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, g.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+        tc::ld32(tc::lane_addr(tm, warp, 0), v);
+        float z3 = net.b3;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) z3 += net.w3[j] * gelu(v[j] + net.b2[j]);
+        const float sh = 1.0f + net.span * tanh_approx(z3);
+        if (use) {
+            float ho[9];
+            higher_order_post(m, sh, ho);
+            collide_ho<DEV>(f, c, ho);
+            store_raw<S>(fout, g, ((long long)z * g.ny + y) * g.pitch + x, f);
+        }
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(g.status, kStatusWaitTimeout);
+        tc::bar_wait(&bar, phase ^ 1, g.spin_limit);  // the MMA that did not report in time
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::dealloc(tm, 32);
+}
+
+#define CLBM_CL_STORE(storage, ...)                                                          \
+    switch (storage) {                                                                       \
+        case CLBM_STORE_F32: { constexpr int S_ = CLBM_STORE_F32; __VA_ARGS__; } break;     \
+        case CLBM_STORE_F16S: { constexpr int S_ = CLBM_STORE_F16S; __VA_ARGS__; } break;   \
+        default: { constexpr int S_ = CLBM_STORE_BF16S; __VA_ARGS__; } break;               \
+    }
+
+template <int S, bool PULL>
+static void closure_sc(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                       const ForceArgs& fa, const ClosureArgs& ca, int grid, cudaStream_t st) {
+    using T = typename Pop<S>::T;
+    if (fmode == kForceSkipBand)
+        k_closure_stream_collide<S, PULL, kForceSkipBand><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+    else
+        k_closure_stream_collide<S, PULL, kForceNone><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+}
+
+int closure_grid(int storage) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    CLBM_CL_STORE(storage, {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_closure_stream_collide<S_, true, kForceSkipBand>, 128, 0);
+    });
+    // tensor memory: 32 columns per block, 512 per SM
+    per = std::min(std::max(per, 1), 16);
+    return std::max(sms, 1) * per;
+}
+
+void launch_closure_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
+                                   const Grid& g, const Coef& c, const ForceArgs& fa,
+                                   const ClosureArgs& ca, int grid, cudaStream_t st) {
+    CLBM_CL_STORE(storage, {
+        if (pull) closure_sc<S_, true>(fmode, fin, fout, g, c, fa, ca, grid, st);
+        else closure_sc<S_, false>(fmode, fin, fout, g, c, fa, ca, grid, st);
+    });
+}
+
+// ------------------------------------------------------------------ training samples
+// Box filter of a fine lattice twice as fine in each direction: coarse cell (I, J, K) gets
+// the mean of the post-stream (pre-collision) populations of fine cells (2I + a, 2J + b,
+// 2K + c), a, b, c in {0, 1}. Float32 fine storage.
+template <bool PULL>
+__global__ void __launch_bounds__(128) k_filter2(const float* __restrict__ ff, Grid gf, Coef cf,
+                                                 float* __restrict__ out, Grid gc) {
+    const int X = blockIdx.x * 128 + threadIdx.x, Y = blockIdx.y, Z = blockIdx.z;
+    if (X >= gc.nx) return;
+    float acc[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) acc[q] = 0.0f;
+    for (int s = 0; s < 8; ++s) {
+        float v[19];
+        gather<CLBM_STORE_F32, PULL, false>(ff, gf, cf, 2 * X + (s & 1), 2 * Y + ((s >> 1) & 1),
+                                            2 * Z + (s >> 2), v);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) acc[q] += v[q];
+    }
+    const long long cell = ((long long)Z * gc.ny + Y) * gc.pitch + X;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) out[q * gc.plane + cell] = 0.125f * acc[q];
+}
+
+void launch_filter2(bool pull, const float* ff, const Grid& gf, const Coef& cf, float* out,
+                    const Grid& gc, cudaStream_t st) {
+    const dim3 grid((gc.nx + 127) / 128, gc.ny, gc.nz);
+    if (pull) k_filter2<true><<<grid, 128, 0, st>>>(ff, gf, cf, out, gc);
+    else k_filter2<false><<<grid, 128, 0, st>>>(ff, gf, cf, out, gc);
+}
+
+// Sample j: coarse cell cells[j] (x + nx (y + ny z), 1 <= x <= nx - 2). Features from the
+// filtered pre-collision state f0; targets from the ideal post-collision state
+// f*_q(x) = f1_q(x + e_q) (f1 one coarse step later), as central moments about the
+// velocity of f0, divided by its density: samples[i * stride + offset + j], i < 19
+// features, 19 <= i < 28 targets (third order, then fourth order minus rho*/9).
+__global__ void k_closure_samples(const float* __restrict__ f0, const float* __restrict__ f1, Grid gc,
+                                  const long long* __restrict__ cells, long long n,
+                                  float* __restrict__ samples, long long stride, long long offset) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const long long id = cells[j];
+    const int x = (int)(id % gc.nx);
+    const long long row = id / gc.nx;
+    const int y = (int)(row % gc.ny), z = (int)(row / gc.ny);
+    const long long cell = ((long long)z * gc.ny + y) * gc.pitch + x;
+    float f[19], fs[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = f0[q * gc.plane + cell];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        int yy = y + ey(q), zz = z + ez(q);
+        yy = yy < 0 ? yy + gc.ny : (yy >= gc.ny ? yy - gc.ny : yy);
+        zz = zz < 0 ? zz + gc.nz : (zz >= gc.nz ? zz - gc.nz : zz);
+        fs[q] = f1[q * gc.plane + ((long long)zz * gc.ny + yy) * gc.pitch + x + ex(q)];
+    }
+    CMom m;
+    moments_full<false>(f, m);
+    const Raw rs = raw_moments<false>(fs);
+    float t[kIn];
+    central_moments(rs, m.u, m.v, m.w, m.r, t);
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) samples[i * stride + offset + j] = m.x[i];
+#pragma unroll
+    for (int i = 0; i < kTargets; ++i) samples[(kIn + i) * stride + offset + j] = t[10 + i];
+}
+
+void launch_closure_samples(const float* f0, const float* f1, const Grid& gc, const long long* cells,
+                            long long n, float* samples, long long stride, long long offset,
+                            cudaStream_t st) {
+    if (n <= 0) return;
+    k_closure_samples<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f0, f1, gc, cells, n, samples, stride,
+                                                                  offset);
+}
+
+// Per-block partial sums of the features and their squares over samples [0, n) and of the
+// squared pre-collision higher-order moments (sum_j x_{10+j}^2), for the standardisation
+// and the loss scale; reduced in a fixed order by k_stats_final.
+constexpr int kStats = 2 * kIn + 1;
+__global__ void __launch_bounds__(256) k_sample_stats(const float* __restrict__ s, long long stride,
+                                                      long long n, double* __restrict__ part) {
+    __shared__ double red[256];
+    double acc[kStats];
+#pragma unroll
+    for (int i = 0; i < kStats; ++i) acc[i] = 0.0;
+    for (long long j = (long long)blockIdx.x * 256 + threadIdx.x; j < n; j += (long long)gridDim.x * 256) {
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) {
+            const double v = s[i * stride + j];
+            acc[i] += v;
+            acc[kIn + i] += v * v;
+            if (i >= 10) acc[2 * kIn] += v * v;
+        }
+    }
+    for (int i = 0; i < kStats; ++i) {
+        red[threadIdx.x] = acc[i];
+        __syncthreads();
+        for (int w = 128; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[(long long)blockIdx.x * kStats + i] = red[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_stats_final(const double* __restrict__ part, int blocks, double* __restrict__ out) {
+    const int i = threadIdx.x;
+    if (i >= kStats) return;
+    double a = 0.0;
+    for (int b = 0; b < blocks; ++b) a += part[(long long)b * kStats + i];
+    out[i] = a;
+}
+
+void launch_sample_stats(const float* s, long long stride, long long n, double* part, int blocks,
+                         double* out, cudaStream_t st) {
+    k_sample_stats<<<blocks, 256, 0, st>>>(s, stride, n, part);
+    k_stats_final<<<1, 64, 0, st>>>(part, blocks, out);
+}
+
+// ------------------------------------------------------------------ training
+// Shared-memory plan of the training kernel (dynamic, 1024-byte aligned):
+//   sX   128 x 32   K-major: features, then h1, then delta2 (A of the three 32-wide MMAs)
+//   sW   W1, W2, W2^T images (B operands)
+//   sAw  128 x 128  K-major over samples: rows 0-31 delta1^T, 32-63 delta2^T, 64 delta3
+//   sBw  112 x 128  K-major over samples: rows 0-31 x^T, 32-63 h1^T, 64 ones, 80-111 h2^T
+// Weight and bias gradients are one MMA chain per tile, D[128 x 112] += sAw * sBw^T,
+// accumulated over the block's tiles in tensor-memory columns 32-143:
+//   D[o][n]          o < 32: dW1[o][n] (n < 32), db1[o] (n = 64)
+//   D[32 + o][32 + n]        dW2[o][n],          db2[o] (n = 64)
+//   D[64][80 + n]            dW3[n],             db3    (n = 64)
+constexpr int kTrSX = 0, kTrSW = 8192, kTrAw = kTrSW + 6144, kTrBw = kTrAw + 32768;
+constexpr int kTrSmem = kTrBw + 112 * 128 * 2;  // 75,776 bytes
+constexpr int kPart = kTrainable + 1;           // gradients, then the loss sum
+constexpr uint32_t kIdescW = tc::idesc_bf16(128, 112);
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ void put_col(unsigned char* tile, int row, int col, float v) {
+    *reinterpret_cast<uint16_t*>(tile + tc::kmajor_offset(row, col, 128)) = bf16_bits(v);
+}
+
+template <bool GRAD>
+__global__ void __launch_bounds__(128) k_closure_train(TrainArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ NetSmem net;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    __shared__ float red[128];
+    unsigned char* sX = smem + kTrSX;
+    unsigned char* sW = smem + kTrSW;
+    unsigned char* sAw = smem + kTrAw;
+    unsigned char* sBw = smem + kTrBw;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < 6144 / 16; i += 128)
+        reinterpret_cast<uint4*>(sW)[i] = reinterpret_cast<const uint4*>(a.img)[i];
+    // zero the weight-gradient operands once (rows that stay zero)
+    for (int i = tid; i < (32768 + 112 * 128 * 2) / 16; i += 128)
+        reinterpret_cast<uint4*>(sAw)[i] = make_uint4(0, 0, 0, 0);
+    load_net(a.params, net, tid, 128);
+    if (warp == 0) tc::alloc(&tbase, 256);
+    if (tid == 0) tc::bar_init(&bar, 1);
+    tc_sync();
+    const uint32_t tm = tbase;
+    const uint32_t aX = tc::smem_addr(sX), aW1 = tc::smem_addr(sW), aW2 = aW1 + 2048, aW2T = aW1 + 4096;
+    const uint32_t aAw = tc::smem_addr(sAw), aBw = tc::smem_addr(sBw);
+    uint32_t phase = 0;
+    bool ok = true;
+    float loss = 0.0f;
+    int ntile = 0;
+    const long long tiles = (a.batch + 127) / 128;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++ntile) {
+        const long long slot = tile * 128 + tid;
+        const bool valid = slot < a.batch;
+        long long sidx = 0;
+        if (valid)
+            sidx = a.random ? a.off + (long long)(mix64(a.seed ^ (unsigned long long)slot) % (unsigned long long)a.count)
+                            : a.off + slot;
+        float x[kIn], tg[kTargets];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) x[i] = valid ? a.samples[i * a.stride + sidx] : 0.0f;
+#pragma unroll
+        for (int i = 0; i < kTargets; ++i) tg[i] = valid ? a.samples[(kIn + i) * a.stride + sidx] : 0.0f;
+        float v[32], z1[32];
+#pragma unroll
+        for (int i = 0; i < kIn; ++i) v[i] = valid ? (x[i] - net.mu[i]) * net.sinv[i] : 0.0f;
+#pragma unroll
+        for (int i = kIn; i < 32; ++i) v[i] = 0.0f;
+        put_row32(sX, tid, v);
+        if (GRAD) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) put_col(sBw, i, tid, v[i]);
+            put_col(sBw, 64, tid, valid ? 1.0f : 0.0f);
+        }
+        tc_sync();
+        if (tid == 0) mma_k32(tm, aX, aW1, &bar);
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, a.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+        tc::ld32(tc::lane_addr(tm, warp, 0), z1);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            z1[j] += net.b1[j];
+            v[j] = gelu(z1[j]);
+        }
+        put_row32(sX, tid, v);
+        if (GRAD) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) put_col(sBw, 32 + j, tid, v[j]);
+        }
+        tc_sync();
+        if (tid == 0) mma_k32(tm, aX, aW2, &bar);
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, a.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+        tc::ld32(tc::lane_addr(tm, warp, 0), v);  // z2 - b2
+        float z3 = net.b3;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            v[j] += net.b2[j];
+            z3 += net.w3[j] * gelu(v[j]);
+        }
+        const float th = tanh_approx(z3);
+        const float oms = -net.span * th;  // 1 - s_h
+        float dlds = 0.0f;
+#pragma unroll
+        for (int i = 0; i < kTargets; ++i) {
+            const float p = x[10 + i];
+            const float r = tg[i] - oms * p;
+            loss += valid ? a.wscale * r * r : 0.0f;
+            dlds += 2.0f * a.wscale * r * p;
+        }
+        if (!GRAD) continue;
+        const float d3 = valid ? dlds * net.span * (1.0f - th * th) : 0.0f;
+        put_col(sAw, 64, tid, d3);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float h2 = gelu(v[j]);
+            put_col(sBw, 80 + j, tid, h2);
+            v[j] = d3 * net.w3[j] * gelu_grad(v[j]);  // delta2
+            put_col(sAw, 32 + j, tid, v[j]);
+        }
+        put_row32(sX, tid, v);
+        tc_sync();
+        if (tid == 0) mma_k32(tm, aX, aW2T, &bar);  // dh1 = delta2 W2
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, a.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+        tc::ld32(tc::lane_addr(tm, warp, 0), v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) put_col(sAw, j, tid, v[j] * gelu_grad(z1[j]));  // delta1
+        tc_sync();
+        if (tid == 0) {
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk)
+                tc::mma(tm + 32, tc::smem_desc(aAw + 256 * kk, 128, 2048), tc::smem_desc(aBw + 256 * kk, 128, 2048),
+                        kIdescW, ntile > 0 || kk > 0);
+            tc::commit(&bar);
+        }
+        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, a.spin_limit));
+        phase ^= 1;
+        if (!ok) break;
+        tc::fence_after();
+    }
+    float* part = a.part + (long long)blockIdx.x * kPart;
+    if (!ok) {
+        if (tid == 0) atomicOr(a.status, kStatusWaitTimeout);
+        tc::bar_wait(&bar, phase ^ 1, a.spin_limit);
+    }
+    // loss: block sum in a fixed order
+    red[tid] = loss;
+    __syncthreads();
+    if (tid == 0) {
+        float s = 0.0f;
+        for (int i = 0; i < 128; ++i) s += red[i];
+        part[kTrainable] = s;
+    }
+    if (GRAD) {
+        tc::fence_after();
+        float d[32];
+        if (warp < 3) {
+            const bool have = ok && ntile > 0;
+            // lanes 0-31: dW1 rows, lanes 32-63: dW2 rows, lane 64: dW3 (row 64 of D)
+            const int col = warp == 0 ? 32 : (warp == 1 ? 64 : 112);
+            tc::ld32(tc::lane_addr(tm, warp, col), d);
+            float db[32];
+            tc::ld32(tc::lane_addr(tm, warp, 96), db);
+            const int o = tid & 31;
+            if (warp == 0) {
+                for (int n = 0; n < 32; ++n) part[kW1 - kW1 + o * 32 + n] = have ? d[n] : 0.0f;
+                part[kB1 - kW1 + o] = have ? db[0] : 0.0f;
+            } else if (warp == 1) {
+                for (int n = 0; n < 32; ++n) part[kW2 - kW1 + o * 32 + n] = have ? d[n] : 0.0f;
+                part[kB2 - kW1 + o] = have ? db[0] : 0.0f;
+            } else if (o == 0) {
+                for (int n = 0; n < 32; ++n) part[kW3 - kW1 + n] = have ? d[n] : 0.0f;
+                part[kB3 - kW1] = have ? db[0] : 0.0f;
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::dealloc(tm, 256);
+}
+
+// Gradient of the mean loss and the loss sum: fixed-order sums of the block partials.
+__global__ void k_closure_reduce(const float* __restrict__ part, int blocks, float inv_batch,
+                                 float* __restrict__ grad, double* __restrict__ loss) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > kTrainable) return;
+    if (j == kTrainable) {
+        double s = 0.0;
+        for (int b = 0; b < blocks; ++b) s += part[(long long)b * kPart + j];
+        *loss = s;
+        return;
+    }
+    float s = 0.0f;
+    for (int b = 0; b < blocks; ++b) s += part[(long long)b * kPart + j];
+    grad[j] = s * inv_batch;
+}
+
+// Adam (Kingma and Ba) on the trainable block of the parameters, step t (from 1).
+__global__ void k_closure_adam(float* __restrict__ p, const float* __restrict__ grad, float* __restrict__ m1,
+                               float* __restrict__ m2, float lr, float b1, float b2, float eps, int t) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kTrainable) return;
+    const int in = (j < 1024) ? (j & 31) : 0;
+    if (j < 1024 && in >= kIn) return;  // padded inputs of W1 stay zero
+    const float g = grad[j];
+    const float a = b1 * m1[j] + (1.0f - b1) * g;
+    const float b = b2 * m2[j] + (1.0f - b2) * g * g;
+    m1[j] = a;
+    m2[j] = b;
+    const float ah = a / (1.0f - powf(b1, (float)t)), bh = b / (1.0f - powf(b2, (float)t));
+    p[kW1 + j] -= lr * ah / (sqrtf(bh) + eps);
+}
+
+int closure_train_smem() { return kTrSmem; }
+int closure_part_floats() { return kPart; }
+
+void launch_closure_train(const TrainArgs& a, bool grad, int grid, cudaStream_t st) {
+    if (grad) {
+        cudaFuncSetAttribute(k_closure_train<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
+        k_closure_train<true><<<grid, 128, kTrSmem, st>>>(a);
+    } else {
+        cudaFuncSetAttribute(k_closure_train<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrSmem);
+        k_closure_train<false><<<grid, 128, kTrSmem, st>>>(a);
+    }
+}
+
+void launch_closure_reduce(const float* part, int blocks, float inv_batch, float* grad, double* loss,
+                           cudaStream_t st) {
+    k_closure_reduce<<<(kTrainable + 1 + 255) / 256, 256, 0, st>>>(part, blocks, inv_batch, grad, loss);
+}
+
+void launch_closure_adam(float* params, const float* grad, float* m1, float* m2, float lr, float b1,
+                         float b2, float eps, int t, cudaStream_t st) {
+    k_closure_adam<<<(kTrainable + 255) / 256, 256, 0, st>>>(params, grad, m1, m2, lr, b1, b2, eps, t);
+}
+
+// ------------------------------------------------------------------ self tests
+// D (128 x n) = A (128 x k) * B^T (n x k) through one MMA chain (k = 32 or 128, n = 32 or
+// 112), operands rounded to bf16: checks the operand layout, the descriptors and the
+// accumulator lanes against a host product.
+__global__ void __launch_bounds__(128) k_tc_selftest(const float* __restrict__ A, const float* __restrict__ B,
+                                                     float* __restrict__ D, int kdim, int n,
+                                                     unsigned int* status, int spin) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tbase;
+    unsigned char* sa = smem;
+    unsigned char* sb = smem + 128 * kdim * 2;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int k = 0; k < kdim; ++k)
+        *reinterpret_cast<uint16_t*>(sa + tc::kmajor_offset(tid, k, kdim)) = bf16_bits(A[tid * kdim + k]);
+    if (tid < n)
+        for (int k = 0; k < kdim; ++k)
+            *reinterpret_cast<uint16_t*>(sb + tc::kmajor_offset(tid, k, kdim)) = bf16_bits(B[tid * kdim + k]);
+    if (warp == 0) tc::alloc(&tbase, 128);
+    if (tid == 0) tc::bar_init(&bar, 1);
+    tc_sync();
+    const uint32_t tm = tbase;
+    const uint32_t sbo = (uint32_t)(kdim / 8) * 128;
+    if (tid == 0) {
+        const uint32_t id = tc::idesc_bf16(128, n);
+        for (int kk = 0; kk < kdim / 16; ++kk)
+            tc::mma(tm, tc::smem_desc(tc::smem_addr(sa) + 256 * kk, 128, sbo),
+                    tc::smem_desc(tc::smem_addr(sb) + 256 * kk, 128, sbo), id, kk > 0);
+        tc::commit(&bar);
+    }
+    const bool ok = !__syncthreads_or(!tc::bar_wait(&bar, 0, spin));
+    if (!ok) {
+        if (tid == 0) atomicOr(status, kStatusWaitTimeout);
+        tc::bar_wait(&bar, 0, spin);
+    } else {
+        tc::fence_after();
+        for (int c0 = 0; c0 < n; c0 += 32) {
+            float v[32];
+            tc::ld32(tc::lane_addr(tm, warp, c0), v);
+            for (int j = 0; j < 32 && c0 + j < n; ++j) D[tid * n + c0 + j] = v[j];
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::dealloc(tm, 128);
+}
+
+void launch_tc_selftest(const float* A, const float* B, float* D, int kdim, int n, unsigned int* status,
+                        int spin, cudaStream_t st) {
+    const int smem = 128 * kdim * 2 + 128 * kdim * 2;
+    cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_tc_selftest<<<1, 128, smem, st>>>(A, B, D, kdim, n, status, spin);
+}
+
+}  // namespace clbm

@@ -1,0 +1,203 @@
+// closure_device.cuh -- device functions of the learned sub-grid closure: the moment
+// features of a cell, the closure relaxation of its third- and fourth-order central
+// moments, and the pieces of the 19 -> 32 -> 32 -> 1 network shared by the fused
+// stream-collide kernel, the training kernel and the self tests.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "lbm_device.cuh"
+#include "tc.cuh"
+
+namespace clbm {
+namespace closure {
+
+// Moments of one cell about its velocity u = m / rho (closure cells carry no body force).
+struct CMom {
+    float r;        // density
+    float u, v, w;  // velocity
+    float x[kIn];   // non-equilibrium central moments / rho, in the M_raw order
+                    // (config_moving.py:62-68): 000, 100, 010, 001, 110, 101, 011,
+                    // 200, 020, 002, 210, 120, 201, 021, 102, 012, 220, 202, 022
+};
+
+// Raw moments of a population vector up to the fourth order present in D3Q19. DEV: f holds
+// deviations f - w; the weights' part of the even moments is kept apart (sum w = 1,
+// sum w e_a^2 = 1/3, sum w e_a^2 e_b^2 = 1/9; odd moments of w vanish).
+struct Raw {
+    float R0;                  // sum f (deviations: sum of deviations)
+    float r;                   // density
+    float mx, my, mz;
+    float Pxx, Pyy, Pzz;       // second diagonal, without the weights' part
+    float Mxx, Myy, Mzz;       // second diagonal, full
+    float pxy, pxz, pyz;
+    float M210, M120, M201, M021, M102, M012;
+    float A220, A202, A022;    // fourth, without the weights' part
+};
+
+template <bool DEV>
+__device__ __forceinline__ Raw raw_moments(const float (&f)[19]) {
+    Raw m;
+    const float sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+    const float a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
+    const float e = f[15] + f[16], h = f[17] + f[18];
+    m.R0 = f[0] + (sx + sy + sz) + (a + b) + (cc + d) + (e + h);
+    m.mx = (f[1] - f[2]) + (f[7] - f[8]) + (f[9] - f[10]) + (f[11] - f[12]) + (f[13] - f[14]);
+    m.my = (f[3] - f[4]) + (a - b) + (f[15] - f[16]) + (f[17] - f[18]);
+    m.mz = (f[5] - f[6]) + (cc - d) + (e - h);
+    m.Pxx = sx + (a + b) + (cc + d);
+    m.Pyy = sy + (a + b) + (e + h);
+    m.Pzz = sz + (cc + d) + (e + h);
+    m.pxy = (f[7] + f[10]) - (f[8] + f[9]);
+    m.pxz = (f[11] + f[14]) - (f[12] + f[13]);
+    m.pyz = (f[15] + f[18]) - (f[16] + f[17]);
+    // plane diagonals e = (+1,+1), (-1,+1), (+1,-1), (-1,-1) in each plane
+    m.M210 = a - b;
+    m.M120 = (f[7] - f[8]) + (f[9] - f[10]);
+    m.M201 = cc - d;
+    m.M102 = (f[11] - f[12]) + (f[13] - f[14]);
+    m.M021 = e - h;
+    m.M012 = (f[15] - f[16]) + (f[17] - f[18]);
+    m.A220 = a + b;
+    m.A202 = cc + d;
+    m.A022 = e + h;
+    const float s3 = DEV ? 1.0f / 3.0f : 0.0f;
+    m.r = m.R0 + (DEV ? 1.0f : 0.0f);
+    m.Mxx = m.Pxx + s3;
+    m.Myy = m.Pyy + s3;
+    m.Mzz = m.Pzz + s3;
+    return m;
+}
+
+// Non-equilibrium central moments about the velocity (u, v, w), divided by rho_n, by the
+// binomial expansion of sum f (e_x - u)^p (e_y - v)^q (e_z - w)^r; the equilibrium
+// values subtracted are rho/3 (second diagonal) and rho/9 (fourth).
+__device__ __forceinline__ void central_moments(const Raw& m, float u, float v, float w, float rho_n,
+                                                float (&x)[kIn]) {
+    const float r = m.r, R0 = m.R0;
+    const float mx = m.mx, my = m.my, mz = m.mz;
+    const float ur = u * r, vr = v * r, wr = w * r;
+    const float uu = u * u, vv = v * v, ww = w * w;
+    float k[kIn];
+    k[0] = 0.0f;
+    k[1] = mx - ur;
+    k[2] = my - vr;
+    k[3] = mz - wr;
+    k[4] = m.pxy - u * my - v * mx + u * vr;
+    k[5] = m.pxz - u * mz - w * mx + u * wr;
+    k[6] = m.pyz - v * mz - w * my + v * wr;
+    // k200 - r/3 = (P - R0/3) - 2u mx + u^2 r
+    k[7] = (m.Pxx - R0 * (1.0f / 3.0f)) + u * (ur - 2.0f * mx);
+    k[8] = (m.Pyy - R0 * (1.0f / 3.0f)) + v * (vr - 2.0f * my);
+    k[9] = (m.Pzz - R0 * (1.0f / 3.0f)) + w * (wr - 2.0f * mz);
+    // third order, e.g. k210 = M210 - 2u M110 - v M200 + 2uv M100 + u^2 M010 - u^2 v M000
+    k[10] = m.M210 - 2.0f * u * m.pxy - v * m.Mxx + 2.0f * u * v * mx + uu * (my - vr);
+    k[11] = m.M120 - 2.0f * v * m.pxy - u * m.Myy + 2.0f * u * v * my + vv * (mx - ur);
+    k[12] = m.M201 - 2.0f * u * m.pxz - w * m.Mxx + 2.0f * u * w * mx + uu * (mz - wr);
+    k[13] = m.M021 - 2.0f * v * m.pyz - w * m.Myy + 2.0f * v * w * my + vv * (mz - wr);
+    k[14] = m.M102 - 2.0f * w * m.pxz - u * m.Mzz + 2.0f * u * w * mz + ww * (mx - ur);
+    k[15] = m.M012 - 2.0f * w * m.pyz - v * m.Mzz + 2.0f * v * w * mz + ww * (my - vr);
+    // fourth order, e.g. k220 - r/9 = (A220 - R0/9) - 2v M210 - 2u M120 + v^2 M200
+    //   + u^2 M020 + 4uv M110 - 2uv^2 M100 - 2u^2 v M010 + u^2 v^2 M000
+    k[16] = (m.A220 - R0 * (1.0f / 9.0f)) - 2.0f * v * m.M210 - 2.0f * u * m.M120 + vv * m.Mxx +
+            uu * m.Myy + 4.0f * u * v * m.pxy - 2.0f * u * vv * mx - 2.0f * uu * v * my + uu * vv * r;
+    k[17] = (m.A202 - R0 * (1.0f / 9.0f)) - 2.0f * w * m.M201 - 2.0f * u * m.M102 + ww * m.Mxx +
+            uu * m.Mzz + 4.0f * u * w * m.pxz - 2.0f * u * ww * mx - 2.0f * uu * w * mz + uu * ww * r;
+    k[18] = (m.A022 - R0 * (1.0f / 9.0f)) - 2.0f * w * m.M021 - 2.0f * v * m.M012 + ww * m.Myy +
+            vv * m.Mzz + 4.0f * v * w * m.pyz - 2.0f * v * ww * my - 2.0f * vv * w * mz + vv * ww * r;
+    const float inv = 1.0f / rho_n;
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) x[i] = k[i] * inv;
+}
+
+// Moments of a cell about its own velocity u = m / rho (closure cells carry no force).
+template <bool DEV>
+__device__ __forceinline__ void moments_full(const float (&f)[19], CMom& c) {
+    const Raw m = raw_moments<DEV>(f);
+    const float inv = 1.0f / m.r;
+    c.r = m.r;
+    c.u = m.mx * inv;
+    c.v = m.my * inv;
+    c.w = m.mz * inv;
+    central_moments(m, c.u, c.v, c.w, m.r, c.x);
+}
+
+// GELU, tanh form (Hendrycks and Gimpel), with the hardware tanh approximation.
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu(float z) {
+    const float t = tanh_approx(0.7978845608028654f * (z + 0.044715f * z * z * z));
+    return 0.5f * z * (1.0f + t);
+}
+// d gelu / dz for the same form.
+__device__ __forceinline__ float gelu_grad(float z) {
+    const float k = 0.7978845608028654f;
+    const float t = tanh_approx(k * (z + 0.044715f * z * z * z));
+    return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k * (1.0f + 3.0f * 0.044715f * z * z);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(float x) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+__device__ __forceinline__ float bf16_round(float x) {
+    return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+// Write one row (32 values, rounded to bf16) of a K-major tile with 32 columns.
+__device__ __forceinline__ void put_row32(unsigned char* tile, int row, const float (&v)[32]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t wv[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            wv[t] = (uint32_t)bf16_bits(v[8 * j + 2 * t]) | ((uint32_t)bf16_bits(v[8 * j + 2 * t + 1]) << 16);
+        *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(row, 8 * j, 32)) =
+            make_uint4(wv[0], wv[1], wv[2], wv[3]);
+    }
+}
+
+// Network constants a block keeps in shared memory next to the BF16 weight images.
+struct NetSmem {
+    float mu[kIn], sinv[kIn];
+    float b1[kHid], b2[kHid], w3[kHid];
+    float b3, span;
+};
+
+__device__ __forceinline__ void load_net(const float* __restrict__ p, NetSmem& n, int tid, int nthreads) {
+    for (int i = tid; i < kIn; i += nthreads) {
+        n.mu[i] = p[kMu + i];
+        n.sinv[i] = p[kSinv + i];
+    }
+    for (int i = tid; i < kHid; i += nthreads) {
+        n.b1[i] = p[kB1 + i];
+        n.b2[i] = p[kB2 + i];
+        n.w3[i] = bf16_round(p[kW3 + i]);
+    }
+    if (tid == 0) {
+        n.b3 = p[kB3];
+        n.span = p[kSpan];
+    }
+}
+
+// Standardised features of a cell, padded to 32 with zeros.
+__device__ __forceinline__ void standardise(const CMom& m, const NetSmem& n, float (&xs)[32]) {
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) xs[i] = (m.x[i] - n.mu[i]) * n.sinv[i];
+#pragma unroll
+    for (int i = kIn; i < 32; ++i) xs[i] = 0.0f;
+}
+
+// Post-collision third-order central moments and fourth-order deviations from r/9 for
+// the rate s_h: k3* = (1 - s_h) k3, k4* - r/9 = (1 - s_h)(k4 - r/9) (in the layout that
+// collide_v<.., HO = true> takes). x holds the moments divided by r.
+__device__ __forceinline__ void higher_order_post(const CMom& m, float sh, float (&ho)[9]) {
+    const float g = (1.0f - sh) * m.r;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) ho[i] = g * m.x[10 + i];
+}
+
+}  // namespace closure
+}  // namespace clbm

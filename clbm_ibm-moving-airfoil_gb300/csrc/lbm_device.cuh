@@ -2,6 +2,8 @@
 // single-lattice kernels (lbm_kernels.cu) and the batched ensemble kernels (ensemble.cu).
 #pragma once
 
+#include <type_traits>
+
 #include "clbm_internal.cuh"
 
 namespace clbm {
@@ -101,106 +103,266 @@ __device__ __forceinline__ Moments moments(const float (&f)[19]) {
     return m;
 }
 
+// ---------------------------------------------------------------- collision arithmetic
+// The collision is written once over a value type V:
+//   F1  one float32 (one cell), plain operators: the compiler may contract a*b + c;
+//   V1  one float32 with explicitly rounded operations (no contraction);
+//   V2  two float32 lanes (two cells) evaluated by the packed f32x2 instructions of
+//       sm_100-class GPUs, which halve the issue slots of the arithmetic.
+// V1 and V2 perform the same IEEE round-to-nearest operations, so the 16-bit kernels that
+// compute one cell (V1) or two cells (V2) per thread give identical bits. The float32
+// kernels are bound by memory bandwidth and use F1.
+struct F1 {
+    float x;
+};
+struct V1 {
+    float x;
+};
+struct V2 {
+    unsigned long long x;
+};
+
+__device__ __forceinline__ F1 operator+(F1 a, F1 b) { return {a.x + b.x}; }
+__device__ __forceinline__ F1 operator-(F1 a, F1 b) { return {a.x - b.x}; }
+__device__ __forceinline__ F1 operator*(F1 a, F1 b) { return {a.x * b.x}; }
+__device__ __forceinline__ F1 vfma(F1 a, F1 b, F1 c) { return {fmaf(a.x, b.x, c.x)}; }
+__device__ __forceinline__ F1 vsplat(float a, F1) { return {a}; }
+__device__ __forceinline__ F1 vrcp(F1 a) { return {__frcp_rn(a.x)}; }
+
+__device__ __forceinline__ V1 operator+(V1 a, V1 b) { return {__fadd_rn(a.x, b.x)}; }
+__device__ __forceinline__ V1 operator-(V1 a, V1 b) { return {__fsub_rn(a.x, b.x)}; }
+__device__ __forceinline__ V1 operator*(V1 a, V1 b) { return {__fmul_rn(a.x, b.x)}; }
+__device__ __forceinline__ V1 vfma(V1 a, V1 b, V1 c) { return {__fmaf_rn(a.x, b.x, c.x)}; }
+__device__ __forceinline__ V1 vsplat(float a, V1) { return {a}; }
+__device__ __forceinline__ V1 vrcp(V1 a) { return {__frcp_rn(a.x)}; }
+
+__device__ __forceinline__ V2 operator+(V2 a, V2 b) {
+    V2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d.x) : "l"(a.x), "l"(b.x));
+    return d;
+}
+__device__ __forceinline__ V2 operator-(V2 a, V2 b) {
+    V2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.x) : "l"(a.x), "l"(b.x));
+    return d;
+}
+__device__ __forceinline__ V2 operator*(V2 a, V2 b) {
+    V2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.x) : "l"(a.x), "l"(b.x));
+    return d;
+}
+__device__ __forceinline__ V2 vfma(V2 a, V2 b, V2 c) {
+    V2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.x) : "l"(a.x), "l"(b.x), "l"(c.x));
+    return d;
+}
+__device__ __forceinline__ V2 vpack(float a, float b) {
+    V2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d.x) : "f"(a), "f"(b));
+    return d;
+}
+__device__ __forceinline__ float2 vunpack(V2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v.x));
+    return r;
+}
+__device__ __forceinline__ V2 vsplat(float a, V2) { return vpack(a, a); }
+__device__ __forceinline__ V2 vrcp(V2 a) {
+    const float2 t = vunpack(a);
+    return vpack(__frcp_rn(t.x), __frcp_rn(t.y));
+}
+
 // Cascaded collision in central-moment space followed by the raw-moment back transform,
-// in place on f. (Fx, Fy, Fz) is the body-force density at the cell.
+// in place on f. (Fx, Fy, Fz) is the body-force density at the cell (zero gives the
+// unforced result).
 // DEV: f holds deviations h = f - w (shifted storage) on input and output. Moments of the
 // weights are added to the zeroth and second moments (sum w = 1, sum w e_a e_b = d_ab / 3)
 // and subtracted again from the raw post-collision moments before the back transform
 // (sum w = 1, sum w e_a^2 = 1/3, sum w e_a^2 e_b^2 = 1/9; all other moments of w vanish),
 // so no per-population shift is needed.
-template <bool FORCE, bool DEV = false>
-__device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx, float Fy,
-                                        float Fz) {
-    Moments m = moments(f);
-    const float drho = m.rho;
+// HO: third- and fourth-order central moments do not relax fully to equilibrium; ho holds
+// their post-collision values (k210, k120, k201, k021, k102, k012, then k220 - r/9,
+// k202 - r/9, k022 - r/9), which the closure computes (the reference's s_q = s_pi = 1
+// gives zeros).
+template <class V, bool FORCE, bool DEV, bool HO = false>
+__device__ __forceinline__ void collide_v(V (&f)[19], const Coef& c, V Fx, V Fy, V Fz,
+                                          const V* ho = nullptr) {
+    const V z0 = f[0];
+    const V one = vsplat(1.0f, z0), third = vsplat(1.0f / 3.0f, z0);
+    const V half = vsplat(0.5f, z0), quarter = vsplat(0.25f, z0), two = vsplat(2.0f, z0);
+    const V m_two = vsplat(-2.0f, z0);
+    // zeroth, first and second raw moments
+    const V sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+    const V a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
+    const V e = f[15] + f[16], h = f[17] + f[18];
+    const V ab = a + b, cd = cc + d, eh = e + h;
+    const V drho = (((f[0] + ((sx + sy) + sz)) + ab) + cd) + eh;
+    const V mx = ((((f[1] - f[2]) + (f[7] - f[8])) + (f[9] - f[10])) + (f[11] - f[12])) + (f[13] - f[14]);
+    const V my = (((f[3] - f[4]) + (a - b)) + (f[15] - f[16])) + (f[17] - f[18]);
+    const V mz = ((f[5] - f[6]) + (cc - d)) + (e - h);
+    V pxx = (sx + ab) + cd, pyy = (sy + ab) + eh, pzz = (sz + cd) + eh;
+    const V pxy = (f[7] + f[10]) - (f[8] + f[9]);
+    const V pxz = (f[11] + f[14]) - (f[12] + f[13]);
+    const V pyz = (f[15] + f[18]) - (f[16] + f[17]);
+    V r = drho;
     if (DEV) {
-        m.rho += 1.0f;
-        m.pxx += 1.0f / 3.0f;
-        m.pyy += 1.0f / 3.0f;
-        m.pzz += 1.0f / 3.0f;
+        r = drho + one;
+        pxx = pxx + third;
+        pyy = pyy + third;
+        pzz = pzz + third;
     }
-    const float r = m.rho;
-    const float inv = __frcp_rn(r);
-    float u = m.mx * inv, v = m.my * inv, w = m.mz * inv;
+    const V inv = vrcp(r);
+    V u = mx * inv, v = my * inv, w = mz * inv;
     if (FORCE) {
-        u += 0.5f * Fx * inv;
-        v += 0.5f * Fy * inv;
-        w += 0.5f * Fz * inv;
+        u = vfma(half * Fx, inv, u);
+        v = vfma(half * Fy, inv, v);
+        w = vfma(half * Fz, inv, w);
     }
+    const V ur = u * r, vr = v * r, wr = w * r;
     // second-order central moments about the shifted velocity
-    const float k200 = m.pxx - 2.0f * u * m.mx + u * u * r;
-    const float k020 = m.pyy - 2.0f * v * m.my + v * v * r;
-    const float k002 = m.pzz - 2.0f * w * m.mz + w * w * r;
-    const float k110 = m.pxy - u * m.my - v * m.mx + u * v * r;
-    const float k101 = m.pxz - u * m.mz - w * m.mx + u * w * r;
-    const float k011 = m.pyz - v * m.mz - w * m.my + v * w * r;
+    const V k200 = vfma(u, vfma(m_two, mx, ur), pxx);
+    const V k020 = vfma(v, vfma(m_two, my, vr), pyy);
+    const V k002 = vfma(w, vfma(m_two, mz, wr), pzz);
+    const V k110 = pxy - vfma(u, my - vr, v * mx);
+    const V k101 = pxz - vfma(u, mz - wr, w * mx);
+    const V k011 = pyz - vfma(v, mz - wr, w * my);
     // relaxation (clbm_moving.py:170-196)
-    const float k110s = k110 * c.one_m_sv, k101s = k101 * c.one_m_sv, k011s = k011 * c.one_m_sv;
-    const float kA = k200 + k020 + k002;
-    const float kAs = kA - c.s_e * (kA - r);
-    const float kDs = (k200 - k020) * c.one_m_sv, kEs = (k200 - k002) * c.one_m_sv;
-    const float k200s = (kAs + kDs + kEs) * (1.0f / 3.0f);
-    const float k020s = (kAs - 2.0f * kDs + kEs) * (1.0f / 3.0f);
-    const float k002s = (kAs + kDs - 2.0f * kEs) * (1.0f / 3.0f);
+    const V osv = vsplat(c.one_m_sv, z0);
+    const V k110s = k110 * osv, k101s = k101 * osv, k011s = k011 * osv;
+    const V kA = (k200 + k020) + k002;
+    const V kAs = vfma(vsplat(-c.s_e, z0), kA - r, kA);
+    const V kDs = (k200 - k020) * osv, kEs = (k200 - k002) * osv;
+    const V k200s = ((kAs + kDs) + kEs) * third;
+    const V k020s = (vfma(m_two, kDs, kAs) + kEs) * third;
+    const V k002s = vfma(m_two, kEs, kAs + kDs) * third;
     // fourth-order equilibrium r/9; its weight part 1/9 is removed here in the shifted form
-    const float r9 = (DEV ? drho : r) * (1.0f / 9.0f);
+    const V r9 = (DEV ? drho : r) * vsplat(1.0f / 9.0f, z0);
     // raw post-collision moments (third-order central moments relax to 0, fourth to r/9)
-    const float ur = u * r, vr = v * r, wr = w * r;
-    const float uu = u * u, vv = v * v, ww = w * w;
-    const float T110 = k110s + u * vr, T101 = k101s + u * wr, T011 = k011s + v * wr;
-    float T200 = k200s + u * ur, T020 = k020s + v * vr, T002 = k002s + w * wr;
-    const float T210 = 2.0f * u * k110s + v * k200s + uu * vr;
-    const float T120 = 2.0f * v * k110s + u * k020s + vv * ur;
-    const float T201 = 2.0f * u * k101s + w * k200s + uu * wr;
-    const float T021 = 2.0f * v * k011s + w * k020s + vv * wr;
-    const float T102 = 2.0f * w * k101s + u * k002s + ww * ur;
-    const float T012 = 2.0f * w * k011s + v * k002s + ww * vr;
-    const float T220 = r9 + 4.0f * u * v * k110s + vv * k200s + uu * k020s + uu * vv * r;
-    const float T202 = r9 + 4.0f * u * w * k101s + ww * k200s + uu * k002s + uu * ww * r;
-    const float T022 = r9 + 4.0f * v * w * k011s + ww * k020s + vv * k002s + vv * ww * r;
+    const V uu = u * u, vv = v * v, ww = w * w;
+    const V u2 = two * u, v2 = two * v, w2 = two * w;
+    const V T110 = vfma(u, vr, k110s), T101 = vfma(u, wr, k101s), T011 = vfma(v, wr, k011s);
+    V T200 = vfma(u, ur, k200s), T020 = vfma(v, vr, k020s), T002 = vfma(w, wr, k002s);
+    const V T210 = vfma(u2, k110s, vfma(v, k200s, uu * vr));
+    const V T120 = vfma(v2, k110s, vfma(u, k020s, vv * ur));
+    const V T201 = vfma(u2, k101s, vfma(w, k200s, uu * wr));
+    const V T021 = vfma(v2, k011s, vfma(w, k020s, vv * wr));
+    const V T102 = vfma(w2, k101s, vfma(u, k002s, ww * ur));
+    const V T012 = vfma(w2, k011s, vfma(v, k002s, ww * vr));
+    V T220 = vfma(u2 * v2, k110s, vfma(vv, k200s, vfma(uu, k020s, vfma(uu, vv * r, r9))));
+    V T202 = vfma(u2 * w2, k101s, vfma(ww, k200s, vfma(uu, k002s, vfma(uu, ww * r, r9))));
+    V T022 = vfma(v2 * w2, k011s, vfma(ww, k020s, vfma(vv, k002s, vfma(vv, ww * r, r9))));
+    V T210x = T210, T120x = T120, T201x = T201, T021x = T021, T102x = T102, T012x = T012;
+    if (HO) {
+        // binomial terms of the non-zero third/fourth-order post-collision central moments
+        T210x = T210 + ho[0]; T120x = T120 + ho[1]; T201x = T201 + ho[2];
+        T021x = T021 + ho[3]; T102x = T102 + ho[4]; T012x = T012 + ho[5];
+        T220 = T220 + vfma(u2, ho[1], vfma(v2, ho[0], ho[6]));
+        T202 = T202 + vfma(u2, ho[4], vfma(w2, ho[2], ho[7]));
+        T022 = T022 + vfma(v2, ho[5], vfma(w2, ho[3], ho[8]));
+    }
     if (DEV) {
-        T200 -= 1.0f / 3.0f; T020 -= 1.0f / 3.0f; T002 -= 1.0f / 3.0f;
+        T200 = T200 - third;
+        T020 = T020 - third;
+        T002 = T002 - third;
     }
     // closed form of M_raw^-1 (config_moving.py:62-73)
-    f[0] = (DEV ? drho : r) - (T200 + T020 + T002) + (T220 + T202 + T022);
-    const float A1 = 0.5f * (T200 - T220 - T202), B1 = 0.5f * (ur - T120 - T102);
-    const float A2 = 0.5f * (T020 - T220 - T022), B2 = 0.5f * (vr - T210 - T012);
-    const float A3 = 0.5f * (T002 - T202 - T022), B3 = 0.5f * (wr - T201 - T021);
+    f[0] = ((DEV ? drho : r) - ((T200 + T020) + T002)) + ((T220 + T202) + T022);
+    const V A1 = half * ((T200 - T220) - T202), B1 = half * ((ur - T120x) - T102x);
+    const V A2 = half * ((T020 - T220) - T022), B2 = half * ((vr - T210x) - T012x);
+    const V A3 = half * ((T002 - T202) - T022), B3 = half * ((wr - T201x) - T021x);
     f[1] = A1 + B1; f[2] = A1 - B1;
     f[3] = A2 + B2; f[4] = A2 - B2;
     f[5] = A3 + B3; f[6] = A3 - B3;
     // plane diagonals: f = (T_aabb + e_a e_b T_ab + e_b T_aab + e_a T_abb) / 4
     {
-        const float s = 0.25f * T220, p = 0.25f * T110, a = 0.25f * T210, b = 0.25f * T120;
-        f[7] = s + p + a + b;   // (+1,+1)
-        f[8] = s - p + a - b;   // (-1,+1)
-        f[9] = s - p - a + b;   // (+1,-1)
-        f[10] = s + p - a - b;  // (-1,-1)
+        const V sp = quarter * (T220 + T110), sm = quarter * (T220 - T110);
+        const V pa = quarter * (T210x + T120x), ma = quarter * (T210x - T120x);
+        f[7] = sp + pa;    // (+1,+1)
+        f[8] = sm + ma;    // (-1,+1)
+        f[9] = sm - ma;    // (+1,-1)
+        f[10] = sp - pa;   // (-1,-1)
     }
     {
-        const float s = 0.25f * T202, p = 0.25f * T101, a = 0.25f * T201, b = 0.25f * T102;
-        f[11] = s + p + a + b;
-        f[12] = s - p + a - b;
-        f[13] = s - p - a + b;
-        f[14] = s + p - a - b;
+        const V sp = quarter * (T202 + T101), sm = quarter * (T202 - T101);
+        const V pa = quarter * (T201x + T102x), ma = quarter * (T201x - T102x);
+        f[11] = sp + pa;
+        f[12] = sm + ma;
+        f[13] = sm - ma;
+        f[14] = sp - pa;
     }
     {
-        const float s = 0.25f * T022, p = 0.25f * T011, a = 0.25f * T021, b = 0.25f * T012;
-        f[15] = s + p + a + b;
-        f[16] = s - p + a - b;
-        f[17] = s - p - a + b;
-        f[18] = s + p - a - b;
+        const V sp = quarter * (T022 + T011), sm = quarter * (T022 - T011);
+        const V pa = quarter * (T021x + T012x), ma = quarter * (T021x - T012x);
+        f[15] = sp + pa;
+        f[16] = sm + ma;
+        f[17] = sm - ma;
+        f[18] = sp - pa;
     }
     if (FORCE) {
         // Guo forcing: w_q (1 - s_v/2) [ (e - u)/cs2 + (e.u) e / cs2^2 ] . F
+        const V three = vsplat(3.0f, z0), nine = vsplat(9.0f, z0);
+        const V u3 = three * u, v3 = three * v, w3 = three * w;
+        const V u9 = nine * u, v9 = nine * v, w9 = nine * w;
+        // per population: 9 (e.u)(e.F) + 3 e.F - 3 u.F, with e_a in {-1, 0, 1}
+        const V zero = vsplat(0.0f, z0);
+        const V nuF3 = zero - vfma(u3, Fx, vfma(v3, Fy, w3 * Fz));
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            const float eu = ex(q) * u + ey(q) * v + ez(q) * w;
-            const float cx = (ex(q) - u) * 3.0f + eu * ex(q) * 9.0f;
-            const float cy = (ey(q) - v) * 3.0f + eu * ey(q) * 9.0f;
-            const float cz = (ez(q) - w) * 3.0f + eu * ez(q) * 9.0f;
-            f[q] += c.wc[q] * (cx * Fx + cy * Fy + cz * Fz);
+            V eu9 = zero, eF = zero;
+            if (ex(q) > 0) { eu9 = eu9 + u9; eF = eF + Fx; }
+            if (ex(q) < 0) { eu9 = eu9 - u9; eF = eF - Fx; }
+            if (ey(q) > 0) { eu9 = eu9 + v9; eF = eF + Fy; }
+            if (ey(q) < 0) { eu9 = eu9 - v9; eF = eF - Fy; }
+            if (ez(q) > 0) { eu9 = eu9 + w9; eF = eF + Fz; }
+            if (ez(q) < 0) { eu9 = eu9 - w9; eF = eF - Fz; }
+            const V term = vfma(eu9, eF, vfma(three, eF, nuF3));
+            f[q] = vfma(vsplat(c.wc[q], z0), term, f[q]);
         }
+    }
+}
+
+// Scalar entry point: one cell held as float[19] (F1 for float32 storage, V1 for the
+// shifted 16-bit forms).
+template <bool FORCE, bool DEV = false>
+__device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx, float Fy,
+                                        float Fz) {
+    using V = typename std::conditional<DEV, V1, F1>::type;
+    V t[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q].x = f[q];
+    collide_v<V, FORCE, DEV>(t, c, V{Fx}, V{Fy}, V{Fz});
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = t[q].x;
+}
+
+// One cell with third- and fourth-order post-collision central moments given (closure).
+template <bool DEV>
+__device__ __forceinline__ void collide_ho(float (&f)[19], const Coef& c, const float (&ho)[9]) {
+    using V = typename std::conditional<DEV, V1, F1>::type;
+    V t[19], h[9];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q].x = f[q];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) h[i].x = ho[i];
+    collide_v<V, false, DEV, true>(t, c, V{0.f}, V{0.f}, V{0.f}, h);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = t[q].x;
+}
+
+// Two cells at once with the packed arithmetic (same bits as two scalar calls).
+template <bool FORCE, bool DEV>
+__device__ __forceinline__ void collide2(float (&f0)[19], float (&f1)[19], const Coef& c,
+                                         float F0x, float F0y, float F0z, float F1x, float F1y,
+                                         float F1z) {
+    V2 t[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q] = vpack(f0[q], f1[q]);
+    collide_v<V2, FORCE, DEV>(t, c, vpack(F0x, F1x), vpack(F0y, F1y), vpack(F0z, F1z));
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const float2 p = vunpack(t[q]);
+        f0[q] = p.x;
+        f1[q] = p.y;
     }
 }
 

@@ -41,13 +41,36 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
     box_pass_body<S, PULL>(fin, fout, g, c, fa, blockIdx.x, gridDim.x);
 }
 
+// Collision of the two cells of a thread. Shifted 16-bit forms (DEV): packed (f32x2) when
+// both are computed, a zero force on the unforced lane when only one is forced (same
+// values as the unforced path). Float32: one scalar call per cell.
+template <bool DEV>
+__device__ __forceinline__ void collide_pair(float (&h0)[19], float (&h1)[19], const Coef& c,
+                                             bool use0, bool use1, bool frc0, bool frc1,
+                                             float F0x, float F0y, float F0z, float F1x,
+                                             float F1y, float F1z) {
+    if (DEV && use0 && use1) {
+        if (frc0 || frc1) collide2<true, DEV>(h0, h1, c, F0x, F0y, F0z, F1x, F1y, F1z);
+        else collide2<false, DEV>(h0, h1, c, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    if (use0) {
+        if (frc0) collide<true, DEV>(h0, c, F0x, F0y, F0z);
+        else collide<false, DEV>(h0, c, 0.f, 0.f, 0.f);
+    }
+    if (use1) {
+        if (frc1) collide<true, DEV>(h1, c, F1x, F1y, F1z);
+        else collide<false, DEV>(h1, c, 0.f, 0.f, 0.f);
+    }
+}
+
 // ------------------------------------------------------------------ 16-bit pair kernel
 // Shifted 16-bit storage moves half the bytes of float32, so the one-cell kernel becomes
 // issue-bound. This variant gives each thread two neighbouring cells (x0, x0 + 1), x0 even:
 // every population is one aligned 32-bit load/store of a half2 (or bf16x2); the x-shifted
 // pulls take the neighbour element from the adjacent lane with a warp shuffle (the lanes at
 // the two warp edges load that one element themselves); the collision works on the
-// deviations directly (collide<.., DEV = true>).
+// deviations directly (collide<.., DEV = true>), both cells at once in packed f32x2.
 template <int S> struct Pair;
 template <> struct Pair<CLBM_STORE_F16S> {
     using T = __half;
@@ -183,14 +206,7 @@ __global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair
             F1z = fa.fz ? fa.fz[row + x0 + 1] : 0.f;
         }
     }
-    if (use0) {
-        if (frc0) collide<true, true>(h0, c, F0x, F0y, F0z);
-        else collide<false, true>(h0, c, 0.f, 0.f, 0.f);
-    }
-    if (use1) {
-        if (frc1) collide<true, true>(h1, c, F1x, F1y, F1z);
-        else collide<false, true>(h1, c, 0.f, 0.f, 0.f);
-    }
+    collide_pair<true>(h0, h1, c, use0, use1, frc0, frc1, F0x, F0y, F0z, F1x, F1y, F1z);
     if (use0 && use1) {
 #pragma unroll
         for (int q = 0; q < 19; ++q) P::st2(fout + q * g.plane + row + x0, h0[q], h1[q]);
@@ -378,14 +394,7 @@ __global__ void __launch_bounds__(256) k_stream_collide_tma(const typename Stg<S
             F1z = fa.fz ? fa.fz[row + x0 + 1] : 0.f;
         }
     }
-    if (use0) {
-        if (frc0) collide<true, DEV>(h0, c, F0x, F0y, F0z);
-        else collide<false, DEV>(h0, c, 0.f, 0.f, 0.f);
-    }
-    if (use1) {
-        if (frc1) collide<true, DEV>(h1, c, F1x, F1y, F1z);
-        else collide<false, DEV>(h1, c, 0.f, 0.f, 0.f);
-    }
+    collide_pair<DEV>(h0, h1, c, use0, use1, frc0, frc1, F0x, F0y, F0z, F1x, F1y, F1z);
     T* o = fout + row + x0;
     if (use0 && use1) {
 #pragma unroll

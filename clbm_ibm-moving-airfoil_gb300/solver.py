@@ -193,6 +193,18 @@ class Solver:
         check(lib().clbm_device_bytes(self._h, ctypes.byref(b)))
         return b.value
 
+    VARIANTS = ("cell", "pair", "staged")
+
+    def kernel_variant(self):
+        """Full-grid kernel chosen at creation and the autotune time per launch of each
+        variant in microseconds (absent: not timed)."""
+        v = ctypes.c_int32()
+        ms = (ctypes.c_float * 3)()
+        check(lib().clbm_kernel_variant(self._h, ctypes.byref(v), ms))
+        return dict(variant=self.VARIANTS[v.value],
+                    us_per_launch={n: round(ms[i] * 1e3, 2) for i, n in enumerate(self.VARIANTS)
+                                   if ms[i] > 0})
+
 
 class IBM:
     """Direct-forcing immersed boundary bound to one Solver (DroneMovingIBM,
