@@ -10,7 +10,7 @@ Drop-in modules for the reference driver (``clbm_moving``, ``airfoil_moving`` an
 ``taichi`` import shim) live in ``compat/``; put that directory first on PYTHONPATH.
 """
 
-from . import analysis, config, driver
+from . import analysis, closure, config, driver
 from ._lib import CLBMError, DivergedError, EXPORTED, lib, lib_path
 from .build import build
 from .config import (SimConfig, fish_case, force_coefficients, full_case,
@@ -19,7 +19,7 @@ from .solver import IBM, Ensemble, PinnedBuffer, Simulation, Solver
 
 __all__ = [
     "CLBMError", "DivergedError", "EXPORTED", "Ensemble", "IBM", "PinnedBuffer", "SimConfig", "Simulation",
-    "Solver", "analysis", "build", "config", "driver", "fish_case", "force_coefficients", "full_case",
+    "Solver", "analysis", "build", "closure", "config", "driver", "fish_case", "force_coefficients", "full_case",
     "highre_airplane_case", "lib", "lib_path", "reference_airplane_case", "small_case",
     "wing_case",
 ]

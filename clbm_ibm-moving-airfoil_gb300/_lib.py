@@ -28,6 +28,10 @@ EXPORTED = (
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
     "clbm_ensemble_tuning", "clbm_ensemble_destroy",
+    "clbm_closure_layout", "clbm_closure_set", "clbm_trainer_create", "clbm_trainer_destroy",
+    "clbm_trainer_capture", "clbm_trainer_read_slot", "clbm_trainer_extract", "clbm_trainer_count",
+    "clbm_trainer_write_samples", "clbm_trainer_read_samples", "clbm_trainer_stats",
+    "clbm_trainer_loss", "clbm_trainer_grad", "clbm_trainer_fit", "clbm_tc_selftest",
 )
 
 
@@ -114,6 +118,22 @@ def lib():
             "clbm_ensemble_tuning": [vp, ctypes.POINTER(i32), ctypes.POINTER(i32),
                                      ctypes.POINTER(i64)],
             "clbm_ensemble_destroy": [vp],
+            "clbm_closure_layout": [P],
+            "clbm_closure_set": [vp, P],
+            "clbm_trainer_create": [i32, vp, i64, pvp],
+            "clbm_trainer_destroy": [vp],
+            "clbm_trainer_capture": [vp, i32],
+            "clbm_trainer_read_slot": [vp, i32, P],
+            "clbm_trainer_extract": [vp, P, i64],
+            "clbm_trainer_count": [vp, ctypes.POINTER(i64)],
+            "clbm_trainer_write_samples": [vp, i64, i64, P],
+            "clbm_trainer_read_samples": [vp, i64, i64, P],
+            "clbm_trainer_stats": [vp, i64, i64, P],
+            "clbm_trainer_loss": [vp, P, i64, i64, ctypes.c_float, ctypes.POINTER(d)],
+            "clbm_trainer_grad": [vp, P, i64, i64, ctypes.c_float, P, ctypes.POINTER(d)],
+            "clbm_trainer_fit": [vp, P, i64, i64, i32, i64, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_uint64, P],
+            "clbm_tc_selftest": [i32, P, P, P, i32, i32],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libclbm_gb300.so")
-SOURCES = ["lbm_kernels.cu", "ibm_kernels.cu", "ensemble.cu", "closure.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["lbm_kernels.cu", "ibm_kernels.cu", "ensemble.cu", "closure.cu", "capi.cu", "closure_api.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2"]
 

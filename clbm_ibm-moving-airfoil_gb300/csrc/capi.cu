@@ -1,45 +1,14 @@
 // capi.cu -- extern "C" entry points (include/clbm_gb300.h): object lifetimes, host-side
 // sequencing of the kernels on the solver's stream, CUDA-graph capture of the time loop,
 // transfers in the reference layout and error reporting.
-#include <cmath>
-#include <cstdarg>
-#include <cstdio>
-#include <cstring>
-#include <string>
-#include <vector>
-#include <algorithm>
-
-#include "clbm_internal.cuh"
+#include "capi_internal.cuh"
 
 using namespace clbm;
+using clbm::api::fail;
 
 namespace {
 
 thread_local std::string g_err;
-
-int fail(int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
-    va_end(ap);
-    g_err = buf;
-    return code;
-}
-
-#define CK(call)                                                                      \
-    do {                                                                              \
-        cudaError_t e_ = (call);                                                      \
-        if (e_ != cudaSuccess)                                                        \
-            return fail(CLBM_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
-    } while (0)
-
-#define CK_LAUNCH()                                                                   \
-    do {                                                                              \
-        cudaError_t e_ = cudaGetLastError();                                          \
-        if (e_ != cudaSuccess)                                                        \
-            return fail(CLBM_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e_)); \
-    } while (0)
 
 constexpr double kWd[19] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
@@ -51,52 +20,17 @@ constexpr int kKernelsPerIbmStep = 6;
 
 }  // namespace
 
+int clbm::api::fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 void clbm::set_last_error(const char* msg) { g_err = msg; }
-
-struct clbm_ibm;
-
-struct clbm_solver {
-    clbm_config cfg{};
-    Grid g{};
-    Coef c{};
-    void* f[2] = {nullptr, nullptr};
-    int cur = 0;
-    bool local = true;        // f[cur] holds a post-stream state (no pull on the next read)
-    bool macro_full = false;  // rho/ux/uy/uz hold the macro fields of the current state
-    float *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
-    float *dfx = nullptr, *dfy = nullptr, *dfz = nullptr;  // dense force, padded layout
-    float* stage = nullptr;
-    size_t stage_bytes = 0;
-    unsigned long long* stats = nullptr;
-    cudaStream_t st = nullptr;     // high priority: IBM chain, box pass, transfers
-    cudaStream_t st2 = nullptr;    // low priority: bulk stream-collide of IBM steps
-    cudaEvent_t ev_bulk = nullptr; // end of the bulk pass (joined into st)
-    cudaEvent_t ev_fork = nullptr; // fork point of a bulk pass without a fresh box event
-    long long version = 0;         // bumped whenever f[cur] changes
-    long long launches = 0;
-    int variant = kVariantStaged;  // full-grid stream-collide kernel (chosen at create)
-    float variant_ms[3] = {0.f, 0.f, 0.f};  // autotune time per launch of each variant (0: not timed)
-    unsigned int* status = nullptr;
-    // profiling of the fused kernel
-    bool prof = false;
-    std::vector<cudaEvent_t> ev;
-    std::vector<int> ev_tag;  // per event pair: 0 bulk / plain pass, 1 box pass
-    size_t ev_used = 0;
-    // cached two-step graph of the time loop
-    cudaGraphExec_t gexec = nullptr;
-    const clbm_ibm* g_ibm = nullptr;
-    clbm_motion g_m{};
-    int g_cur = -1;
-    std::vector<clbm_ibm*> ibms;  // IBMs bound to this solver (orphaned on destroy)
-};
-
-struct clbm_ibm {
-    clbm_solver* s = nullptr;
-    IbmArrays a{};
-    long long calls = 0;          // host mirror of the device call counter
-    cudaEvent_t ev_box = nullptr; // recorded on st after the marker kernel of compute_force
-    long long box_version = -1;   // solver state version that ev_box belongs to
-};
 
 namespace {
 
@@ -130,12 +64,21 @@ int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bo
         s->ev_tag.resize(s->ev_used / 2 + 1);
         s->ev_tag[s->ev_used / 2] = box ? 1 : 0;
     }
-    if (box)
+    if (box) {
         launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
                                   s->c, fa, box_cells, st);
-    else
+    } else if (s->closure && (fmode == kForceNone || fmode == kForceSkipBand)) {
+        ClosureArgs ca{};
+        ca.params = s->cl_params;
+        ca.img = s->cl_img;
+        ca.cells = (long long)cells(s);
+        ca.tiles = (ca.cells + 127) / 128;
+        launch_closure_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur],
+                                      s->g, s->c, fa, ca, s->cl_grid, st);
+    } else {
         launch_stream_collide(s->cfg.storage, !s->local, fmode, s->variant, s->f[s->cur],
                               s->f[1 - s->cur], s->g, s->c, fa, st);
+    }
     CK_LAUNCH();
     if (s->prof)
         if (int rc = record_event(s, st)) return rc;
@@ -321,15 +264,15 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
 int clbm_destroy(clbm_solver* s) {
     if (!s) return CLBM_OK;
     if (s->st) cudaStreamSynchronize(s->st);
+    if (s->st2) cudaStreamSynchronize(s->st2);
     free_graph(s);
     for (clbm_ibm* ibm : s->ibms) ibm->s = nullptr;
     s->ibms.clear();
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
     void* ptrs[] = {s->f[0], s->f[1], s->rho, s->ux, s->uy, s->uz, s->dfx, s->dfy, s->dfz,
-                    s->stage, s->stats, s->status};
+                    s->stage, s->stats, s->status, s->cl_params, s->cl_img};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    if (s->st2) cudaStreamSynchronize(s->st2);
     if (s->ev_bulk) cudaEventDestroy(s->ev_bulk);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->st2) cudaStreamDestroy(s->st2);
@@ -837,6 +780,29 @@ int clbm_device_bytes(const clbm_solver* s, int64_t* out) {
     if (s->dfx) b += 3 * pb;
     b += s->stage_bytes;
     *out = (int64_t)b;
+    return CLBM_OK;
+}
+
+int clbm_closure_set(clbm_solver* s, const float* params) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_closure_set: null solver");
+    CK(cudaStreamSynchronize(s->st));
+    CK(cudaStreamSynchronize(s->st2));
+    free_graph(s);  // the captured bulk-pass kernel changes
+    if (!params) {
+        s->closure = false;
+        return CLBM_OK;
+    }
+    for (int i = 0; i < closure::kParams; ++i)
+        if (!std::isfinite(params[i])) return fail(CLBM_ERR_ARG, "clbm_closure_set: parameter %d not finite", i);
+    if (!s->cl_params) CK(cudaMalloc(&s->cl_params, sizeof(float) * closure::kParams));
+    if (!s->cl_img) CK(cudaMalloc(&s->cl_img, sizeof(uint16_t) * closure::kImgElems));
+    CK(cudaMemcpyAsync(s->cl_params, params, sizeof(float) * closure::kParams, cudaMemcpyHostToDevice, s->st));
+    launch_closure_images(s->cl_params, s->cl_img, s->st);
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(s->st));
+    s->cl_grid = closure_grid(s->cfg.storage);
+    s->closure = true;
+    s->launches += 1;
     return CLBM_OK;
 }
 

@@ -78,7 +78,7 @@ constexpr int kTrainable = kSpan - kW1;        // W1 .. b3
 // BF16 images of W1, W2 and W2^T in the K-major core-matrix layout of the MMAs.
 constexpr int kImgElems = 3 * kHid * kHid;
 constexpr int kTargets = 9;                    // third- and fourth-order moments per sample
-constexpr int kSampleFloats = kIn + 2 * kTargets;
+constexpr int kSampleFloats = kIn + kTargets;  // floats per training sample
 }  // namespace closure
 
 // Band box of the IBM stencils: all six entries are reduced with atomicMin, maxima stored

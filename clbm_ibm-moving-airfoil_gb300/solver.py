@@ -193,6 +193,16 @@ class Solver:
         check(lib().clbm_device_bytes(self._h, ctypes.byref(b)))
         return b.value
 
+    def set_closure(self, params):
+        """Use the learned closure (a parameter array of closure.Layout, or a
+        closure.ClosureNet) for the bulk pass of later steps; None restores the plain
+        cascaded collision."""
+        if params is None:
+            check(lib().clbm_closure_set(self._h, None))
+            return
+        p = np.ascontiguousarray(getattr(params, "params", params), np.float32)
+        check(lib().clbm_closure_set(self._h, _ptr(p)))
+
     VARIANTS = ("cell", "pair", "staged")
 
     def kernel_variant(self):

@@ -202,6 +202,58 @@ int clbm_device_bytes(const clbm_solver* s, int64_t* out);
  * counterpart: the reference has one kernel per phase (clbm_moving.py:326-343). */
 int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_launch);
 
+/* ---- Learned sub-grid closure --------------------------------------------------------
+ * A 19 -> 32 -> 32 -> 1 network (GELU, BF16 weights, FP32 accumulation) maps the 19
+ * normalised non-equilibrium central moments of a cell to the relaxation rate s_h of its
+ * third- and fourth-order central moments, which the reference relaxes fully (s_q = s_pi
+ * = 1 in _collide, clbm_moving.py:186-194). Not part of the reference.
+ *
+ * Parameter array offsets (floats): out[0..14] = mu, sinv, W1, b1, W2, b2, W3, b3, span,
+ * total, inputs (19), hidden width (32), targets per sample (9), trainable count, floats
+ * per training sample (28). */
+int clbm_closure_layout(int32_t* out);
+
+/* Enable the closure for the bulk pass of later steps (params: host array of the layout
+ * above, copied), or disable it (params NULL: the plain cascaded collision, the
+ * fallback). Cells of the IBM force box and dense-force steps keep the plain collision. */
+int clbm_closure_set(clbm_solver* s, const float* params);
+
+/* Trainer: samples from box-filtered fields of a fine lattice (twice the coarse one in
+ * each direction, float32 storage) and Adam training on the device. Sample i holds 19
+ * features (moments of the filtered pre-collision state) and 9 targets (third- and
+ * fourth-order moments of the ideal post-collision state f*_q(x) = f_q(x + e_q) one
+ * coarse step later). fine may be NULL (samples written by the caller). */
+typedef struct clbm_trainer clbm_trainer;
+int clbm_trainer_create(int32_t device, const clbm_solver* fine, int64_t capacity, clbm_trainer** out);
+int clbm_trainer_destroy(clbm_trainer* t);
+/* Filter the fine lattice's current post-stream state into slot 0 or 1. */
+int clbm_trainer_capture(clbm_trainer* t, int32_t slot);
+/* A captured slot in the reference layout (nx/2, ny/2, nz/2, 19), z fastest. */
+int clbm_trainer_read_slot(clbm_trainer* t, int32_t slot, float* out);
+/* Append samples at coarse cells (x + nx (y + ny z), 1 <= x <= nx - 2) from slots 0 -> 1. */
+int clbm_trainer_extract(clbm_trainer* t, const int64_t* cells, int64_t n);
+int clbm_trainer_count(const clbm_trainer* t, int64_t* n);
+/* Samples as [n][28] host rows. */
+int clbm_trainer_write_samples(clbm_trainer* t, int64_t off, int64_t n, const float* in);
+int clbm_trainer_read_samples(clbm_trainer* t, int64_t off, int64_t n, float* out);
+/* Sums of the 19 features, of their squares and of the squared third/fourth-order
+ * features over a sample range (39 doubles). */
+int clbm_trainer_stats(clbm_trainer* t, int64_t off, int64_t n, double* out);
+/* Loss sum_j (t_j - (1 - s_h) p_j)^2 * wscale summed over a sample range. */
+int clbm_trainer_loss(clbm_trainer* t, const float* params, int64_t off, int64_t n, float wscale,
+                      double* loss_sum);
+/* Gradient of the mean loss over a sample range w.r.t. W1, b1, W2, b2, W3, b3 (in the
+ * order of the parameter array from W1 on). */
+int clbm_trainer_grad(clbm_trainer* t, const float* params, int64_t off, int64_t n, float wscale,
+                      float* grad, double* loss_sum);
+/* Adam with a cosine learning-rate decay over random minibatches of a sample range;
+ * params updated in place; loss_hist (iters doubles, may be NULL) gets minibatch sums. */
+int clbm_trainer_fit(clbm_trainer* t, float* params, int64_t off, int64_t n, int32_t iters, int64_t batch,
+                     float lr, float wscale, uint64_t seed, double* loss_hist);
+/* Tensor-core self test: D (128 x n) = A (128 x kdim) B^T (n x kdim), BF16 operands,
+ * kdim 32 or 128, n 32 or 112 (the operand layouts of the closure kernels). */
+int clbm_tc_selftest(int32_t device, const float* A, const float* B, float* D, int32_t kdim, int32_t n);
+
 /* Page-locked host buffers for fast transfers. */
 int clbm_host_alloc(int64_t bytes, void** out);
 int clbm_host_free(void* p);

@@ -12,6 +12,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "clbm_oracle.c")
+SRCS = [SRC, os.path.join(HERE, "closure_oracle.c")]
 
 FLAGS = ["-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
          "-fno-math-errno", "-Wall", "-Wno-unused-variable"]
@@ -27,9 +28,9 @@ def build(force=False):
     for real, ctype in (("f32", "float"), ("f64", "double")):
         out = lib_path(real)
         if (not force and os.path.exists(out)
-                and os.path.getmtime(out) >= os.path.getmtime(SRC)):
+                and os.path.getmtime(out) >= max(os.path.getmtime(f) for f in SRCS)):
             continue
-        cmd = ["gcc", *FLAGS, f"-DORACLE_REAL={ctype}", SRC, "-o", out + ".tmp", "-lm"]
+        cmd = ["gcc", *FLAGS, f"-DORACLE_REAL={ctype}", *SRCS, "-o", out + ".tmp", "-lm"]
         procs.append((subprocess.Popen(cmd), out))
     for p, out in procs:
         if p.wait() != 0:

@@ -65,9 +65,13 @@ static const int PQR[19][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1
                                {2, 1, 0}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2},
                                {0, 1, 2}, {2, 2, 0}, {2, 0, 2}, {0, 2, 2}};
 
+/* closure_oracle.c: post-collision higher-order moments of the learned closure */
+void oracle_closure_post(const float *params, const double *f, double *post9);
+
 typedef struct {
     int nx, ny, nz, n;
     double s_v, s_e, ux_in, uy_in;
+    float *closure;  /* learned-closure parameters (NULL: the reference's s_q = s_pi = 1) */
     REAL minv[19][19];
     REAL *f, *f_post, *rho, *ux, *uy, *uz, *fx, *fy, *fz;
     REAL *X0, *Y0, *Z0, *X, *Y, *Z, *VX, *VY, *Uk, *Vk, *FXk, *FYk;
@@ -203,8 +207,18 @@ static void or_collide(oracle_t *o) {
         REAL k200s = (kAs + kDs + kEs) / (REAL)3.0;
         REAL k020s = (kAs - (REAL)2.0 * kDs + kEs) / (REAL)3.0;
         REAL k002s = (kAs + kDs - (REAL)2.0 * kEs) / (REAL)3.0;
-        const REAL k210s = 0, k120s = 0, k201s = 0, k021s = 0, k102s = 0, k012s = 0;
+        REAL k210s = 0, k120s = 0, k201s = 0, k021s = 0, k102s = 0, k012s = 0;
         REAL k220s = r / (REAL)9.0, k202s = r / (REAL)9.0, k022s = r / (REAL)9.0;
+        if (o->closure) {
+            /* learned closure (not part of the reference): third/fourth-order central
+               moments relax with the network's rate s_h instead of 1 */
+            double fd[19], post[9];
+            for (int q = 0; q < 19; ++q) fd[q] = (double)fc[q];
+            oracle_closure_post(o->closure, fd, post);
+            k210s = (REAL)post[0]; k120s = (REAL)post[1]; k201s = (REAL)post[2];
+            k021s = (REAL)post[3]; k102s = (REAL)post[4]; k012s = (REAL)post[5];
+            k220s += (REAL)post[6]; k202s += (REAL)post[7]; k022s += (REAL)post[8];
+        }
         /* central -> raw, clbm_moving.py:198-231 */
         REAL T[19];
         T[0] = r;
@@ -463,9 +477,19 @@ void oracle_destroy(void *h) {
     if (!o) return;
     void *p[] = {o->f, o->f_post, o->rho, o->ux, o->uy, o->uz, o->fx, o->fy, o->fz,
                  o->X0, o->Y0, o->Z0, o->X, o->Y, o->Z, o->VX, o->VY, o->Uk, o->Vk,
-                 o->FXk, o->FYk};
+                 o->FXk, o->FYk, o->closure};
     for (size_t t = 0; t < sizeof(p) / sizeof(p[0]); ++t) free(p[t]);
     free(o);
+}
+
+/* Learned closure for later collisions (params: 2186 floats, copied; NULL: off). */
+void oracle_set_closure(void *h, const float *params) {
+    oracle_t *o = (oracle_t *)h;
+    free(o->closure);
+    o->closure = NULL;
+    if (!params) return;
+    o->closure = (float *)malloc(sizeof(float) * 2186);
+    memcpy(o->closure, params, sizeof(float) * 2186);
 }
 
 int oracle_real_size(void) { return (int)sizeof(REAL); }

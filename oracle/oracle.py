@@ -40,6 +40,12 @@ def load(real="f32"):
         lib.oracle_set_threads.argtypes = [i]
         lib.oracle_max_threads.restype = i
         lib.oracle_real_size.restype = i
+        lib.oracle_set_closure.argtypes = [vp, P]
+        lib.oracle_closure_nparams.restype = i
+        lib.oracle_closure_features.argtypes = [P, i, P]
+        lib.oracle_closure_samples.argtypes = [P, P, i, i, i, P, i, P]
+        lib.oracle_closure_forward.argtypes = [P, P, i, i, P]
+        lib.oracle_closure_loss_grad.argtypes = [P, P, i, d, i, P, P]
         _LIBS[real] = lib
     return _LIBS[real]
 
@@ -84,6 +90,14 @@ class Oracle:
 
     def compute_force(self, xc, yc, theta, vx, vy, omega):
         self.lib.oracle_compute_force(self.h, xc, yc, theta, vx, vy, omega)
+
+    def set_closure(self, params):
+        """Learned closure in later collisions (parameter array), None: off."""
+        if params is None:
+            self.lib.oracle_set_closure(self.h, None)
+        else:
+            self._closure = np.ascontiguousarray(params, np.float32)
+            self.lib.oracle_set_closure(self.h, _ptr(self._closure))
 
     def lbm_step(self):
         self.lib.oracle_lbm_step(self.h)
@@ -134,3 +148,44 @@ class Oracle:
         out = np.empty((19, 19), self.dtype)
         self.lib.oracle_minv(self.h, _ptr(out))
         return out
+
+
+# ---------------------------------------------------------------- learned closure
+def closure_features(f):
+    """Features (non-equilibrium central moments / rho, M_raw order) of populations
+    f [..., 19], computed directly as sums of f (e - u)^p (e - v)^q (e - w)^r."""
+    f = np.ascontiguousarray(np.asarray(f, np.float64).reshape(-1, 19))
+    x = np.empty((f.shape[0], 19), np.float64)
+    load("f64").oracle_closure_features(_ptr(f), int(f.shape[0]), _ptr(x))
+    return x
+
+
+def closure_samples(f0, f1, cells):
+    """Samples [n, 28] of coarse cells from filtered states in the reference layout."""
+    f0 = np.ascontiguousarray(f0, np.float64)
+    f1 = np.ascontiguousarray(f1, np.float64)
+    nx, ny, nz, _ = f0.shape
+    c = np.ascontiguousarray(cells, np.int64)
+    out = np.empty((c.size, 28), np.float64)
+    load("f64").oracle_closure_samples(_ptr(f0), _ptr(f1), nx, ny, nz, _ptr(c), int(c.size),
+                                       _ptr(out))
+    return out
+
+
+def closure_forward(params, x, round_bf16=True):
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float64)
+    s = np.empty(x.shape[0], np.float64)
+    load("f64").oracle_closure_forward(_ptr(p), _ptr(x), int(x.shape[0]), int(round_bf16), _ptr(s))
+    return s
+
+
+def closure_loss_grad(params, samples, wscale, round_bf16=True, grad=True):
+    """Loss sum over the samples and the gradient of the mean loss (trainable block)."""
+    p = np.ascontiguousarray(params, np.float32)
+    sm = np.ascontiguousarray(samples, np.float64)
+    loss = np.zeros(1, np.float64)
+    g = np.zeros(2145, np.float64) if grad else None
+    load("f64").oracle_closure_loss_grad(_ptr(p), _ptr(sm), int(sm.shape[0]), float(wscale),
+                                         int(round_bf16), _ptr(loss), _ptr(g) if grad else None)
+    return (loss[0], g) if grad else loss[0]

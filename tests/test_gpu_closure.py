@@ -1,0 +1,190 @@
+"""Learned closure on the GPU: the tensor-core operand layouts, the training kernels
+against the CPU oracle (loss, back-propagated gradients), training gain over the plain
+method, the fused closure collision against the oracle solver, and the sample pipeline
+(box filter of a fine lattice, sample extraction) against NumPy and the oracle."""
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from test_closure_oracle import W, feq, random_params, random_samples
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(a):
+    a = np.ascontiguousarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("kdim,n", [(32, 32), (128, 112)])
+def test_tensor_core_layout(built_pkg, kdim, n):
+    rng = np.random.default_rng(kdim + n)
+    A = rng.standard_normal((128, kdim)).astype(np.float32)
+    B = rng.standard_normal((n, kdim)).astype(np.float32)
+    D = built_pkg.closure.tc_selftest(A, B)
+    want = bf16(A).astype(np.float64) @ bf16(B).astype(np.float64).T
+    np.testing.assert_allclose(D, want, rtol=1e-5, atol=1e-4)
+
+
+def _trainer_with(pkg, samples):
+    tr = pkg.closure.Trainer(capacity=len(samples))
+    tr.write_samples(0, samples)
+    return tr
+
+
+def test_loss_and_gradient_match_oracle(built_pkg, oracle_mod):
+    rng = np.random.default_rng(21)
+    p = random_params(rng)
+    sm = random_samples(rng, 1000)
+    wscale = 1.0 / np.mean(np.sum(sm[:, 10:19] ** 2, axis=1))
+    tr = _trainer_with(built_pkg, sm)
+    back = tr.read_samples(0, len(sm))
+    np.testing.assert_array_equal(back, sm.astype(np.float32))
+    net = built_pkg.closure.ClosureNet(p)
+    loss = tr.loss(net, 0, len(sm), wscale)
+    ref_loss = oracle_mod.closure_loss_grad(p, back.astype(np.float64), wscale, grad=False) / len(sm)
+    assert loss == pytest.approx(ref_loss, rel=2e-3)
+    g, loss_g = tr.grad(net, 0, len(sm), wscale)
+    assert loss_g == pytest.approx(loss, rel=1e-6)
+    _, ref_g = oracle_mod.closure_loss_grad(p, back.astype(np.float64), wscale)
+    # blocks of the gradient: W1 (inputs < 19), b1, W2, b2, W3, b3
+    w1 = g[:1024].reshape(32, 32)[:, :19]
+    rw1 = ref_g[:1024].reshape(32, 32)[:, :19]
+    assert rel_l2(w1, rw1) < 3e-2
+    for lo, hi in ((1024, 1056), (1056, 2080), (2080, 2112), (2112, 2144), (2144, 2145)):
+        assert rel_l2(g[lo:hi], ref_g[lo:hi]) < 3e-2, (lo, hi, rel_l2(g[lo:hi], ref_g[lo:hi]))
+    np.testing.assert_array_equal(g[:1024].reshape(32, 32)[:, 19:], 0.0)
+    tr.close()
+
+
+def test_training_beats_the_plain_rate(built_pkg):
+    """Synthetic samples whose ideal rate depends on a shear moment: the trained network
+    lowers the held-out loss well below the plain method's (s_h = 1)."""
+    rng = np.random.default_rng(22)
+    sm = random_samples(rng, 24000)
+    train, held = sm[:20000], sm[20000:]
+    tr = _trainer_with(built_pkg, sm)
+    mean, std, p2 = tr.stats(0, len(train))
+    np.testing.assert_allclose(mean, train[:, :19].mean(axis=0), rtol=1e-4, atol=1e-12)
+    wscale = 1.0 / p2
+    net0 = built_pkg.closure.ClosureNet.initial(mean, std, span=0.8, seed=1)
+    plain = tr.loss(net0, 20000, 4000, wscale)
+    net, hist = tr.fit(net0, 0, 20000, iters=600, batch=2048, lr=3e-3, wscale=wscale, seed=3)
+    trained = tr.loss(net, 20000, 4000, wscale)
+    assert np.all(np.isfinite(hist)) and hist[-50:].mean() < hist[:50].mean()
+    assert trained < 0.5 * plain, (trained, plain)
+    tr.close()
+
+
+def _perturbed(shape, rng, u=0.04):
+    f = np.broadcast_to(feq(1.0, np.array([u, 0.0, 0.0])), shape + (19,)).copy()
+    f *= 1 + 2e-3 * rng.standard_normal(f.shape)
+    return f.astype(np.float32)
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 2e-3), ("f16", 5e-3)])
+def test_closure_solver_matches_oracle(built_pkg, oracle_mod, storage, tol):
+    rng = np.random.default_rng(31)
+    shape = (40, 12, 6)
+    p = random_params(rng, span=0.9)
+    f0 = _perturbed(shape, rng)
+    s = built_pkg.Solver(*shape, 1.7, 1.0, 0.04, 0.0, storage=storage)
+    s.write_populations(f0)
+    s.set_closure(p)
+    o = oracle_mod.Oracle(*shape, 1.7, 1.0, 0.04, 0.0, [], [], [], real="f64")
+    o.set_f(f0.astype(np.float64))
+    o.set_closure(p)
+    plain = oracle_mod.Oracle(*shape, 1.7, 1.0, 0.04, 0.0, [], [], [], real="f64")
+    plain.set_f(f0.astype(np.float64))
+    for _ in range(4):
+        s.step()
+        o.lbm_step()
+        plain.lbm_step()
+    got = s.read_populations().astype(np.float64) - W
+    want = o.f() - W
+    err = rel_l2(got, want)
+    effect = rel_l2(plain.f() - W, want)
+    # the comparison error is that of the BF16 network (s_h to about 2^-8); the closure's
+    # effect on the populations is resolved well beyond it
+    assert err < tol, (err, effect)
+    assert effect > (50 if storage == "f32" else 5) * err, (err, effect)
+    s.close()
+    o.close()
+    plain.close()
+
+
+def test_closure_plain_limit_equals_plain_kernel(built_pkg):
+    rng = np.random.default_rng(32)
+    shape = (64, 16, 8)
+    p = random_params(rng)
+    p[2152:2185] = 0.0     # W3 = b3 = 0: s_h = 1
+    f0 = _perturbed(shape, rng)
+    out = []
+    for closure in (None, p):
+        s = built_pkg.Solver(*shape, 1.7, 1.0, 0.04, 0.0)
+        s.write_populations(f0)
+        s.set_closure(closure)
+        for _ in range(3):
+            s.step()
+        out.append(s.read_populations())
+        s.close()
+    assert rel_l2(out[1] - W, out[0] - W) < 1e-5
+
+
+def test_closure_with_ibm_graph_and_direct(built_pkg):
+    """IBM steps with the closure on the bulk pass: graph replay (motion on the device)
+    agrees with direct launches (motion on the host), the run stays finite and close to
+    the plain run."""
+    rng = np.random.default_rng(33)
+    p = random_params(rng, span=0.3)
+    cfg = built_pkg.small_case()
+    runs = {}
+    for mode in ("graph", "direct", "plain"):
+        sim = built_pkg.Simulation(cfg)
+        if mode != "plain":
+            sim.solver.set_closure(p)
+        sim.run(20, graph=(mode == "graph"))
+        runs[mode] = (sim.solver.read_populations(), sim.ibm.force_history(20))
+        assert sim.solver.check()["nonfinite"] == 0
+        sim.close()
+    assert rel_l2(runs["graph"][0] - W, runs["direct"][0] - W) < 1e-5
+    assert rel_l2(runs["graph"][1], runs["direct"][1]) < 1e-4
+    assert rel_l2(runs["graph"][0] - W, runs["plain"][0] - W) < 0.05
+
+
+def test_filter_and_samples(built_pkg, oracle_mod):
+    """Box filter of a fine lattice against NumPy on the exported post-stream state, and
+    the extracted samples against the oracle's restatement."""
+    rng = np.random.default_rng(34)
+    fine_shape = (24, 12, 8)
+    fine = built_pkg.Solver(*fine_shape, 1.6, 1.0, 0.04, 0.0)
+    fine.write_populations(_perturbed(fine_shape, rng))
+    fine.step()
+    fine.step()
+    tr = built_pkg.closure.Trainer(capacity=2000, fine=fine)
+    tr.capture(0)
+    f_fine = fine.read_populations().astype(np.float64)
+    nx, ny, nz = (n // 2 for n in fine_shape)
+    want = f_fine.reshape(nx, 2, ny, 2, nz, 2, 19).mean(axis=(1, 3, 5))
+    got0 = tr.read_slot(0).astype(np.float64)
+    np.testing.assert_allclose(got0, want, rtol=1e-6, atol=1e-8)
+    fine.step()
+    fine.step()
+    tr.capture(1)
+    got1 = tr.read_slot(1).astype(np.float64)
+    cells = built_pkg.closure.sample_cells((nx, ny, nz), (4, 6, 2, 3), 300, rng)
+    tr.extract(cells)
+    assert tr.count == len(cells)
+    sm = tr.read_samples(0, len(cells)).astype(np.float64)
+    ref = oracle_mod.closure_samples(got0, got1, cells)
+    # first-order central moments about the cell's own velocity vanish up to rounding
+    # (float32 on the device, double in the oracle): compare on a common scale floor
+    scale = np.maximum(np.abs(ref).max(axis=0), 1e-3 * np.abs(ref[:, 4:]).max())
+    assert np.max(np.abs(sm - ref) / scale) < 2e-3
+    with pytest.raises(built_pkg.CLBMError):
+        tr.extract(np.array([0], np.int64))       # x = 0 is not a valid sample cell
+    tr.close()
+    fine.close()
