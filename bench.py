@@ -39,7 +39,21 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=200)
+    p.add_argument("--closure", default=None,
+                   help="learned closure on the bulk pass: a parameter file (.npy) or "
+                        "'random' (a fixed random network, for timing)")
     return p.parse_args()
+
+
+def closure_params(pkg, spec):
+    """Closure parameters for --closure: a saved array or a fixed random network."""
+    import numpy as np
+    if spec == "random":
+        rng = np.random.default_rng(0)
+        net = pkg.closure.ClosureNet.initial(np.zeros(19), np.full(19, 1e-4), span=0.5, seed=0)
+        net.view("W3")[:] = rng.standard_normal(32) * 0.1
+        return net
+    return pkg.closure.ClosureNet.load(spec)
 
 
 def dist_env():
@@ -218,6 +232,8 @@ def run_gpu(args, rank, world, local):
     cfg = pkg.full_case(storage=args.storage)
     sim = pkg.Simulation(cfg, device=local)
     solver, ibm = sim.solver, sim.ibm
+    if args.closure:
+        solver.set_closure(closure_params(pkg, args.closure))
     stream = torch.cuda.ExternalStream(solver.stream_handle(), device=torch.device("cuda", local))
 
     # ---- device-timed region: inputs resident in HBM, direct launches, fused kernel timed
@@ -297,13 +313,15 @@ def run_gpu(args, rank, world, local):
                 "l2": "inputs larger than L2: 2 x %.0f MB population buffers" %
                       (cfg.cells * 19 * (4 if args.storage == "f32" else 2) / 1e6),
                 "timed_region": "direct launches, per-step IBM + fused stream-collide",
+                "closure": args.closure or "off",
             },
             "graph_value": cfg.cells * args.steps * world / (graph_ms / 1e3) / 1e6,
             "gpu_launches": gpu_launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "bulk stream-collide pass (cells outside the force box), "
-                                   f"{variant['variant']} variant",
+                                   + ("fused learned closure (tcgen05)" if args.closure
+                                      else f"{variant['variant']} variant"),
                          "variant_autotune_us": variant["us_per_launch"],
                          "ms_per_launch": bulk_ms, "launches": prof["bulk_launches"],
                          "algorithmic_bytes_per_launch": alg_bytes,

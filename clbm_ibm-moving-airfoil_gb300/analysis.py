@@ -20,13 +20,15 @@ def force_statistics(coeffs, start=0):
 
 def wake_vorticity_spectrum(wz, chord, x_start, x_stop=None):
     """Power spectrum of wz (Nx, Ny) along x over [x_start, x_stop), mean over y.
-    Returns (k, power) with k in cycles per chord."""
+    Returns (k, power) with k in cycles per chord. The power of a bin is the squared
+    amplitude it holds (|FFT|^2 / n^2 with a Hann window), so the same physical segment
+    sampled at different resolutions gives the same values on the same wavenumber bins."""
     seg = np.asarray(wz, np.float64)[int(x_start):(None if x_stop is None else int(x_stop))]
     seg = seg - seg.mean(axis=0, keepdims=True)
     n = seg.shape[0]
     win = np.hanning(n)[:, None]
     spec = np.abs(np.fft.rfft(seg * win, axis=0)) ** 2
-    power = spec.mean(axis=1) / max(n, 1)
+    power = spec.mean(axis=1) / max(n, 1) ** 2
     k = np.fft.rfftfreq(n, d=1.0) * chord
     return k, power
 

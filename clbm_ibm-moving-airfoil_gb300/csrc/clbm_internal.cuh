@@ -58,9 +58,15 @@ struct Coef {
 };
 
 // Learned sub-grid closure: a 19 -> 32 -> 32 -> 1 network (GELU, BF16 weights, FP32
-// accumulation) maps the 19 normalised non-equilibrium central moments of a cell to the
-// relaxation rate s_h of its third- and fourth-order central moments (the reference fixes
-// s_q = s_pi = 1, clbm_moving.py:186-194). Parameters are one float32 array:
+// accumulation) maps the 19 normalised non-equilibrium central moments of a cell to one
+// relaxation rate of its collision. Two forms (parameter `mode`):
+//   0  higher-order rate: third- and fourth-order central moments relax with
+//      s_h = 1 + span tanh(z3) (the reference fixes s_q = s_pi = 1, clbm_moving.py:186-194);
+//   1  eddy viscosity: the deviatoric second-order moments relax with
+//      s_eff = 1 / (1/2 + 3 nu 2^(span g)), g = tanh(z3) where positive and tanh(z3) / 20
+//      below, nu the lattice viscosity: the network adds viscosity and may remove at most
+//      a factor 2^(-span/20); s_v where it outputs zero.
+// Parameters are one float32 array:
 namespace closure {
 constexpr int kIn = 19;                        // input features (moment order of M_raw)
 constexpr int kHid = 32;                       // hidden width; inputs are padded to 32
@@ -72,13 +78,21 @@ constexpr int kW2 = kB1 + kHid;                // [32 out][32 in]
 constexpr int kB2 = kW2 + kHid * kHid;         // [32]
 constexpr int kW3 = kB2 + kHid;                // [32]
 constexpr int kB3 = kW3 + kHid;                // [1]
-constexpr int kSpan = kB3 + 1;                 // [1] s_h = 1 + span * tanh(z3)
-constexpr int kParams = kSpan + 1;
+constexpr int kSpan = kB3 + 1;                 // [1] output range
+constexpr int kMode = kSpan + 1;               // [1] 0 higher-order rate, 1 eddy viscosity
+constexpr int kNu = kMode + 1;                 // [1] lattice viscosity the training assumes
+constexpr int kParams = kNu + 1;
 constexpr int kTrainable = kSpan - kW1;        // W1 .. b3
 // BF16 images of W1, W2 and W2^T in the K-major core-matrix layout of the MMAs.
 constexpr int kImgElems = 3 * kHid * kHid;
 constexpr int kTargets = 9;                    // third- and fourth-order moments per sample
-constexpr int kSampleFloats = kIn + kTargets;  // floats per training sample
+// Sub-grid stress targets of the eddy-viscosity form: the deviatoric parts (xy, xz, yz,
+// xx - yy, xx - zz) of tau = <u u> - <u><u> (box filter of the fine velocity) and of the
+// strain rate of the filtered velocity.
+constexpr int kSgs = 10;
+constexpr int kAux = 9;                        // filtered <u> (3) and <u u> (6) per coarse cell
+constexpr int kSampleFloats = kIn + kTargets + kSgs;  // floats per training sample
+constexpr int kStats = 2 * kIn + 2;            // feature sums, squares, two loss scales
 }  // namespace closure
 
 // Band box of the IBM stencils: all six entries are reduced with atomicMin, maxima stored

@@ -3,10 +3,14 @@
 // and the training kernels (forward, backward and weight gradients on the tensor cores,
 // deterministic reductions, Adam).
 //
-// The network maps the 19 normalised non-equilibrium central moments of a cell to the
-// rate s_h of its third- and fourth-order central moments, which the reference relaxes
-// fully (s_q = s_pi = 1, clbm_moving.py:186-194):
-//   k3* = (1 - s_h) k3,  k4* = r/9 + (1 - s_h)(k4 - r/9),  s_h = 1 + span tanh(z3).
+// The network maps the 19 normalised non-equilibrium central moments of a cell to one
+// relaxation rate (th = tanh(z3)):
+//   mode 0, higher-order rate (the reference fixes s_q = s_pi = 1, clbm_moving.py:186-194):
+//     k3* = (1 - s_h) k3,  k4* = r/9 + (1 - s_h)(k4 - r/9),  s_h = 1 + span th;
+//   mode 1, eddy viscosity: the deviatoric second-order moments relax with
+//     s_eff = 1 / (1/2 + 3 nu 2^(span g)), g = th (th >= 0) or th / 20 (th < 0), instead of
+//     s_v (nu the solver's viscosity): the network adds an eddy viscosity nu_t, trained
+//     against the sub-grid stress of the box-filtered fine velocity, tau = -2 nu_t S.
 // Dense layers run as tcgen05 MMAs (BF16 operands from shared memory, FP32 accumulators in
 // tensor memory, M = 128 rows = one cell or sample per thread of a 128-thread block).
 #include <algorithm>
@@ -58,9 +62,10 @@ __device__ __forceinline__ void tc_sync() {
 // takes tiles of 128 consecutive cells (x fastest across row ends). Per tile: gather,
 // moments and features (row of the A tile), layer 1 MMA, GELU, layer 2 MMA, GELU, output
 // layer on the CUDA cores, collision with s_h, store. Cells of the IBM force box (SkipBand)
-// are left to the box pass, which uses the plain collision with forcing.
+// are left to the box pass, which uses the plain collision with forcing; the inlet and
+// outlet columns (x = 0, nx - 1) keep the plain rates.
 template <int S, bool PULL, int FMODE>
-__global__ void __launch_bounds__(128) k_closure_stream_collide(const typename Pop<S>::T* __restrict__ fin,
+__global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typename Pop<S>::T* __restrict__ fin,
                                                                 typename Pop<S>::T* __restrict__ fout,
                                                                 Grid g, Coef c, ForceArgs fa,
                                                                 ClosureArgs ca) {
@@ -79,6 +84,7 @@ __global__ void __launch_bounds__(128) k_closure_stream_collide(const typename P
     tc_sync();
     const uint32_t tm = tbase;
     const uint32_t aA = tc::smem_addr(sA), aW1 = tc::smem_addr(sW), aW2 = aW1 + 2048;
+    const float nu = (1.0f / (1.0f - c.one_m_sv) - 0.5f) * (1.0f / 3.0f);  // solver viscosity
     uint32_t phase = 0;
     bool ok = true;
     const Band band = (FMODE == kForceSkipBand) ? band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz)
@@ -95,10 +101,10 @@ __global__ void __launch_bounds__(128) k_closure_stream_collide(const typename P
             if (FMODE == kForceSkipBand && in_band(band, x, y, z, g.ny, g.nz)) use = false;
         }
         float f[19];
-        CMom m;
         float v[32];
         if (use) {
             gather<S, PULL, true>(fin, g, c, x, y, z, f);
+            CMom m;
             moments_full<DEV>(f, m);
             standardise(m, net, v);
         } else {
@@ -107,30 +113,59 @@ __global__ void __launch_bounds__(128) k_closure_stream_collide(const typename P
         }
         put_row32(sA, tid, v);
         tc_sync();
-        if (tid == 0) mma_k32(tm, aA, aW1, &bar);
-        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, g.spin_limit));
+        // one thread issues the MMAs and waits for them; the barrier releases the block
+        bool w = true;
+        if (tid == 0) {
+            mma_k32(tm, aA, aW1, &bar);
+            w = tc::bar_wait(&bar, phase, g.spin_limit);
+        }
+        ok = !__syncthreads_or(!w);
         phase ^= 1;
         if (!ok) break;
         tc::fence_after();
         tc::ld32(tc::lane_addr(tm, warp, 0), v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] = gelu(v[j] + net.b1[j]);
+        for (int j = 0; j < 16; ++j) {
+            const float2 b = reinterpret_cast<const float2*>(net.b1)[j];
+            const float2 h = vunpack(gelu2(vpack(v[2 * j], v[2 * j + 1]) + vpack(b.x, b.y)));
+            v[2 * j] = h.x;
+            v[2 * j + 1] = h.y;
+        }
         put_row32(sA, tid, v);
         tc_sync();
-        if (tid == 0) mma_k32(tm, aA, aW2, &bar);
-        ok = !__syncthreads_or(!tc::bar_wait(&bar, phase, g.spin_limit));
+        if (tid == 0) {
+            mma_k32(tm, aA, aW2, &bar);
+            w = tc::bar_wait(&bar, phase, g.spin_limit);
+        }
+        ok = !__syncthreads_or(!w);
         phase ^= 1;
         if (!ok) break;
         tc::fence_after();
         tc::ld32(tc::lane_addr(tm, warp, 0), v);
-        float z3 = net.b3;
+        V2 acc = vsplat(0.0f, V2{});
 #pragma unroll
-        for (int j = 0; j < 32; ++j) z3 += net.w3[j] * gelu(v[j] + net.b2[j]);
-        const float sh = 1.0f + net.span * tanh_approx(z3);
+        for (int j = 0; j < 16; ++j) {
+            const float2 b = reinterpret_cast<const float2*>(net.b2)[j];
+            const float2 w3 = reinterpret_cast<const float2*>(net.w3)[j];
+            acc = vfma(vpack(w3.x, w3.y), gelu2(vpack(v[2 * j], v[2 * j + 1]) + vpack(b.x, b.y)), acc);
+        }
+        const float2 accs = vunpack(acc);
+        const float z3 = net.b3 + (accs.x + accs.y);
+        // inlet and outlet columns keep the plain rates (no training samples there)
+        const bool edge = x == 0 || x == g.nx - 1;
         if (use) {
-            float ho[9];
-            higher_order_post(m, sh, ho);
-            collide_ho<DEV>(f, c, ho);
+            const float th = tanh_approx(z3);
+            if (net.mode == 1) {
+                const float se = edge ? 1.0f - c.one_m_sv : eddy_rate(nu, net.span, th);
+                collide_sv<DEV>(f, c, 1.0f - se);
+            } else {
+                const float sh = edge ? 1.0f : 1.0f + net.span * th;
+                CMom m;  // recomputed rather than kept live across the network
+                moments_full<DEV>(f, m);
+                float ho[9];
+                higher_order_post(m, sh, ho);
+                collide_ho<DEV>(f, c, ho);
+            }
             store_raw<S>(fout, g, ((long long)z * g.ny + y) * g.pitch + x, f);
         }
     }
@@ -161,15 +196,20 @@ static void closure_sc(int fmode, const void* fin, void* fout, const Grid& g, co
         k_closure_stream_collide<S, PULL, kForceNone><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
 }
 
+// Persistent grid: the blocks that fit on an SM by registers (65,536 per SM) and by
+// tensor memory (32 of 512 columns per block), times the SM count.
 int closure_grid(int storage) {
-    int dev = 0, sms = 0, per = 0;
+    int dev = 0, sms = 0, regs = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncAttributes fa{};
     CLBM_CL_STORE(storage, {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_closure_stream_collide<S_, true, kForceSkipBand>, 128, 0);
+        if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand>) == cudaSuccess)
+            regs = fa.numRegs;
     });
-    // tensor memory: 32 columns per block, 512 per SM
-    per = std::min(std::max(per, 1), 16);
+    cudaGetLastError();
+    const int per_regs = regs > 0 ? 65536 / (128 * ((regs + 7) / 8 * 8)) : 4;
+    const int per = std::min(std::max(per_regs, 1), 16);
     return std::max(sms, 1) * per;
 }
 
@@ -185,25 +225,42 @@ void launch_closure_stream_collide(int storage, bool pull, int fmode, const void
 // ------------------------------------------------------------------ training samples
 // Box filter of a fine lattice twice as fine in each direction: coarse cell (I, J, K) gets
 // the mean of the post-stream (pre-collision) populations of fine cells (2I + a, 2J + b,
-// 2K + c), a, b, c in {0, 1}. Float32 fine storage.
+// 2K + c), a, b, c in {0, 1} (planes 0-18 of `out`), and the means of the fine velocity
+// u = m / rho and of its products u_i u_j (planes 19-21: ux, uy, uz; 22-27: xx, yy, zz,
+// xy, xz, yz). Float32 fine storage.
 template <bool PULL>
 __global__ void __launch_bounds__(128) k_filter2(const float* __restrict__ ff, Grid gf, Coef cf,
                                                  float* __restrict__ out, Grid gc) {
     const int X = blockIdx.x * 128 + threadIdx.x, Y = blockIdx.y, Z = blockIdx.z;
     if (X >= gc.nx) return;
-    float acc[19];
+    float acc[19], aux[kAux];
 #pragma unroll
     for (int q = 0; q < 19; ++q) acc[q] = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kAux; ++i) aux[i] = 0.0f;
     for (int s = 0; s < 8; ++s) {
         float v[19];
         gather<CLBM_STORE_F32, PULL, false>(ff, gf, cf, 2 * X + (s & 1), 2 * Y + ((s >> 1) & 1),
                                             2 * Z + (s >> 2), v);
+        float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
 #pragma unroll
-        for (int q = 0; q < 19; ++q) acc[q] += v[q];
+        for (int q = 0; q < 19; ++q) {
+            acc[q] += v[q];
+            r += v[q];
+            mx += (float)ex(q) * v[q];
+            my += (float)ey(q) * v[q];
+            mz += (float)ez(q) * v[q];
+        }
+        const float u = mx / r, w = mz / r, vv = my / r;
+        aux[0] += u; aux[1] += vv; aux[2] += w;
+        aux[3] += u * u; aux[4] += vv * vv; aux[5] += w * w;
+        aux[6] += u * vv; aux[7] += u * w; aux[8] += vv * w;
     }
     const long long cell = ((long long)Z * gc.ny + Y) * gc.pitch + X;
 #pragma unroll
     for (int q = 0; q < 19; ++q) out[q * gc.plane + cell] = 0.125f * acc[q];
+#pragma unroll
+    for (int i = 0; i < kAux; ++i) out[(19 + i) * gc.plane + cell] = 0.125f * aux[i];
 }
 
 void launch_filter2(bool pull, const float* ff, const Grid& gf, const Coef& cf, float* out,
@@ -213,11 +270,15 @@ void launch_filter2(bool pull, const float* ff, const Grid& gf, const Coef& cf, 
     else k_filter2<false><<<grid, 128, 0, st>>>(ff, gf, cf, out, gc);
 }
 
-// Sample j: coarse cell cells[j] (x + nx (y + ny z), 1 <= x <= nx - 2). Features from the
-// filtered pre-collision state f0; targets from the ideal post-collision state
-// f*_q(x) = f1_q(x + e_q) (f1 one coarse step later), as central moments about the
-// velocity of f0, divided by its density: samples[i * stride + offset + j], i < 19
-// features, 19 <= i < 28 targets (third order, then fourth order minus rho*/9).
+// Sample j: coarse cell cells[j] (x + nx (y + ny z), 2 <= x <= nx - 3). Features from the
+// filtered pre-collision state f0; higher-order targets from the ideal post-collision
+// state f*_q(x) = f1_q(x + e_q) (f1 one coarse step later), as central moments about the
+// velocity of f0, divided by its density; sub-grid stress targets from the filtered
+// velocity fields of f0: tau_ij = <u_i u_j> - <u_i><u_j> at the cell and the strain rate
+// S_ij = (d_i <u_j> + d_j <u_i>) / 2 by central differences (y, z periodic). Layout
+// samples[i * stride + offset + j]: i < 19 features, 19 <= i < 28 third order then fourth
+// order minus rho*/9, 28 <= i < 33 tau and 33 <= i < 38 S, each as (xy, xz, yz, xx - yy,
+// xx - zz).
 __global__ void k_closure_samples(const float* __restrict__ f0, const float* __restrict__ f1, Grid gc,
                                   const long long* __restrict__ cells, long long n,
                                   float* __restrict__ samples, long long stride, long long offset) {
@@ -228,25 +289,48 @@ __global__ void k_closure_samples(const float* __restrict__ f0, const float* __r
     const long long row = id / gc.nx;
     const int y = (int)(row % gc.ny), z = (int)(row / gc.ny);
     const long long cell = ((long long)z * gc.ny + y) * gc.pitch + x;
+    const int ym = y == 0 ? gc.ny - 1 : y - 1, yp = y == gc.ny - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? gc.nz - 1 : z - 1, zp = z == gc.nz - 1 ? 0 : z + 1;
+    auto at = [&](int xx, int yy, int zz) { return ((long long)zz * gc.ny + yy) * gc.pitch + xx; };
     float f[19], fs[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = f0[q * gc.plane + cell];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        int yy = y + ey(q), zz = z + ez(q);
-        yy = yy < 0 ? yy + gc.ny : (yy >= gc.ny ? yy - gc.ny : yy);
-        zz = zz < 0 ? zz + gc.nz : (zz >= gc.nz ? zz - gc.nz : zz);
-        fs[q] = f1[q * gc.plane + ((long long)zz * gc.ny + yy) * gc.pitch + x + ex(q)];
+        const int yy = ey(q) > 0 ? yp : (ey(q) < 0 ? ym : y);
+        const int zz = ez(q) > 0 ? zp : (ez(q) < 0 ? zm : z);
+        fs[q] = f1[q * gc.plane + at(x + ex(q), yy, zz)];
     }
     CMom m;
     moments_full<false>(f, m);
     const Raw rs = raw_moments<false>(fs);
     float t[kIn];
     central_moments(rs, m.u, m.v, m.w, m.r, t);
+    float* out = samples + offset + j;
 #pragma unroll
-    for (int i = 0; i < kIn; ++i) samples[i * stride + offset + j] = m.x[i];
+    for (int i = 0; i < kIn; ++i) out[i * stride] = m.x[i];
 #pragma unroll
-    for (int i = 0; i < kTargets; ++i) samples[(kIn + i) * stride + offset + j] = t[10 + i];
+    for (int i = 0; i < kTargets; ++i) out[(kIn + i) * stride] = t[10 + i];
+    // sub-grid stress and filtered strain rate
+    const float* a = f0 + 19 * gc.plane;  // aux planes
+    const float ux = a[cell], uy = a[gc.plane + cell], uz = a[2 * gc.plane + cell];
+    const float txx = a[3 * gc.plane + cell] - ux * ux, tyy = a[4 * gc.plane + cell] - uy * uy;
+    const float tzz = a[5 * gc.plane + cell] - uz * uz, txy = a[6 * gc.plane + cell] - ux * uy;
+    const float txz = a[7 * gc.plane + cell] - ux * uz, tyz = a[8 * gc.plane + cell] - uy * uz;
+    auto d = [&](int comp, long long cp, long long cm) {
+        return 0.5f * (a[comp * gc.plane + cp] - a[comp * gc.plane + cm]);
+    };
+    const long long xp_ = at(x + 1, y, z), xm_ = at(x - 1, y, z);
+    const long long yp_ = at(x, yp, z), ym_ = at(x, ym, z);
+    const long long zp_ = at(x, y, zp), zm_ = at(x, y, zm);
+    const float dux_dx = d(0, xp_, xm_), duy_dy = d(1, yp_, ym_), duz_dz = d(2, zp_, zm_);
+    const float sxy = 0.5f * (d(0, yp_, ym_) + d(1, xp_, xm_));
+    const float sxz = 0.5f * (d(0, zp_, zm_) + d(2, xp_, xm_));
+    const float syz = 0.5f * (d(1, zp_, zm_) + d(2, yp_, ym_));
+    const float sg[kSgs] = {txy, txz, tyz, txx - tyy, txx - tzz,
+                            sxy, sxz, syz, dux_dx - duy_dy, dux_dx - duz_dz};
+#pragma unroll
+    for (int i = 0; i < kSgs; ++i) out[(kIn + kTargets + i) * stride] = sg[i];
 }
 
 void launch_closure_samples(const float* f0, const float* f1, const Grid& gc, const long long* cells,
@@ -257,10 +341,10 @@ void launch_closure_samples(const float* f0, const float* f1, const Grid& gc, co
                                                                   offset);
 }
 
-// Per-block partial sums of the features and their squares over samples [0, n) and of the
-// squared pre-collision higher-order moments (sum_j x_{10+j}^2), for the standardisation
-// and the loss scale; reduced in a fixed order by k_stats_final.
-constexpr int kStats = 2 * kIn + 1;
+// Per-block partial sums of the features and their squares over samples [0, n), of the
+// squared pre-collision higher-order moments (sum_j x_{10+j}^2) and of the squared
+// deviatoric sub-grid stress, for the standardisation and the loss scales; reduced in a
+// fixed order by k_stats_final.
 __global__ void __launch_bounds__(256) k_sample_stats(const float* __restrict__ s, long long stride,
                                                       long long n, double* __restrict__ part) {
     __shared__ double red[256];
@@ -268,12 +352,19 @@ __global__ void __launch_bounds__(256) k_sample_stats(const float* __restrict__ 
 #pragma unroll
     for (int i = 0; i < kStats; ++i) acc[i] = 0.0;
     for (long long j = (long long)blockIdx.x * 256 + threadIdx.x; j < n; j += (long long)gridDim.x * 256) {
+        float xf[kIn];
 #pragma unroll
         for (int i = 0; i < kIn; ++i) {
-            const double v = s[i * stride + j];
+            xf[i] = s[i * stride + j];
+            const double v = xf[i];
             acc[i] += v;
             acc[kIn + i] += v * v;
             if (i >= 10) acc[2 * kIn] += v * v;
+        }
+#pragma unroll
+        for (int i = 0; i < kSgs / 2; ++i) {
+            const double tv = s[(kIn + kTargets + i) * stride + j];
+            acc[2 * kIn + 1] += tv * tv;
         }
     }
     for (int i = 0; i < kStats; ++i) {
@@ -365,11 +456,14 @@ __global__ void __launch_bounds__(128) k_closure_train(TrainArgs a) {
         if (valid)
             sidx = a.random ? a.off + (long long)(mix64(a.seed ^ (unsigned long long)slot) % (unsigned long long)a.count)
                             : a.off + slot;
-        float x[kIn], tg[kTargets];
+        float x[kIn], tg[kSgs];
 #pragma unroll
         for (int i = 0; i < kIn; ++i) x[i] = valid ? a.samples[i * a.stride + sidx] : 0.0f;
+        // mode 0: nine higher-order targets; mode 1: tau (5) and S (5)
+        const int t0 = net.mode == 1 ? kIn + kTargets : kIn;
+        const int nt = net.mode == 1 ? kSgs : kTargets;
 #pragma unroll
-        for (int i = 0; i < kTargets; ++i) tg[i] = valid ? a.samples[(kIn + i) * a.stride + sidx] : 0.0f;
+        for (int i = 0; i < kSgs; ++i) tg[i] = (valid && i < nt) ? a.samples[(t0 + i) * a.stride + sidx] : 0.0f;
         float v[32], z1[32];
 #pragma unroll
         for (int i = 0; i < kIn; ++i) v[i] = valid ? (x[i] - net.mu[i]) * net.sinv[i] : 0.0f;
@@ -412,17 +506,33 @@ __global__ void __launch_bounds__(128) k_closure_train(TrainArgs a) {
             z3 += net.w3[j] * gelu(v[j]);
         }
         const float th = tanh_approx(z3);
-        const float oms = -net.span * th;  // 1 - s_h
-        float dlds = 0.0f;
+        float dldth = 0.0f;  // d loss / d th
+        if (net.mode == 1) {
+            // tau_j + 2 nu_t S_j over the five deviatoric components
+            float dnudth;
+            const float nut = eddy_nu(net.nu, net.span, th, &dnudth) - net.nu;
+            float dldnu = 0.0f;
 #pragma unroll
-        for (int i = 0; i < kTargets; ++i) {
-            const float p = x[10 + i];
-            const float r = tg[i] - oms * p;
-            loss += valid ? a.wscale * r * r : 0.0f;
-            dlds += 2.0f * a.wscale * r * p;
+            for (int i = 0; i < kSgs / 2; ++i) {
+                const float r = tg[i] + 2.0f * nut * tg[kSgs / 2 + i];
+                loss += valid ? a.wscale * r * r : 0.0f;
+                dldnu += 4.0f * a.wscale * r * tg[kSgs / 2 + i];
+            }
+            dldth = dldnu * dnudth;
+        } else {
+            // t_j - (1 - s_h) p_j, s_h = 1 + span th, p_j the pre-collision moments
+            const float oms = -net.span * th;
+            float dlds = 0.0f;
+#pragma unroll
+            for (int i = 0; i < kTargets; ++i) {
+                const float r = tg[i] - oms * x[10 + i];
+                loss += valid ? a.wscale * r * r : 0.0f;
+                dlds += 2.0f * a.wscale * r * x[10 + i];
+            }
+            dldth = dlds * net.span;
         }
         if (!GRAD) continue;
-        const float d3 = valid ? dlds * net.span * (1.0f - th * th) : 0.0f;
+        const float d3 = valid ? dldth * (1.0f - th * th) : 0.0f;
         put_col(sAw, 64, tid, d3);
 #pragma unroll
         for (int j = 0; j < 32; ++j) {

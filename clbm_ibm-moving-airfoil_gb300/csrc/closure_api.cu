@@ -99,8 +99,9 @@ int clbm_closure_layout(int32_t* out) {
     const int32_t v[] = {closure::kMu, closure::kSinv, closure::kW1, closure::kB1, closure::kW2,
                          closure::kB2, closure::kW3, closure::kB3, closure::kSpan, closure::kParams,
                          closure::kIn, closure::kHid, closure::kTargets, closure::kTrainable,
-                         closure::kSampleFloats};
-    for (int i = 0; i < 15; ++i) out[i] = v[i];
+                         closure::kSampleFloats, closure::kMode, closure::kNu, closure::kSgs,
+                         closure::kStats};
+    for (int i = 0; i < 19; ++i) out[i] = v[i];
     return CLBM_OK;
 }
 
@@ -133,8 +134,8 @@ int clbm_trainer_create(int32_t device, const clbm_solver* fine, int64_t capacit
         cudaMalloc(&t->grad, sizeof(float) * closure::kTrainable) != cudaSuccess ||
         cudaMalloc(&t->m1, sizeof(float) * closure::kTrainable) != cudaSuccess ||
         cudaMalloc(&t->m2, sizeof(float) * closure::kTrainable) != cudaSuccess ||
-        cudaMalloc(&t->stats_part, sizeof(double) * (2 * closure::kIn + 1) * 1024) != cudaSuccess ||
-        cudaMalloc(&t->stats, sizeof(double) * (2 * closure::kIn + 1)) != cudaSuccess ||
+        cudaMalloc(&t->stats_part, sizeof(double) * closure::kStats * 1024) != cudaSuccess ||
+        cudaMalloc(&t->stats, sizeof(double) * closure::kStats) != cudaSuccess ||
         cudaMalloc(&t->status, sizeof(unsigned int)) != cudaSuccess ||
         cudaMemset(t->status, 0, sizeof(unsigned int)) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "clbm_trainer_create: device allocation failed"));
@@ -146,7 +147,7 @@ int clbm_trainer_create(int32_t device, const clbm_solver* fine, int64_t capacit
         g.pitch = (g.nx + 31) / 32 * 32;
         g.plane = (long long)g.pitch * g.ny * g.nz;
         g.status = t->status;
-        const size_t bytes = sizeof(float) * 19 * (size_t)g.plane;
+        const size_t bytes = sizeof(float) * (19 + closure::kAux) * (size_t)g.plane;
         for (int k = 0; k < 2; ++k)
             if (cudaMalloc(&t->slot[k], bytes) != cudaSuccess)
                 return bail(fail(CLBM_ERR_CUDA, "clbm_trainer_create: device allocation failed"));
@@ -184,14 +185,16 @@ int clbm_trainer_read_slot(clbm_trainer* t, int32_t slot, float* out) {
     if (!t || slot < 0 || slot > 1 || !out || !t->slot[0])
         return fail(CLBM_ERR_ARG, "clbm_trainer_read_slot: invalid argument");
     const Grid& g = t->gc;
-    std::vector<float> h((size_t)19 * g.plane);
+    constexpr int nch = 19 + closure::kAux;
+    std::vector<float> h((size_t)nch * g.plane);
     CK(cudaMemcpy(h.data(), t->slot[slot], sizeof(float) * h.size(), cudaMemcpyDeviceToHost));
-    // reference layout (nx, ny, nz, 19), z fastest
+    // reference layout (nx, ny, nz, 28), z fastest: 19 populations, then the filtered
+    // velocity (3) and velocity products (xx, yy, zz, xy, xz, yz)
     for (int x = 0; x < g.nx; ++x)
         for (int y = 0; y < g.ny; ++y)
             for (int z = 0; z < g.nz; ++z)
-                for (int q = 0; q < 19; ++q)
-                    out[(((size_t)x * g.ny + y) * g.nz + z) * 19 + q] =
+                for (int q = 0; q < nch; ++q)
+                    out[(((size_t)x * g.ny + y) * g.nz + z) * nch + q] =
                         h[(size_t)q * g.plane + ((size_t)z * g.ny + y) * g.pitch + x];
     return CLBM_OK;
 }
@@ -266,7 +269,7 @@ int clbm_trainer_stats(clbm_trainer* t, int64_t off, int64_t n, double* out) {
     const int blocks = (int)std::min<long long>(1024, (n + 255) / 256);
     launch_sample_stats(t->samples + off, t->capacity, n, t->stats_part, blocks, t->stats, t->st);
     CK_LAUNCH();
-    CK(cudaMemcpyAsync(out, t->stats, sizeof(double) * (2 * closure::kIn + 1), cudaMemcpyDeviceToHost, t->st));
+    CK(cudaMemcpyAsync(out, t->stats, sizeof(double) * closure::kStats, cudaMemcpyDeviceToHost, t->st));
     return tr_sync(t);
 }
 

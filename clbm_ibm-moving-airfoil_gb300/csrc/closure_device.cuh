@@ -146,24 +146,44 @@ __device__ __forceinline__ float bf16_round(float x) {
     return __bfloat162float(__float2bfloat16_rn(x));
 }
 
+// Two values rounded to bf16 and packed (first in the low half), one conversion.
+__device__ __forceinline__ uint32_t bf16x2_bits(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 // Write one row (32 values, rounded to bf16) of a K-major tile with 32 columns.
 __device__ __forceinline__ void put_row32(unsigned char* tile, int row, const float (&v)[32]) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         uint32_t wv[4];
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-            wv[t] = (uint32_t)bf16_bits(v[8 * j + 2 * t]) | ((uint32_t)bf16_bits(v[8 * j + 2 * t + 1]) << 16);
+        for (int t = 0; t < 4; ++t) wv[t] = bf16x2_bits(v[8 * j + 2 * t], v[8 * j + 2 * t + 1]);
         *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(row, 8 * j, 32)) =
             make_uint4(wv[0], wv[1], wv[2], wv[3]);
     }
+}
+
+// GELU of two values with the packed f32x2 arithmetic and one half2 hardware tanh (the
+// inference path; the training kernels use the float32 form above).
+__device__ __forceinline__ V2 gelu2(V2 z) {
+    const V2 zz = z * z;
+    const V2 inner = z * vfma(vsplat(0.7978845608028654f * 0.044715f, z), zz, vsplat(0.7978845608028654f, z));
+    const float2 in = vunpack(inner);
+    const __half2 hin = __floats2half2_rn(in.x, in.y);
+    uint32_t hout;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(hout) : "r"(*reinterpret_cast<const uint32_t*>(&hin)));
+    const float2 t = __half22float2(*reinterpret_cast<const __half2*>(&hout));
+    const V2 hz = vsplat(0.5f, z) * z;
+    return vfma(hz, vpack(t.x, t.y), hz);
 }
 
 // Network constants a block keeps in shared memory next to the BF16 weight images.
 struct NetSmem {
     float mu[kIn], sinv[kIn];
     float b1[kHid], b2[kHid], w3[kHid];
-    float b3, span;
+    float b3, span, nu;
+    int mode;
 };
 
 __device__ __forceinline__ void load_net(const float* __restrict__ p, NetSmem& n, int tid, int nthreads) {
@@ -179,6 +199,8 @@ __device__ __forceinline__ void load_net(const float* __restrict__ p, NetSmem& n
     if (tid == 0) {
         n.b3 = p[kB3];
         n.span = p[kSpan];
+        n.mode = (int)p[kMode];
+        n.nu = p[kNu];
     }
 }
 
@@ -188,6 +210,21 @@ __device__ __forceinline__ void standardise(const CMom& m, const NetSmem& n, flo
     for (int i = 0; i < kIn; ++i) xs[i] = (m.x[i] - n.mu[i]) * n.sinv[i];
 #pragma unroll
     for (int i = kIn; i < 32; ++i) xs[i] = 0.0f;
+}
+
+// Eddy-viscosity closure for the network output th = tanh(z3): effective viscosity
+// nu 2^(span g), g = th for th >= 0 and th / 20 below (the network adds viscosity and may
+// remove at most a factor 2^(-span/20)), its rate s = 1 / (1/2 + 3 nu_eff), and
+// d nu_eff / d th.
+constexpr float kEddyLeak = 0.05f;
+__device__ __forceinline__ float eddy_nu(float nu, float span, float th, float* dnudth) {
+    const float slope = th >= 0.0f ? 1.0f : kEddyLeak;
+    const float nue = nu * exp2f(span * slope * th);
+    if (dnudth) *dnudth = nue * 0.69314718f * span * slope;
+    return nue;
+}
+__device__ __forceinline__ float eddy_rate(float nu, float span, float th) {
+    return 1.0f / (0.5f + 3.0f * eddy_nu(nu, span, th, nullptr));
 }
 
 // Post-collision third-order central moments and fourth-order deviations from r/9 for

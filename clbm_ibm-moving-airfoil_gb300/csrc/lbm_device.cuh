@@ -184,9 +184,11 @@ __device__ __forceinline__ V2 vrcp(V2 a) {
 // their post-collision values (k210, k120, k201, k021, k102, k012, then k220 - r/9,
 // k202 - r/9, k022 - r/9), which the closure computes (the reference's s_q = s_pi = 1
 // gives zeros).
-template <class V, bool FORCE, bool DEV, bool HO = false>
+// SVC: the deviatoric second-order moments relax with the per-cell rate s (osv_cell =
+// 1 - s) instead of s_v (eddy-viscosity closure).
+template <class V, bool FORCE, bool DEV, bool HO = false, bool SVC = false>
 __device__ __forceinline__ void collide_v(V (&f)[19], const Coef& c, V Fx, V Fy, V Fz,
-                                          const V* ho = nullptr) {
+                                          const V* ho = nullptr, V osv_cell = V{}) {
     const V z0 = f[0];
     const V one = vsplat(1.0f, z0), third = vsplat(1.0f / 3.0f, z0);
     const V half = vsplat(0.5f, z0), quarter = vsplat(0.25f, z0), two = vsplat(2.0f, z0);
@@ -227,7 +229,7 @@ __device__ __forceinline__ void collide_v(V (&f)[19], const Coef& c, V Fx, V Fy,
     const V k101 = pxz - vfma(u, mz - wr, w * mx);
     const V k011 = pyz - vfma(v, mz - wr, w * my);
     // relaxation (clbm_moving.py:170-196)
-    const V osv = vsplat(c.one_m_sv, z0);
+    const V osv = SVC ? osv_cell : vsplat(c.one_m_sv, z0);
     const V k110s = k110 * osv, k101s = k101 * osv, k011s = k011 * osv;
     const V kA = (k200 + k020) + k002;
     const V kAs = vfma(vsplat(-c.s_e, z0), kA - r, kA);
@@ -345,6 +347,18 @@ __device__ __forceinline__ void collide_ho(float (&f)[19], const Coef& c, const 
 #pragma unroll
     for (int i = 0; i < 9; ++i) h[i].x = ho[i];
     collide_v<V, false, DEV, true>(t, c, V{0.f}, V{0.f}, V{0.f}, h);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = t[q].x;
+}
+
+// One cell whose deviatoric second-order moments relax with 1 - osv (closure).
+template <bool DEV>
+__device__ __forceinline__ void collide_sv(float (&f)[19], const Coef& c, float osv) {
+    using V = typename std::conditional<DEV, V1, F1>::type;
+    V t[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q].x = f[q];
+    collide_v<V, false, DEV, false, true>(t, c, V{0.f}, V{0.f}, V{0.f}, nullptr, V{osv});
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = t[q].x;
 }

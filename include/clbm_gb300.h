@@ -208,9 +208,13 @@ int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_la
  * third- and fourth-order central moments, which the reference relaxes fully (s_q = s_pi
  * = 1 in _collide, clbm_moving.py:186-194). Not part of the reference.
  *
- * Parameter array offsets (floats): out[0..14] = mu, sinv, W1, b1, W2, b2, W3, b3, span,
- * total, inputs (19), hidden width (32), targets per sample (9), trainable count, floats
- * per training sample (28). */
+ * Parameter array offsets (floats): out[0..18] = mu, sinv, W1, b1, W2, b2, W3, b3, span,
+ * total, inputs (19), hidden width (32), higher-order targets per sample (9), trainable
+ * count, floats per training sample (38), mode, nu, sub-grid stress values per sample
+ * (10), statistics count (40). mode 0: the rate of the third/fourth-order moments,
+ * s_h = 1 + span tanh(z3); mode 1: an eddy viscosity, the deviatoric second-order moments
+ * relax with 1 / (1/2 + 3 nu 2^(span g)), g = tanh(z3) where positive and tanh(z3) / 20
+ * below, nu the solver's viscosity (the nu entry is the viscosity the training assumes). */
 int clbm_closure_layout(int32_t* out);
 
 /* Enable the closure for the bulk pass of later steps (params: host array of the layout
@@ -220,26 +224,31 @@ int clbm_closure_set(clbm_solver* s, const float* params);
 
 /* Trainer: samples from box-filtered fields of a fine lattice (twice the coarse one in
  * each direction, float32 storage) and Adam training on the device. Sample i holds 19
- * features (moments of the filtered pre-collision state) and 9 targets (third- and
- * fourth-order moments of the ideal post-collision state f*_q(x) = f_q(x + e_q) one
- * coarse step later). fine may be NULL (samples written by the caller). */
+ * features (moments of the filtered pre-collision state), 9 higher-order targets (moments
+ * of the ideal post-collision state f*_q(x) = f_q(x + e_q) one coarse step later) and 10
+ * sub-grid stress values (deviatoric parts of tau = <u u> - <u><u> of the filtered fine
+ * velocity and of the filtered strain rate). fine may be NULL (samples written by the
+ * caller). */
 typedef struct clbm_trainer clbm_trainer;
 int clbm_trainer_create(int32_t device, const clbm_solver* fine, int64_t capacity, clbm_trainer** out);
 int clbm_trainer_destroy(clbm_trainer* t);
 /* Filter the fine lattice's current post-stream state into slot 0 or 1. */
 int clbm_trainer_capture(clbm_trainer* t, int32_t slot);
-/* A captured slot in the reference layout (nx/2, ny/2, nz/2, 19), z fastest. */
+/* A captured slot in the reference layout (nx/2, ny/2, nz/2, 28), z fastest: 19 filtered
+ * populations, the filtered velocity (3) and velocity products (xx, yy, zz, xy, xz, yz). */
 int clbm_trainer_read_slot(clbm_trainer* t, int32_t slot, float* out);
 /* Append samples at coarse cells (x + nx (y + ny z), 1 <= x <= nx - 2) from slots 0 -> 1. */
 int clbm_trainer_extract(clbm_trainer* t, const int64_t* cells, int64_t n);
 int clbm_trainer_count(const clbm_trainer* t, int64_t* n);
-/* Samples as [n][28] host rows. */
+/* Samples as [n][38] host rows. */
 int clbm_trainer_write_samples(clbm_trainer* t, int64_t off, int64_t n, const float* in);
 int clbm_trainer_read_samples(clbm_trainer* t, int64_t off, int64_t n, float* out);
-/* Sums of the 19 features, of their squares and of the squared third/fourth-order
- * features over a sample range (39 doubles). */
+/* Sums of the 19 features, of their squares, of the squared third/fourth-order features
+ * and of the squared deviatoric sub-grid stress over a sample range (40 doubles). */
 int clbm_trainer_stats(clbm_trainer* t, int64_t off, int64_t n, double* out);
-/* Loss sum_j (t_j - (1 - s_h) p_j)^2 * wscale summed over a sample range. */
+/* Loss summed over a sample range: mode 0, sum_j (t_j - (1 - s_h) p_j)^2 over the nine
+ * higher-order moments; mode 1, sum_j (tau_j + 2 nu_t S_j)^2 over the five deviatoric
+ * components; times wscale. */
 int clbm_trainer_loss(clbm_trainer* t, const float* params, int64_t off, int64_t n, float wscale,
                       double* loss_sum);
 /* Gradient of the mean loss over a sample range w.r.t. W1, b1, W2, b2, W3, b3 (in the

@@ -65,8 +65,9 @@ static const int PQR[19][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1
                                {2, 1, 0}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2},
                                {0, 1, 2}, {2, 2, 0}, {2, 0, 2}, {0, 2, 2}};
 
-/* closure_oracle.c: post-collision higher-order moments of the learned closure */
-void oracle_closure_post(const float *params, const double *f, double *post9);
+/* closure_oracle.c: the learned closure for one cell (higher-order post-collision
+   moments, or the shear rate of the eddy-viscosity form) */
+double oracle_closure_post(const float *params, const double *f, double nu, double *post9);
 
 typedef struct {
     int nx, ny, nz, n;
@@ -197,28 +198,37 @@ static void or_collide(oracle_t *o) {
         }
         (void)k210; (void)k120; (void)k201; (void)k021; (void)k102; (void)k012;
         (void)k220; (void)k202; (void)k022;
+        REAL k210s = 0, k120s = 0, k201s = 0, k021s = 0, k102s = 0, k012s = 0;
+        REAL osv = one_m_sv;  /* 1 - shear rate of this cell */
+        REAL k220s = r / (REAL)9.0, k202s = r / (REAL)9.0, k022s = r / (REAL)9.0;
+        if (o->closure && (size_t)cl / ((size_t)o->ny * o->nz) > 0 &&
+            (size_t)cl / ((size_t)o->ny * o->nz) < (size_t)o->nx - 1) {
+            /* learned closure (not part of the reference): the third/fourth-order central
+               moments relax with the network's rate instead of 1 (mode 0), or the shear
+               moments with the network's eddy-viscosity rate instead of s_v (mode 1); the
+               inlet and outlet columns keep the plain rates */
+            double fd[19], post[9];
+            for (int q = 0; q < 19; ++q) fd[q] = (double)fc[q];
+            const double nu = (1.0 / o->s_v - 0.5) / 3.0;
+            const double se = oracle_closure_post(o->closure, fd, nu, post);
+            if (se > 0.0) {
+                osv = (REAL)(1.0 - se);
+            } else {
+                k210s = (REAL)post[0]; k120s = (REAL)post[1]; k201s = (REAL)post[2];
+                k021s = (REAL)post[3]; k102s = (REAL)post[4]; k012s = (REAL)post[5];
+                k220s += (REAL)post[6]; k202s += (REAL)post[7]; k022s += (REAL)post[8];
+            }
+        }
         /* cascade relaxation, clbm_moving.py:170-196 */
-        REAL k110s = k110 * one_m_sv, k101s = k101 * one_m_sv, k011s = k011 * one_m_sv;
+        REAL k110s = k110 * osv, k101s = k101 * osv, k011s = k011 * osv;
         REAL kA = k200 + k020 + k002;
         REAL kA_eq = r;
         REAL kD = k200 - k020, kE = k200 - k002;
         REAL kAs = kA - s_e * (kA - kA_eq);
-        REAL kDs = kD * one_m_sv, kEs = kE * one_m_sv;
+        REAL kDs = kD * osv, kEs = kE * osv;
         REAL k200s = (kAs + kDs + kEs) / (REAL)3.0;
         REAL k020s = (kAs - (REAL)2.0 * kDs + kEs) / (REAL)3.0;
         REAL k002s = (kAs + kDs - (REAL)2.0 * kEs) / (REAL)3.0;
-        REAL k210s = 0, k120s = 0, k201s = 0, k021s = 0, k102s = 0, k012s = 0;
-        REAL k220s = r / (REAL)9.0, k202s = r / (REAL)9.0, k022s = r / (REAL)9.0;
-        if (o->closure) {
-            /* learned closure (not part of the reference): third/fourth-order central
-               moments relax with the network's rate s_h instead of 1 */
-            double fd[19], post[9];
-            for (int q = 0; q < 19; ++q) fd[q] = (double)fc[q];
-            oracle_closure_post(o->closure, fd, post);
-            k210s = (REAL)post[0]; k120s = (REAL)post[1]; k201s = (REAL)post[2];
-            k021s = (REAL)post[3]; k102s = (REAL)post[4]; k012s = (REAL)post[5];
-            k220s += (REAL)post[6]; k202s += (REAL)post[7]; k022s += (REAL)post[8];
-        }
         /* central -> raw, clbm_moving.py:198-231 */
         REAL T[19];
         T[0] = r;
@@ -482,14 +492,14 @@ void oracle_destroy(void *h) {
     free(o);
 }
 
-/* Learned closure for later collisions (params: 2186 floats, copied; NULL: off). */
+/* Learned closure for later collisions (params: 2188 floats, copied; NULL: off). */
 void oracle_set_closure(void *h, const float *params) {
     oracle_t *o = (oracle_t *)h;
     free(o->closure);
     o->closure = NULL;
     if (!params) return;
-    o->closure = (float *)malloc(sizeof(float) * 2186);
-    memcpy(o->closure, params, sizeof(float) * 2186);
+    o->closure = (float *)malloc(sizeof(float) * 2188);
+    memcpy(o->closure, params, sizeof(float) * 2188);
 }
 
 int oracle_real_size(void) { return (int)sizeof(REAL); }

@@ -44,6 +44,7 @@ def load(real="f32"):
         lib.oracle_closure_nparams.restype = i
         lib.oracle_closure_features.argtypes = [P, i, P]
         lib.oracle_closure_samples.argtypes = [P, P, i, i, i, P, i, P]
+        lib.oracle_closure_filter.argtypes = [P, i, i, i, P]
         lib.oracle_closure_forward.argtypes = [P, P, i, i, P]
         lib.oracle_closure_loss_grad.argtypes = [P, P, i, d, i, P, P]
         _LIBS[real] = lib
@@ -160,13 +161,23 @@ def closure_features(f):
     return x
 
 
+def closure_filter(f_fine):
+    """Box filter of fine post-stream populations (nx, ny, nz, 19) onto the coarse lattice:
+    (nx/2, ny/2, nz/2, 28) with the mean populations, velocity and velocity products."""
+    f = np.ascontiguousarray(f_fine, np.float64)
+    nx, ny, nz, _ = f.shape
+    out = np.empty((nx // 2, ny // 2, nz // 2, 28), np.float64)
+    load("f64").oracle_closure_filter(_ptr(f), nx, ny, nz, _ptr(out))
+    return out
+
+
 def closure_samples(f0, f1, cells):
-    """Samples [n, 28] of coarse cells from filtered states in the reference layout."""
+    """Samples [n, 38] of coarse cells from two filtered states (nx, ny, nz, 28)."""
     f0 = np.ascontiguousarray(f0, np.float64)
     f1 = np.ascontiguousarray(f1, np.float64)
     nx, ny, nz, _ = f0.shape
     c = np.ascontiguousarray(cells, np.int64)
-    out = np.empty((c.size, 28), np.float64)
+    out = np.empty((c.size, 38), np.float64)
     load("f64").oracle_closure_samples(_ptr(f0), _ptr(f1), nx, ny, nz, _ptr(c), int(c.size),
                                        _ptr(out))
     return out
