@@ -24,7 +24,7 @@ import numpy as np
 
 from . import analysis, closure
 from ._lib import DivergedError
-from .config import force_coefficients, wing_case
+from .config import body_xy_extent, force_coefficients, wing_case
 from .solver import Simulation
 
 
@@ -87,15 +87,18 @@ def run_fine(coarse_steps, sample_every, sample_start, cells_per_snapshot, seed,
              base=BASE, re=5000.0):
     cfg = study_case(scale=2, storage="f32", re=re, base=base)
     coarse_shape = (cfg.nx // 2, cfg.ny // 2, cfg.nz // 2)
-    ccfg = study_case(scale=1, re=re, base=base)
     sim = Simulation(cfg)
     snaps = max(0, (coarse_steps - sample_start) // sample_every + 1)
     trainer = closure.Trainer(capacity=max(1, snaps * cells_per_snapshot), fine=sim.solver)
     rng = np.random.default_rng(seed)
-    # training cells: away from the inlet/outlet and from the region the body sweeps
-    exclude = (int(ccfg.x0 - 0.5 * ccfg.chord), int(ccfg.x0 + 1.25 * ccfg.chord),
-               int(ccfg.y0 - ccfg.a_heave - 0.5 * ccfg.chord),
-               int(ccfg.y0 + ccfg.a_heave + 0.5 * ccfg.chord))
+
+    def exclude_at(fine_step):
+        """Coarse cells near the body at this step (its fine-lattice marker extent halved,
+        widened by 3 coarse cells: the IBM stencils and forced cells), so the samples
+        include the flow up to the edge of the forced region but no forced cell."""
+        x0, x1, y0, y1 = body_xy_extent(cfg, cfg.motion_state(fine_step))
+        return (int(math.floor(x0 / 2)) - 3, int(math.ceil(x1 / 2)) + 3,
+                int(math.floor(y0 / 2)) - 3, int(math.ceil(y1 / 2)) + 3)
     fine_steps = 2 * coarse_steps
     chunk = 2000
     period = _period(cfg)
@@ -120,7 +123,7 @@ def run_fine(coarse_steps, sample_every, sample_start, cells_per_snapshot, seed,
             wall_total += w
             done += d
             trainer.capture(1)
-            trainer.extract(closure.sample_cells(coarse_shape, exclude, cells_per_snapshot, rng))
+            trainer.extract(closure.sample_cells(coarse_shape, exclude_at(m), cells_per_snapshot, rng))
             sample_wall += time.perf_counter() - t0 - w
         log(f"fine step {done}/{fine_steps}, samples {trainer.count}")
     window = _window(fine_steps, period)

@@ -357,6 +357,15 @@ def from_config_module(mod, storage="f32"):
     return cfg
 
 
+def body_xy_extent(cfg, state):
+    """x and y extent (min, max) of the markers for one motion state (xc, yc, theta, ...)."""
+    xc, yc, th = (np.float32(v) for v in state[:3])
+    c, s = np.cos(th), np.sin(th)
+    x = xc + cfg.X0 * c - cfg.Y0 * s
+    y = yc + cfg.X0 * s + cfg.Y0 * c
+    return float(x.min()), float(x.max()), float(y.min()), float(y.max())
+
+
 def stencil_box_cells(cfg, state):
     """Cells of the box that bounds every 4x4x4 Peskin stencil for one motion state
     (xc, yc, theta, ...), by the rule the marker kernel applies: stencil base floor(x) - 1,

@@ -72,7 +72,6 @@ int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bo
         ca.params = s->cl_params;
         ca.img = s->cl_img;
         ca.cells = (long long)cells(s);
-        ca.tiles = (ca.cells + 127) / 128;
         launch_closure_stream_collide(s->cfg.storage, !s->local, fmode, s->f[s->cur], s->f[1 - s->cur],
                                       s->g, s->c, fa, ca, s->cl_grid, st);
     } else {

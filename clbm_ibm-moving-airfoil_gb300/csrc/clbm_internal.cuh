@@ -346,7 +346,7 @@ struct ClosureArgs {
     const float* params;      // closure parameter array (closure::kParams floats)
     const uint16_t* img;      // BF16 weight images (closure::kImgElems)
     long long cells;          // nx * ny * nz
-    long long tiles;          // ceil(cells / 128)
+    long long tiles;          // set by the launcher from its tile size
 };
 
 struct TrainArgs {

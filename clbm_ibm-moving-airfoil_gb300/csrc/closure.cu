@@ -40,11 +40,12 @@ namespace {
 
 constexpr uint32_t kIdescFwd = tc::idesc_bf16(128, 32);
 
-// Issue D = A (128 x 32, K-major) * B^T (32 x 32) as two K = 16 MMAs and commit.
+// Issue D = A (128 x 32, K-major) * B^T (32 x 32) as two K = 16 MMAs; commit to `bar`
+// (the completion of every MMA this thread issued so far) unless it is null.
 __device__ __forceinline__ void mma_k32(uint32_t tmem, uint32_t a, uint32_t b, uint64_t* bar) {
     tc::mma(tmem, tc::smem_desc(a, 128, 512), tc::smem_desc(b, 128, 512), kIdescFwd, false);
     tc::mma(tmem, tc::smem_desc(a + 256, 128, 512), tc::smem_desc(b + 256, 128, 512), kIdescFwd, true);
-    tc::commit(bar);
+    if (bar) tc::commit(bar);
 }
 
 // Block-wide barrier that also orders tensor-core work around it.
@@ -215,7 +216,9 @@ int closure_grid(int storage) {
 
 void launch_closure_stream_collide(int storage, bool pull, int fmode, const void* fin, void* fout,
                                    const Grid& g, const Coef& c, const ForceArgs& fa,
-                                   const ClosureArgs& ca, int grid, cudaStream_t st) {
+                                   const ClosureArgs& cargs, int grid, cudaStream_t st) {
+    ClosureArgs ca = cargs;
+    ca.tiles = (ca.cells + 127) / 128;
     CLBM_CL_STORE(storage, {
         if (pull) closure_sc<S_, true>(fmode, fin, fout, g, c, fa, ca, grid, st);
         else closure_sc<S_, false>(fmode, fin, fout, g, c, fa, ca, grid, st);

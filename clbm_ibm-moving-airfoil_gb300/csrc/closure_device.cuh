@@ -21,26 +21,28 @@ struct CMom {
                     // 200, 020, 002, 210, 120, 201, 021, 102, 012, 220, 202, 022
 };
 
-// Raw moments of a population vector up to the fourth order present in D3Q19. DEV: f holds
+// Raw moments of a population vector up to the fourth order present in D3Q19, over a
+// value type T (F1: one cell; V2: two cells in packed f32x2 arithmetic). DEV: f holds
 // deviations f - w; the weights' part of the even moments is kept apart (sum w = 1,
 // sum w e_a^2 = 1/3, sum w e_a^2 e_b^2 = 1/9; odd moments of w vanish).
-struct Raw {
-    float R0;                  // sum f (deviations: sum of deviations)
-    float r;                   // density
-    float mx, my, mz;
-    float Pxx, Pyy, Pzz;       // second diagonal, without the weights' part
-    float Mxx, Myy, Mzz;       // second diagonal, full
-    float pxy, pxz, pyz;
-    float M210, M120, M201, M021, M102, M012;
-    float A220, A202, A022;    // fourth, without the weights' part
+template <class T>
+struct RawT {
+    T R0;                      // sum f (deviations: sum of deviations)
+    T r;                       // density
+    T mx, my, mz;
+    T Pxx, Pyy, Pzz;           // second diagonal, without the weights' part
+    T Mxx, Myy, Mzz;           // second diagonal, full
+    T pxy, pxz, pyz;
+    T M210, M120, M201, M021, M102, M012;
+    T A220, A202, A022;        // fourth, without the weights' part
 };
 
-template <bool DEV>
-__device__ __forceinline__ Raw raw_moments(const float (&f)[19]) {
-    Raw m;
-    const float sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
-    const float a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
-    const float e = f[15] + f[16], h = f[17] + f[18];
+template <class T, bool DEV>
+__device__ __forceinline__ RawT<T> raw_moments_t(const T (&f)[19]) {
+    RawT<T> m;
+    const T sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+    const T a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
+    const T e = f[15] + f[16], h = f[17] + f[18];
     m.R0 = f[0] + (sx + sy + sz) + (a + b) + (cc + d) + (e + h);
     m.mx = (f[1] - f[2]) + (f[7] - f[8]) + (f[9] - f[10]) + (f[11] - f[12]) + (f[13] - f[14]);
     m.my = (f[3] - f[4]) + (a - b) + (f[15] - f[16]) + (f[17] - f[18]);
@@ -61,25 +63,29 @@ __device__ __forceinline__ Raw raw_moments(const float (&f)[19]) {
     m.A220 = a + b;
     m.A202 = cc + d;
     m.A022 = e + h;
-    const float s3 = DEV ? 1.0f / 3.0f : 0.0f;
-    m.r = m.R0 + (DEV ? 1.0f : 0.0f);
+    const T s3 = vsplat(DEV ? 1.0f / 3.0f : 0.0f, f[0]);
+    m.r = m.R0 + vsplat(DEV ? 1.0f : 0.0f, f[0]);
     m.Mxx = m.Pxx + s3;
     m.Myy = m.Pyy + s3;
     m.Mzz = m.Pzz + s3;
     return m;
 }
 
-// Non-equilibrium central moments about the velocity (u, v, w), divided by rho_n, by the
-// binomial expansion of sum f (e_x - u)^p (e_y - v)^q (e_z - w)^r; the equilibrium
+// Non-equilibrium central moments about the velocity (u, v, w), times inv_rho (1 / rho_n),
+// by the binomial expansion of sum f (e_x - u)^p (e_y - v)^q (e_z - w)^r; the equilibrium
 // values subtracted are rho/3 (second diagonal) and rho/9 (fourth).
-__device__ __forceinline__ void central_moments(const Raw& m, float u, float v, float w, float rho_n,
-                                                float (&x)[kIn]) {
-    const float r = m.r, R0 = m.R0;
-    const float mx = m.mx, my = m.my, mz = m.mz;
-    const float ur = u * r, vr = v * r, wr = w * r;
-    const float uu = u * u, vv = v * v, ww = w * w;
-    float k[kIn];
-    k[0] = 0.0f;
+template <class T>
+__device__ __forceinline__ void central_moments_t(const RawT<T>& m, T u, T v, T w, T inv_rho,
+                                                  T (&x)[kIn]) {
+    const T c2 = vsplat(2.0f, u), c4 = vsplat(4.0f, u);
+    const T c13 = vsplat(1.0f / 3.0f, u), c19 = vsplat(1.0f / 9.0f, u);
+    const T r = m.r, R0 = m.R0;
+    const T mx = m.mx, my = m.my, mz = m.mz;
+    const T ur = u * r, vr = v * r, wr = w * r;
+    const T uu = u * u, vv = v * v, ww = w * w;
+    const T uv2 = c2 * u * v, uw2 = c2 * u * w, vw2 = c2 * v * w;
+    T k[kIn];
+    k[0] = vsplat(0.0f, u);
     k[1] = mx - ur;
     k[2] = my - vr;
     k[3] = mz - wr;
@@ -87,39 +93,66 @@ __device__ __forceinline__ void central_moments(const Raw& m, float u, float v, 
     k[5] = m.pxz - u * mz - w * mx + u * wr;
     k[6] = m.pyz - v * mz - w * my + v * wr;
     // k200 - r/3 = (P - R0/3) - 2u mx + u^2 r
-    k[7] = (m.Pxx - R0 * (1.0f / 3.0f)) + u * (ur - 2.0f * mx);
-    k[8] = (m.Pyy - R0 * (1.0f / 3.0f)) + v * (vr - 2.0f * my);
-    k[9] = (m.Pzz - R0 * (1.0f / 3.0f)) + w * (wr - 2.0f * mz);
+    k[7] = (m.Pxx - R0 * c13) + u * (ur - c2 * mx);
+    k[8] = (m.Pyy - R0 * c13) + v * (vr - c2 * my);
+    k[9] = (m.Pzz - R0 * c13) + w * (wr - c2 * mz);
     // third order, e.g. k210 = M210 - 2u M110 - v M200 + 2uv M100 + u^2 M010 - u^2 v M000
-    k[10] = m.M210 - 2.0f * u * m.pxy - v * m.Mxx + 2.0f * u * v * mx + uu * (my - vr);
-    k[11] = m.M120 - 2.0f * v * m.pxy - u * m.Myy + 2.0f * u * v * my + vv * (mx - ur);
-    k[12] = m.M201 - 2.0f * u * m.pxz - w * m.Mxx + 2.0f * u * w * mx + uu * (mz - wr);
-    k[13] = m.M021 - 2.0f * v * m.pyz - w * m.Myy + 2.0f * v * w * my + vv * (mz - wr);
-    k[14] = m.M102 - 2.0f * w * m.pxz - u * m.Mzz + 2.0f * u * w * mz + ww * (mx - ur);
-    k[15] = m.M012 - 2.0f * w * m.pyz - v * m.Mzz + 2.0f * v * w * mz + ww * (my - vr);
+    k[10] = m.M210 - c2 * u * m.pxy - v * m.Mxx + uv2 * mx + uu * (my - vr);
+    k[11] = m.M120 - c2 * v * m.pxy - u * m.Myy + uv2 * my + vv * (mx - ur);
+    k[12] = m.M201 - c2 * u * m.pxz - w * m.Mxx + uw2 * mx + uu * (mz - wr);
+    k[13] = m.M021 - c2 * v * m.pyz - w * m.Myy + vw2 * my + vv * (mz - wr);
+    k[14] = m.M102 - c2 * w * m.pxz - u * m.Mzz + uw2 * mz + ww * (mx - ur);
+    k[15] = m.M012 - c2 * w * m.pyz - v * m.Mzz + vw2 * mz + ww * (my - vr);
     // fourth order, e.g. k220 - r/9 = (A220 - R0/9) - 2v M210 - 2u M120 + v^2 M200
     //   + u^2 M020 + 4uv M110 - 2uv^2 M100 - 2u^2 v M010 + u^2 v^2 M000
-    k[16] = (m.A220 - R0 * (1.0f / 9.0f)) - 2.0f * v * m.M210 - 2.0f * u * m.M120 + vv * m.Mxx +
-            uu * m.Myy + 4.0f * u * v * m.pxy - 2.0f * u * vv * mx - 2.0f * uu * v * my + uu * vv * r;
-    k[17] = (m.A202 - R0 * (1.0f / 9.0f)) - 2.0f * w * m.M201 - 2.0f * u * m.M102 + ww * m.Mxx +
-            uu * m.Mzz + 4.0f * u * w * m.pxz - 2.0f * u * ww * mx - 2.0f * uu * w * mz + uu * ww * r;
-    k[18] = (m.A022 - R0 * (1.0f / 9.0f)) - 2.0f * w * m.M021 - 2.0f * v * m.M012 + ww * m.Myy +
-            vv * m.Mzz + 4.0f * v * w * m.pyz - 2.0f * v * ww * my - 2.0f * vv * w * mz + vv * ww * r;
-    const float inv = 1.0f / rho_n;
+    k[16] = (m.A220 - R0 * c19) - c2 * v * m.M210 - c2 * u * m.M120 + vv * m.Mxx + uu * m.Myy +
+            c4 * u * v * m.pxy - uv2 * v * mx - uv2 * u * my + uu * vv * r;
+    k[17] = (m.A202 - R0 * c19) - c2 * w * m.M201 - c2 * u * m.M102 + ww * m.Mxx + uu * m.Mzz +
+            c4 * u * w * m.pxz - uw2 * w * mx - uw2 * u * mz + uu * ww * r;
+    k[18] = (m.A022 - R0 * c19) - c2 * w * m.M021 - c2 * v * m.M012 + ww * m.Myy + vv * m.Mzz +
+            c4 * v * w * m.pyz - vw2 * w * my - vw2 * v * mz + vv * ww * r;
 #pragma unroll
-    for (int i = 0; i < kIn; ++i) x[i] = k[i] * inv;
+    for (int i = 0; i < kIn; ++i) x[i] = k[i] * inv_rho;
 }
 
-// Moments of a cell about its own velocity u = m / rho (closure cells carry no force).
+// Moments of a cell (or two) about its own velocity u = m / rho (closure cells carry no
+// force): density r and the scaled non-equilibrium central moments x.
+template <class T, bool DEV>
+__device__ __forceinline__ void moments_full_t(const T (&f)[19], T& r, T (&x)[kIn]) {
+    const RawT<T> m = raw_moments_t<T, DEV>(f);
+    const T inv = vrcp(m.r);
+    r = m.r;
+    central_moments_t(m, m.mx * inv, m.my * inv, m.mz * inv, inv, x);
+}
+
+// Float forms of the above for one cell.
+using Raw = RawT<F1>;
+
+template <bool DEV>
+__device__ __forceinline__ Raw raw_moments(const float (&f)[19]) {
+    F1 t[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) t[q].x = f[q];
+    return raw_moments_t<F1, DEV>(t);
+}
+
+__device__ __forceinline__ void central_moments(const Raw& m, float u, float v, float w, float rho_n,
+                                                float (&x)[kIn]) {
+    F1 t[kIn];
+    central_moments_t(m, F1{u}, F1{v}, F1{w}, F1{1.0f / rho_n}, t);
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) x[i] = t[i].x;
+}
+
 template <bool DEV>
 __device__ __forceinline__ void moments_full(const float (&f)[19], CMom& c) {
     const Raw m = raw_moments<DEV>(f);
-    const float inv = 1.0f / m.r;
-    c.r = m.r;
-    c.u = m.mx * inv;
-    c.v = m.my * inv;
-    c.w = m.mz * inv;
-    central_moments(m, c.u, c.v, c.w, m.r, c.x);
+    const float inv = 1.0f / m.r.x;
+    c.r = m.r.x;
+    c.u = m.mx.x * inv;
+    c.v = m.my.x * inv;
+    c.w = m.mz.x * inv;
+    central_moments(m, c.u, c.v, c.w, m.r.x, c.x);
 }
 
 // GELU, tanh form (Hendrycks and Gimpel), with the hardware tanh approximation.
