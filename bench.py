@@ -38,6 +38,8 @@ def parse_args():
     p.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
+    p.add_argument("--no-forms", action="store_true",
+                   help="skip the FP16/BF16 and closure measurements of the same workload")
     p.add_argument("--e2e-steps", type=int, default=200)
     p.add_argument("--closure", default=None,
                    help="learned closure on the bulk pass: a parameter file (.npy) or "
@@ -151,6 +153,26 @@ def cpu_baseline(cfg, steps=3):
             "sample": f"{steps} full steps of {cfg.nx}x{cfg.ny}x{cfg.nz} "
                       f"({cfg.n_markers} markers) after 1 warm-up step, "
                       "C/OpenMP restatement of the reference's unfused step"}
+
+
+def measure_form(pkg, torch, device, storage, closure=None, steps=200, warmup=10):
+    """MLUPS of the same workload in another storage form, or with the learned closure on
+    the bulk pass (direct launches, events on the solver stream)."""
+    cfg = pkg.full_case(storage=storage)
+    sim = pkg.Simulation(cfg, device=device)
+    if closure is not None:
+        sim.solver.set_closure(closure)
+    stream = torch.cuda.ExternalStream(sim.solver.stream_handle(), device=torch.device("cuda", device))
+    sim.run(warmup, graph=False)
+    sim.solver.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.run(steps, graph=False)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    sim.close()
+    return {"value": cfg.cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "steps": steps}
 
 
 def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
@@ -337,6 +359,16 @@ def run_gpu(args, rank, world, local):
             "clocks": clk.summary(),
         }
     sim.close()
+    if result is not None and not args.no_forms and args.storage == "f32" and not args.closure:
+        # the other forms of the same workload, measured in this run: FP16/BF16 shifted
+        # storage and FP16 with the trained learned closure on the bulk pass
+        forms = {st: measure_form(pkg, torch, local, st) for st in ("f16", "bf16")}
+        net = os.path.join(ROOT, pkg.__name__, "data", "closure_wing_re2000_eddy.npy")
+        if os.path.exists(net):
+            forms["f16_closure"] = measure_form(pkg, torch, local, "f16", pkg.closure.ClosureNet.load(net))
+        for v in forms.values():
+            v["speedup_vs_f32"] = v["value"] / result["value"]
+        result["forms"] = forms
     if result is not None and not args.no_ensemble:
         result["ensemble"] = {s: measure_ensemble(pkg, torch, local, s) for s in ("f32", "f16")}
     if result is not None and not args.no_cpu_baseline:

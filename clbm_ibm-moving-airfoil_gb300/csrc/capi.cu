@@ -835,10 +835,12 @@ struct clbm_ensemble {
     int storage = 0;
     EnsDesc* d_desc = nullptr;
     long long* d_tile0 = nullptr;
+    long long* d_off = nullptr;  // flat force-box offsets: new box [n + 1], then previous box [n + 1]
+    int flat_grid = 0;           // blocks of the flat band-prepare and box passes
     long long ntiles = 0;
     int bx = 128;            // bulk tile width (cells)
     int grid = 0;            // persistent bulk blocks
-    int max_marker_blocks = 0, max_spread_blocks = 0, box_blocks = 0;
+    int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
     bool local = true, macro_full = true;
     cudaStream_t st = nullptr, st2 = nullptr;
@@ -926,18 +928,21 @@ int ens_step(clbm_ensemble* e) {
     const bool pull = !e->local;
     launch_ens_markers(e->d_desc, e->n, e->max_marker_blocks, e->st);
     CK(cudaEventRecord(e->ev_box, e->st));
-    launch_ens_band_prepare(e->storage, pull, e->d_desc, e->n, e->cur, !e->macro_full,
-                            e->box_blocks, e->st);
+    long long* off_new = e->d_off;
+    long long* off_old = e->d_off + e->n + 1;
+    launch_ens_box_scan(e->d_desc, e->n, off_new, off_old, e->st);
+    launch_ens_band_prepare_flat(e->storage, pull, e->d_desc, e->n, off_new, off_old, e->cur, !e->macro_full,
+                                 e->flat_grid, e->st);
     launch_ens_interp_spread(e->d_desc, e->n, e->max_spread_blocks, e->st);
     launch_ens_finish(e->d_desc, e->n, e->st);
     CK(cudaStreamWaitEvent(e->st2, e->ev_box, 0));
     launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
                     e->grid, e->st2);
     CK(cudaEventRecord(e->ev_bulk, e->st2));
-    launch_ens_box(e->storage, pull, e->d_desc, e->n, e->cur, e->box_blocks, e->st);
+    launch_ens_box_flat(e->storage, pull, e->d_desc, e->n, off_new, e->cur, e->flat_grid, e->st);
     CK(cudaStreamWaitEvent(e->st, e->ev_bulk, 0));
     CK_LAUNCH();
-    e->launches += 6;
+    e->launches += 7;
     e->cur ^= 1;
     e->local = false;
     e->macro_full = false;
@@ -989,9 +994,13 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         if (b) {
             e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + 255) / 256);
             e->max_spread_blocks = std::max(e->max_spread_blocks, (int)(((long long)b->a.n * 32 + 255) / 256));
-            const long long cells = (long long)b->a.max_bx * b->a.max_by * b->a.max_bz;
-            e->box_blocks = std::max(e->box_blocks, (int)std::min<long long>((cells + 255) / 256, 4 * 152));
         }
+    }
+    {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e->flat_grid = 4 * std::max(sms, 1);
     }
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
@@ -1001,7 +1010,8 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         cudaEventCreateWithFlags(&e->ev_bulk, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&e->ev_sync, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&e->d_desc, sizeof(EnsDesc) * n) != cudaSuccess ||
-        cudaMalloc(&e->d_tile0, sizeof(long long) * n) != cudaSuccess)
+        cudaMalloc(&e->d_tile0, sizeof(long long) * n) != cudaSuccess ||
+        cudaMalloc(&e->d_off, sizeof(long long) * 2 * (n + 1)) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream/event/allocation failed"));
     for (clbm_solver* s : e->s) {   // members' queued work (initialisation) comes first
         if (cudaEventRecord(e->ev_sync, s->st) != cudaSuccess ||
@@ -1100,6 +1110,7 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     ens_free_graph(e);
     if (e->d_desc) cudaFree(e->d_desc);
     if (e->d_tile0) cudaFree(e->d_tile0);
+    if (e->d_off) cudaFree(e->d_off);
     cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};
     for (cudaEvent_t ev : evs)
         if (ev) cudaEventDestroy(ev);

@@ -328,18 +328,23 @@ struct EnsDesc {
     int has_ibm;
 };
 
-// One ensemble step is six batched launches: markers (device motion), band prepare,
-// interpolation + spreading, force sums, box pass on `st`; the bulk pass over the flat
-// tile list of all instances (tile width bx, `grid` persistent blocks) on `st2`.
+// One ensemble step is seven batched launches: markers (device motion), the flat offsets
+// of all force boxes, band prepare, interpolation + spreading, force sums, box pass on
+// `st`; the bulk pass over the flat tile list of all instances (tile width bx, `grid`
+// persistent blocks) on `st2`.
 void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st);
-void launch_ens_band_prepare(int storage, bool pull, const EnsDesc* d, int n, int parity,
-                             bool compute_macro, int blocks, cudaStream_t st);
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st);
 void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st);
-void launch_ens_box(int storage, bool pull, const EnsDesc* d, int n, int parity, int blocks,
-                    cudaStream_t st);
 void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,
                      int n, long long ntiles, int parity, int grid, cudaStream_t st);
+// Force-box cells of all members as one flat list (offsets per member, n + 1 each), then
+// band-prepare and box pass over it with `grid` blocks of 256 threads.
+void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st);
+void launch_ens_band_prepare_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new,
+                                  const long long* off_old, int parity, bool compute_macro, int grid,
+                                  cudaStream_t st);
+void launch_ens_box_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new, int parity,
+                         int grid, cudaStream_t st);
 
 // ---- learned closure (closure.cu)
 struct ClosureArgs {

@@ -1,10 +1,12 @@
 // ensemble.cu -- batched kernels that step many independent lattices at once.
 //
 // Each lattice of an ensemble keeps its own buffers; a device array of descriptors
-// (EnsDesc) tells the batched kernels where they are. The IBM kernels index the instance
-// with blockIdx.y (each instance uses as many x-blocks as it needs, the rest leave). The
-// bulk stream-collide pass runs persistent blocks over one flat list of tiles (runs of
-// consecutive cells) of all instances, so lattices of different sizes share the GPU without tail effects;
+// (EnsDesc) tells the batched kernels where they are. The marker, interpolation and
+// force-sum kernels index the instance with blockIdx.y (each instance uses as many x-blocks
+// as it needs, the rest leave); band-prepare and the box pass run one thread per force-box
+// cell over a flat list of all instances' boxes. The bulk stream-collide pass runs
+// persistent blocks over one flat list of tiles (runs of consecutive cells) of all
+// instances, so lattices of different sizes share the GPU without tail effects;
 // the tile width and the number of persistent blocks are picked by timing at creation.
 // Every per-cell and per-marker computation is the single-lattice code (lbm_device.cuh,
 // ibm_device.cuh), so an instance gives the same bits as when it is stepped alone.
@@ -21,16 +23,6 @@ __global__ void __launch_bounds__(kMarkerBlock) kb_markers(const EnsDesc* __rest
     ibm_markers_body<true>(D.a, D.g, MotionF{}, D.m, blockIdx.x);
 }
 
-template <int S, bool PULL>
-__global__ void __launch_bounds__(256) kb_band_prepare(const EnsDesc* __restrict__ d, int parity,
-                                                       bool compute_macro) {
-    const EnsDesc& D = d[blockIdx.y];
-    if (!D.has_ibm) return;
-    band_prepare_body<S, PULL>((const typename Pop<S>::T*)D.f[parity], D.g, D.c, D.a.dev, D.a.fx,
-                               D.a.fy, D.rho, D.ux, D.uy, D.uz, compute_macro, blockIdx.x,
-                               gridDim.x);
-}
-
 __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
     const int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5;
@@ -44,17 +36,98 @@ __global__ void __launch_bounds__(kFinishBlock) kb_finish(const EnsDesc* __restr
     ibm_finish_body(D.a, D.g, blockIdx.x, gridDim.x);
 }
 
+// Force boxes of all members as one flat list: off_new[i] (off_old[i]) is the first flat
+// index of member i's box of this compute_force call (of the previous call), i <= n, so the
+// band-prepare and box passes run one thread per box cell over every member without
+// blocks for members with small boxes. One block; n <= kEnsMaxMembers.
+constexpr int kEnsMaxMembers = 4096;
+
+__global__ void __launch_bounds__(1024) kb_box_scan(const EnsDesc* __restrict__ d, int n,
+                                                    long long* __restrict__ off_new,
+                                                    long long* __restrict__ off_old) {
+    __shared__ int cn[kEnsMaxMembers], co[kEnsMaxMembers];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const EnsDesc& D = d[i];
+        int a = 0, b = 0;
+        if (D.has_ibm) {
+            const long long s = D.a.dev->step + 1;
+            const Band nb = band_from_box(D.a.dev->box[s & 1], D.g.nx, D.g.ny, D.g.nz);
+            const Band ob = band_from_box(D.a.dev->box[(s - 1) & 1], D.g.nx, D.g.ny, D.g.nz);
+            a = nb.ilen * nb.jlen * nb.klen;
+            b = ob.ilen * ob.jlen * ob.klen;
+        }
+        cn[i] = a;
+        co[i] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long sa = 0, sb = 0;
+        for (int i = 0; i < n; ++i) {
+            off_new[i] = sa;
+            off_old[i] = sb;
+            sa += cn[i];
+            sb += co[i];
+        }
+        off_new[n] = sa;
+        off_old[n] = sb;
+    }
+}
+
+// Member of flat index t: the last i with off[i] <= t.
+__device__ __forceinline__ int member_of(const long long* __restrict__ off, int n, long long t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 template <int S, bool PULL>
-__global__ void __launch_bounds__(256) kb_box(const EnsDesc* __restrict__ d, int parity) {
-    const EnsDesc& D = d[blockIdx.y];
-    if (!D.has_ibm) return;
-    ForceArgs fa{};
-    fa.qx = D.a.fx;
-    fa.qy = D.a.fy;
-    fa.dev = D.a.dev;
+__global__ void __launch_bounds__(256) kb_band_prepare_flat(const EnsDesc* __restrict__ d, int n,
+                                                            const long long* __restrict__ off_new,
+                                                            const long long* __restrict__ off_old,
+                                                            int parity, bool compute_macro) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total_old = off_old[n];
+    for (long long t = t0; t < total_old; t += stride) {
+        const int i = member_of(off_old, n, t);
+        const EnsDesc& D = d[i];
+        const long long s = D.a.dev->step + 1;
+        const Band ob = band_from_box(D.a.dev->box[(s - 1) & 1], D.g.nx, D.g.ny, D.g.nz);
+        band_zero_cell(D.g, D.a.fx, D.a.fy, ob, (int)(t - off_old[i]));
+    }
+    if (!compute_macro) return;
+    const long long total_new = off_new[n];
+    for (long long t = t0; t < total_new; t += stride) {
+        const int i = member_of(off_new, n, t);
+        const EnsDesc& D = d[i];
+        const long long s = D.a.dev->step + 1;
+        const Band nb = band_from_box(D.a.dev->box[s & 1], D.g.nx, D.g.ny, D.g.nz);
+        band_macro_cell<S, PULL>((const typename Pop<S>::T*)D.f[parity], D.g, D.c, D.rho, D.ux, D.uy,
+                                 D.uz, nb, (int)(t - off_new[i]));
+    }
+}
+
+template <int S, bool PULL>
+__global__ void __launch_bounds__(256) kb_box_flat(const EnsDesc* __restrict__ d, int n,
+                                                   const long long* __restrict__ off_new, int parity) {
     using T = typename Pop<S>::T;
-    box_pass_body<S, PULL>((const T*)D.f[parity], (T*)D.f[parity ^ 1], D.g, D.c, fa, blockIdx.x,
-                           gridDim.x);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long total = off_new[n];
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int i = member_of(off_new, n, t);
+        const EnsDesc& D = d[i];
+        ForceArgs fa{};
+        fa.qx = D.a.fx;
+        fa.qy = D.a.fy;
+        fa.dev = D.a.dev;
+        const Band b = band_from_box(D.a.dev->box[D.a.dev->cur & 1], D.g.nx, D.g.ny, D.g.nz);
+        box_pass_cell<S, PULL>((const T*)D.f[parity], (T*)D.f[parity ^ 1], D.g, D.c, fa, b,
+                               (int)(t - off_new[i]));
+    }
 }
 
 template <int S, bool PULL, int BX>
@@ -105,15 +178,6 @@ void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     kb_markers<<<dim3(blocks, n), kMarkerBlock, 0, st>>>(d);
 }
 
-void launch_ens_band_prepare(int storage, bool pull, const EnsDesc* d, int n, int parity,
-                             bool compute_macro, int blocks, cudaStream_t st) {
-    const dim3 grid(std::max(blocks, 1), n);
-    CLBM_ENS_STORE(storage, {
-        if (pull) kb_band_prepare<S_, true><<<grid, 256, 0, st>>>(d, parity, compute_macro);
-        else kb_band_prepare<S_, false><<<grid, 256, 0, st>>>(d, parity, compute_macro);
-    });
-}
-
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     if (blocks < 1) return;
     kb_interp_spread<<<dim3(blocks, n), kSpreadBlock, 0, st>>>(d);
@@ -123,12 +187,24 @@ void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st) {
     kb_finish<<<dim3(kFinishBlocks, n), kFinishBlock, 0, st>>>(d);
 }
 
-void launch_ens_box(int storage, bool pull, const EnsDesc* d, int n, int parity, int blocks,
-                    cudaStream_t st) {
-    const dim3 grid(std::max(blocks, 1), n);
+void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st) {
+    kb_box_scan<<<1, 1024, 0, st>>>(d, n, off_new, off_old);
+}
+
+void launch_ens_band_prepare_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new,
+                                  const long long* off_old, int parity, bool compute_macro, int grid,
+                                  cudaStream_t st) {
     CLBM_ENS_STORE(storage, {
-        if (pull) kb_box<S_, true><<<grid, 256, 0, st>>>(d, parity);
-        else kb_box<S_, false><<<grid, 256, 0, st>>>(d, parity);
+        if (pull) kb_band_prepare_flat<S_, true><<<grid, 256, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
+        else kb_band_prepare_flat<S_, false><<<grid, 256, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
+    });
+}
+
+void launch_ens_box_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new, int parity,
+                         int grid, cudaStream_t st) {
+    CLBM_ENS_STORE(storage, {
+        if (pull) kb_box_flat<S_, true><<<grid, 256, 0, st>>>(d, n, off_new, parity);
+        else kb_box_flat<S_, false><<<grid, 256, 0, st>>>(d, n, off_new, parity);
     });
 }
 

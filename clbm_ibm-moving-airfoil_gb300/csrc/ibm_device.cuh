@@ -147,28 +147,12 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     const int cells = b.ilen * b.jlen * b.klen;
     const int stride = nbx * kFinishBlock;
     double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;
-    // four cells per round with their loads issued together: the few blocks of this
-    // kernel are latency-bound, not bandwidth-bound
-    constexpr int kU = 4;
-    for (int t0 = bx * kFinishBlock + threadIdx.x; t0 < cells; t0 += kU * stride) {
-        long long qx[kU], qy[kU];
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-            const int t = t0 + u * stride;
-            qx[u] = qy[u] = 0;
-            if (t < cells) {
-                int x, y, z;
-                box_cell(b, g.ny, g.nz, t, x, y, z);
-                const long long c = ((long long)z * g.ny + y) * g.pitch + x;
-                qx[u] = a.fx[c];
-                qy[u] = a.fy[c];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-            sx += (double)fminf(fmaxf(qforce(qx[u]), -0.05f), 0.05f);
-            sy += (double)fminf(fmaxf(qforce(qy[u]), -0.05f), 0.05f);
-        }
+    for (int t = bx * kFinishBlock + threadIdx.x; t < cells; t += stride) {
+        int x, y, z;
+        box_cell(b, g.ny, g.nz, t, x, y, z);
+        const long long c = ((long long)z * g.ny + y) * g.pitch + x;
+        sx += (double)fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f);
+        sy += (double)fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f);
     }
     for (int t = bx * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
         mx += (double)a.FXk[t];

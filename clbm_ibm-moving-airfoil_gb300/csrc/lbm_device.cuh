@@ -416,6 +416,23 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
     store_raw<S>(fout, g, cell, f);
 }
 
+// Forced stream-collide of box cell t of band b (the box pass, one cell).
+template <int S, bool PULL>
+__device__ __forceinline__ void box_pass_cell(const typename Pop<S>::T* __restrict__ fin,
+                                              typename Pop<S>::T* __restrict__ fout,
+                                              const Grid& g, const Coef& c, const ForceArgs& fa,
+                                              const Band& b, int t) {
+    int x, y, z;
+    box_cell(b, g.ny, g.nz, t, x, y, z);
+    float f[19];
+    gather<S, PULL, true>(fin, g, c, x, y, z, f);
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
+    const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+    collide<true, Pop<S>::kShifted>(f, c, Fx, Fy, 0.0f);
+    store_raw<S>(fout, g, cell, f);
+}
+
 // Forced stream-collide of the cells of the IBM force box; block bx of nbx (256 threads)
 // takes cells bx * 256 + threadIdx.x, stepping by nbx * 256.
 template <int S, bool PULL>
@@ -425,17 +442,42 @@ __device__ __forceinline__ void box_pass_body(const typename Pop<S>::T* __restri
                                               int bx, int nbx) {
     const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
     const int cells = b.ilen * b.jlen * b.klen;
-    for (int t = bx * blockDim.x + threadIdx.x; t < cells; t += nbx * blockDim.x) {
-        int x, y, z;
-        box_cell(b, g.ny, g.nz, t, x, y, z);
-        float f[19];
-        gather<S, PULL, true>(fin, g, c, x, y, z, f);
-        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-        const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
-        const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
-        collide<true, Pop<S>::kShifted>(f, c, Fx, Fy, 0.0f);
-        store_raw<S>(fout, g, cell, f);
+    for (int t = bx * blockDim.x + threadIdx.x; t < cells; t += nbx * blockDim.x)
+        box_pass_cell<S, PULL>(fin, fout, g, c, fa, b, t);
+}
+
+// The two pieces of band-prepare for one cell: zero the force of box cell t of band ob,
+// and _macro_post (clbm_moving.py:305-321) of box cell t of band nb.
+__device__ __forceinline__ void band_zero_cell(const Grid& g, long long* fx, long long* fy,
+                                               const Band& ob, int t) {
+    int x, y, z;
+    box_cell(ob, g.ny, g.nz, t, x, y, z);
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    fx[cell] = 0;
+    fy[cell] = 0;
+}
+
+template <int S, bool PULL>
+__device__ __forceinline__ void band_macro_cell(const typename Pop<S>::T* __restrict__ fin,
+                                                const Grid& g, const Coef& c, float* rho, float* ux,
+                                                float* uy, float* uz, const Band& nb, int t) {
+    int x, y, z;
+    box_cell(nb, g.ny, g.nz, t, x, y, z);
+    float f[19];
+    gather<S, PULL>(fin, g, c, x, y, z, f);
+    float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        r += f[q];
+        mx += (float)ex(q) * f[q];
+        my += (float)ey(q) * f[q];
+        mz += (float)ez(q) * f[q];
     }
+    const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    rho[cell] = r;
+    ux[cell] = mx / r;
+    uy[cell] = my / r;
+    uz[cell] = mz / r;
 }
 
 // Zero the force box of the previous compute_force call (_zero_forces,
@@ -453,34 +495,11 @@ __device__ __forceinline__ void band_prepare_body(const typename Pop<S>::T* __re
     const Band ob = band_from_box(dev->box[(s - 1) & 1], g.nx, g.ny, g.nz);
     const int stride = nbx * blockDim.x;
     const int ocells = ob.ilen * ob.jlen * ob.klen;
-    for (int t = bx * blockDim.x + threadIdx.x; t < ocells; t += stride) {
-        int x, y, z;
-        box_cell(ob, g.ny, g.nz, t, x, y, z);
-        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-        fx[cell] = 0;
-        fy[cell] = 0;
-    }
+    for (int t = bx * blockDim.x + threadIdx.x; t < ocells; t += stride) band_zero_cell(g, fx, fy, ob, t);
     if (!compute_macro) return;
     const int ncells = nb.ilen * nb.jlen * nb.klen;
-    for (int t = bx * blockDim.x + threadIdx.x; t < ncells; t += stride) {
-        int x, y, z;
-        box_cell(nb, g.ny, g.nz, t, x, y, z);
-        float f[19];
-        gather<S, PULL>(fin, g, c, x, y, z, f);
-        float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
-#pragma unroll
-        for (int q = 0; q < 19; ++q) {
-            r += f[q];
-            mx += (float)ex(q) * f[q];
-            my += (float)ey(q) * f[q];
-            mz += (float)ez(q) * f[q];
-        }
-        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-        rho[cell] = r;
-        ux[cell] = mx / r;
-        uy[cell] = my / r;
-        uz[cell] = mz / r;
-    }
+    for (int t = bx * blockDim.x + threadIdx.x; t < ncells; t += stride)
+        band_macro_cell<S, PULL>(fin, g, c, rho, ux, uy, uz, nb, t);
 }
 
 }  // namespace clbm
