@@ -872,7 +872,9 @@ int ens_upload(clbm_ensemble* e, int bx) {
         D.cells = s->g.nx * s->g.ny * s->g.nz;
         D.tile0 = tiles;
         t0[i] = tiles;
-        tiles += (D.cells + bx - 1) / bx;
+        // the 16-bit forms take two cells per thread
+        const int tile_cells = e->storage == CLBM_STORE_F32 ? bx : 2 * bx;
+        tiles += (D.cells + tile_cells - 1) / tile_cells;
     }
     CK(cudaMemcpyAsync(e->d_desc, h.data(), sizeof(EnsDesc) * e->n, cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->d_tile0, t0.data(), sizeof(long long) * e->n, cudaMemcpyHostToDevice, e->st));

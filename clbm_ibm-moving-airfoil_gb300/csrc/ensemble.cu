@@ -130,11 +130,16 @@ __global__ void __launch_bounds__(256) kb_box_flat(const EnsDesc* __restrict__ d
     }
 }
 
+// Bulk pass over the flat tile list. Float32: one cell per thread, tiles of BX cells.
+// 16-bit shifted forms: two cells per thread (t and BX + t of a tile of 2 BX cells), the
+// collision of both in packed f32x2 arithmetic (the same bits as the one-cell form).
 template <int S, bool PULL, int BX>
 __global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
                                               const long long* __restrict__ tile0, int n,
                                               long long ntiles, int parity) {
     using T = typename Pop<S>::T;
+    constexpr bool DEV = Pop<S>::kShifted;
+    constexpr int K = DEV ? 2 : 1;  // cells per thread
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         // instance of tile t: the last i with tile0[i] <= t
         int lo = 0, hi = n - 1;
@@ -145,24 +150,38 @@ __global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
         }
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
-        // tiles run over the instance's cells in x-fastest order across row ends, so no
-        // lane idles at the end of a row that is not a multiple of the tile width
-        const unsigned i = (unsigned)(t - D.tile0) * BX + threadIdx.x;
-        if (i >= (unsigned)D.cells) continue;
-        const unsigned row = i / (unsigned)g.nx;
-        const int x = (int)(i - row * (unsigned)g.nx);
-        const int y = (int)(row % (unsigned)g.ny), z = (int)(row / (unsigned)g.ny);
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
-        if (D.has_ibm) {
-            ForceArgs fa{};
-            fa.qx = D.a.fx;
-            fa.qy = D.a.fy;
-            fa.dev = D.a.dev;
-            stream_collide_cell<S, PULL, kForceSkipBand>(fin, fout, g, D.c, fa, x, y, z);
-        } else {
-            stream_collide_cell<S, PULL, kForceNone>(fin, fout, g, D.c, ForceArgs{}, x, y, z);
+        Band band{};
+        if (D.has_ibm) band = band_from_box(D.a.dev->box[D.a.dev->cur & 1], g.nx, g.ny, g.nz);
+        // tiles run over the instance's cells in x-fastest order across row ends, so no
+        // lane idles at the end of a row that is not a multiple of the tile width
+        int x[K], y[K], z[K];
+        bool use[K];
+        float h[K][19];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const unsigned i = (unsigned)(t - D.tile0) * (BX * K) + k * BX + threadIdx.x;
+            use[k] = i < (unsigned)D.cells;
+            x[k] = y[k] = z[k] = 0;
+            if (use[k]) {
+                const unsigned row = i / (unsigned)g.nx;
+                x[k] = (int)(i - row * (unsigned)g.nx);
+                y[k] = (int)(row % (unsigned)g.ny);
+                z[k] = (int)(row / (unsigned)g.ny);
+                if (D.has_ibm && in_band(band, x[k], y[k], z[k], g.ny, g.nz)) use[k] = false;
+            }
+            if (use[k]) gather<S, PULL, true>(fin, g, D.c, x[k], y[k], z[k], h[k]);
         }
+        if (K == 2) {
+            collide_pair<DEV>(h[0], h[K - 1], D.c, use[0], use[K - 1], false, false, 0.f, 0.f, 0.f,
+                              0.f, 0.f, 0.f);
+        } else if (use[0]) {
+            collide<false, DEV>(h[0], D.c, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (use[k]) store_raw<S>(fout, g, ((long long)z[k] * g.ny + y[k]) * g.pitch + x[k], h[k]);
     }
 }
 

@@ -380,6 +380,29 @@ __device__ __forceinline__ void collide2(float (&f0)[19], float (&f1)[19], const
     }
 }
 
+// Collision of the two cells of a thread. Shifted 16-bit forms (DEV): packed (f32x2) when
+// both are computed, a zero force on the unforced lane when only one is forced (same
+// values as the unforced path). Float32: one scalar call per cell.
+template <bool DEV>
+__device__ __forceinline__ void collide_pair(float (&h0)[19], float (&h1)[19], const Coef& c,
+                                             bool use0, bool use1, bool frc0, bool frc1,
+                                             float F0x, float F0y, float F0z, float F1x,
+                                             float F1y, float F1z) {
+    if (DEV && use0 && use1) {
+        if (frc0 || frc1) collide2<true, DEV>(h0, h1, c, F0x, F0y, F0z, F1x, F1y, F1z);
+        else collide2<false, DEV>(h0, h1, c, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    if (use0) {
+        if (frc0) collide<true, DEV>(h0, c, F0x, F0y, F0z);
+        else collide<false, DEV>(h0, c, 0.f, 0.f, 0.f);
+    }
+    if (use1) {
+        if (frc1) collide<true, DEV>(h1, c, F1x, F1y, F1z);
+        else collide<false, DEV>(h1, c, 0.f, 0.f, 0.f);
+    }
+}
+
 // One cell of the full-grid pass: gather, force (per FMODE), collide, store.
 template <int S, bool PULL, int FMODE>
 __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __restrict__ fin,

@@ -41,29 +41,6 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
     box_pass_body<S, PULL>(fin, fout, g, c, fa, blockIdx.x, gridDim.x);
 }
 
-// Collision of the two cells of a thread. Shifted 16-bit forms (DEV): packed (f32x2) when
-// both are computed, a zero force on the unforced lane when only one is forced (same
-// values as the unforced path). Float32: one scalar call per cell.
-template <bool DEV>
-__device__ __forceinline__ void collide_pair(float (&h0)[19], float (&h1)[19], const Coef& c,
-                                             bool use0, bool use1, bool frc0, bool frc1,
-                                             float F0x, float F0y, float F0z, float F1x,
-                                             float F1y, float F1z) {
-    if (DEV && use0 && use1) {
-        if (frc0 || frc1) collide2<true, DEV>(h0, h1, c, F0x, F0y, F0z, F1x, F1y, F1z);
-        else collide2<false, DEV>(h0, h1, c, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-        return;
-    }
-    if (use0) {
-        if (frc0) collide<true, DEV>(h0, c, F0x, F0y, F0z);
-        else collide<false, DEV>(h0, c, 0.f, 0.f, 0.f);
-    }
-    if (use1) {
-        if (frc1) collide<true, DEV>(h1, c, F1x, F1y, F1z);
-        else collide<false, DEV>(h1, c, 0.f, 0.f, 0.f);
-    }
-}
-
 // ------------------------------------------------------------------ 16-bit pair kernel
 // Shifted 16-bit storage moves half the bytes of float32, so the one-cell kernel becomes
 // issue-bound. This variant gives each thread two neighbouring cells (x0, x0 + 1), x0 even:
