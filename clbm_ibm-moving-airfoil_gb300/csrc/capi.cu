@@ -17,6 +17,9 @@ constexpr int kHistCap = 1 << 16;
 // kernels one graph-captured step launches: markers, band-prepare, interp/spread, finish,
 // bulk stream-collide, box stream-collide
 constexpr int kKernelsPerIbmStep = 6;
+// steps per captured graph (even, so buffer and box-slot parities repeat); within a graph
+// each step's marker kernel overlaps the previous step's bulk pass
+constexpr int kGraphSteps = 8;
 
 }  // namespace
 
@@ -56,6 +59,15 @@ int record_event(clbm_solver* s, cudaStream_t st) {
     return CLBM_OK;
 }
 
+// Make the main stream wait for a bulk pass that a step left running on the second stream.
+int join_bulk(clbm_solver* s) {
+    if (s->bulk_pending) {
+        CK(cudaStreamWaitEvent(s->st, s->ev_bulk, 0));
+        s->bulk_pending = false;
+    }
+    return CLBM_OK;
+}
+
 // One fused stream-collide launch on stream `st`, bracketed by timing events if profiling.
 int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bool box,
              long long box_cells) {
@@ -86,6 +98,7 @@ int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bo
 }
 
 int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ibm) {
+    if (int rc = join_bulk(s)) return rc;
     if (fmode != kForceBand) {
         if (int rc = sc_timed(s, fmode, fa, s->st, false, 0)) return rc;
     } else {
@@ -104,7 +117,7 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         CK(cudaEventRecord(s->ev_bulk, s->st2));
         const long long box_cells = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
         if (int rc = sc_timed(s, kForceBand, fa, s->st, true, box_cells)) return rc;
-        CK(cudaStreamWaitEvent(s->st, s->ev_bulk, 0));
+        s->bulk_pending = true;  // joined by the next call (after the next marker kernel)
     }
     s->cur = 1 - s->cur;
     s->local = false;
@@ -115,8 +128,10 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
 
 int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motion& m) {
     clbm_solver* s = ibm->s;
+    // the marker kernel needs only the motion: it runs beside the previous step's bulk pass
     launch_ibm_markers(ibm->a, s->g, devm, mf, m, s->st);
     CK(cudaEventRecord(ibm->ev_box, s->st));
+    if (int rc = join_bulk(s)) return rc;
     ibm->box_version = s->version;
     launch_band_prepare(s->cfg.storage, !s->local, s->f[s->cur], s->g, s->c, ibm->a.dev,
                         ibm->a.fx, ibm->a.fy, s->rho, s->ux, s->uy, s->uz, ibm->a.max_bx,
@@ -181,6 +196,7 @@ void free_graph(clbm_solver* s) {
     s->gexec = nullptr;
     s->g_ibm = nullptr;
     s->g_cur = -1;
+    s->g_slot = -1;
 }
 
 }  // namespace
@@ -288,6 +304,7 @@ int clbm_step(clbm_solver* s, const clbm_ibm* ibm) {
         fa.qx = ibm->a.fx;
         fa.qy = ibm->a.fy;
         fa.dev = ibm->a.dev;
+        fa.slot = (int)(ibm->calls & 1);  // box of the last compute_force call
     }
     return step_impl(s, ibm ? kForceBand : kForceNone, fa, ibm);
 }
@@ -342,6 +359,7 @@ static int materialize(clbm_solver* s, bool with_stats) {
 
 int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_read_macro: null solver");
+    if (int rc = join_bulk(s)) return rc;
     int rc = materialize(s, false);
     if (rc) return rc;
     const size_t n = cells(s);
@@ -364,6 +382,7 @@ int clbm_read_macro(clbm_solver* s, float* rho, float* ux, float* uy, float* uz)
 int clbm_read_vorticity_slice(clbm_solver* s, int32_t z, float* out) {
     if (!s || !out || z < 0 || z >= s->g.nz)
         return fail(CLBM_ERR_ARG, "clbm_read_vorticity_slice: invalid argument");
+    if (int rc = join_bulk(s)) return rc;
     int rc = materialize(s, false);
     if (rc) return rc;
     const size_t n = (size_t)s->g.nx * s->g.ny;
@@ -379,6 +398,7 @@ int clbm_read_vorticity_slice(clbm_solver* s, int32_t z, float* out) {
 
 int clbm_read_populations(clbm_solver* s, float* f_host) {
     if (!s || !f_host) return fail(CLBM_ERR_ARG, "clbm_read_populations: null argument");
+    if (int rc = join_bulk(s)) return rc;
     const size_t n = cells(s) * 19;
     int rc = ensure_stage(s, n * sizeof(float));
     if (rc) return rc;
@@ -393,6 +413,7 @@ int clbm_read_populations(clbm_solver* s, float* f_host) {
 
 int clbm_write_populations(clbm_solver* s, const float* f_host) {
     if (!s || !f_host) return fail(CLBM_ERR_ARG, "clbm_write_populations: null argument");
+    if (int rc = join_bulk(s)) return rc;
     const size_t n = cells(s) * 19;
     int rc = ensure_stage(s, n * sizeof(float));
     if (rc) return rc;
@@ -418,6 +439,7 @@ static double from_ordered(unsigned long long v) {
 int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_max,
                double* u_max, int64_t* nonfinite) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_check: null solver");
+    if (int rc = join_bulk(s)) return rc;
     int rc = materialize(s, true);
     if (rc) return rc;
     unsigned long long h[4];
@@ -547,6 +569,7 @@ int ibm_compute_force_motion(clbm_ibm* ibm, const clbm_motion* m) {
 int ibm_read_forces(const clbm_ibm* ibm, float* fx, float* fy, float* fz) {
     if (int rc = check_bound(ibm, "ibm_read_forces")) return rc;
     clbm_solver* s = ibm->s;
+    if (int rc = join_bulk(s)) return rc;
     const size_t n = cells(s);
     int rc = ensure_stage(s, 2 * n * sizeof(float));
     if (rc) return rc;
@@ -637,18 +660,21 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
         if (rc) return rc;
         ++done;
     }
-    if (graph && nsteps - done >= 2) {
-        const bool same = s->gexec && s->g_ibm == ibm && s->g_cur == s->cur &&
+    if (graph && nsteps - done >= kGraphSteps) {
+        const int slot = ibm ? (int)(ibm->calls & 1) : 0;
+        const bool same = s->gexec && s->g_ibm == ibm && s->g_cur == s->cur && s->g_slot == slot &&
                           (!ibm || std::memcmp(&s->g_m, m, sizeof(clbm_motion)) == 0);
         if (!same) {
             free_graph(s);
             const int cur0 = s->cur;
             const long long launches0 = s->launches;
             const long long calls0 = ibm ? ibm->calls : 0;
+            if (int rc = join_bulk(s)) return rc;  // no dependency on work outside the capture
             CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
             capturing = true;
-            int rc = one();
-            if (!rc) rc = one();
+            int rc = CLBM_OK;
+            for (int k = 0; k < kGraphSteps && !rc; ++k) rc = one();
+            if (!rc) rc = join_bulk(s);  // all captured work rejoins the capture stream
             capturing = false;
             cudaGraph_t graph_obj = nullptr;
             cudaError_t e = cudaStreamEndCapture(s->st, &graph_obj);
@@ -662,21 +688,23 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
             }
             if (e != cudaSuccess)
                 return fail(CLBM_ERR_CUDA, "clbm_run: graph capture failed: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&s->gexec, graph_obj, 0);
+            // keep the stream priorities of the captured kernels (IBM chain over bulk pass)
+            e = cudaGraphInstantiateWithFlags(&s->gexec, graph_obj, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(graph_obj);
             if (e != cudaSuccess)
                 return fail(CLBM_ERR_CUDA, "clbm_run: graph instantiate failed: %s", cudaGetErrorString(e));
             s->g_ibm = ibm;
             if (ibm) s->g_m = *m;
             s->g_cur = cur0;
+            s->g_slot = slot;
         }
         const int per = ibm ? (ibm->a.n > 0 ? kKernelsPerIbmStep : kKernelsPerIbmStep - 2) : 1;
-        while (nsteps - done >= 2) {
+        while (nsteps - done >= kGraphSteps) {
             CK(cudaGraphLaunch(s->gexec, s->st));
-            done += 2;
-            s->version += 2;
-            s->launches += 2 * per;
-            if (ibm) ibm->calls += 2;
+            done += kGraphSteps;
+            s->version += kGraphSteps;
+            s->launches += kGraphSteps * per;
+            if (ibm) ibm->calls += kGraphSteps;
         }
         s->local = false;
         s->macro_full = false;
@@ -686,11 +714,12 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
         if (rc) return rc;
         ++done;
     }
-    return CLBM_OK;
+    return join_bulk(s);  // the run's work is complete on the solver stream
 }
 
 int clbm_synchronize(clbm_solver* s) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_synchronize: null solver");
+    if (int rc = join_bulk(s)) return rc;
     unsigned int status = 0;
     CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
@@ -703,6 +732,7 @@ int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit) {
     // at least 1024 polls, so every block's copies have landed before it gives up and exits
     if (!s || spin_limit < 1024)
         return fail(CLBM_ERR_ARG, "clbm_selftest_wait_timeout: spin_limit must be >= 1024");
+    if (int rc = join_bulk(s)) return rc;
     CK(cudaStreamSynchronize(s->st));
     Grid g = s->g;
     g.spin_limit = spin_limit;
@@ -724,6 +754,8 @@ int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit) {
 
 int clbm_stream(const clbm_solver* s, void** out) {
     if (!s || !out) return fail(CLBM_ERR_ARG, "clbm_stream: null argument");
+    // work queued so far is complete on the returned stream
+    if (int rc = join_bulk(const_cast<clbm_solver*>(s))) return rc;
     *out = (void*)s->st;
     return CLBM_OK;
 }
@@ -739,6 +771,7 @@ int clbm_profile_enable(clbm_solver* s, int32_t on) {
 int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
                       int64_t* total_launches) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_profile_read: null solver");
+    if (int rc = join_bulk(s)) return rc;
     CK(cudaStreamSynchronize(s->st));
     double ms = 0.0;
     for (size_t i = 0; i + 1 < s->ev_used; i += 2) {
@@ -755,6 +788,7 @@ int clbm_profile_read(clbm_solver* s, double* fused_ms, int64_t* fused_launches,
 int clbm_profile_read_split(clbm_solver* s, double* bulk_ms, int64_t* bulk_launches,
                             double* box_ms, int64_t* box_launches) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_profile_read_split: null solver");
+    if (int rc = join_bulk(s)) return rc;
     CK(cudaStreamSynchronize(s->st));
     double ms[2] = {0.0, 0.0};
     int64_t n[2] = {0, 0};
@@ -784,6 +818,7 @@ int clbm_device_bytes(const clbm_solver* s, int64_t* out) {
 
 int clbm_closure_set(clbm_solver* s, const float* params) {
     if (!s) return fail(CLBM_ERR_ARG, "clbm_closure_set: null solver");
+    if (int rc = join_bulk(s)) return rc;
     CK(cudaStreamSynchronize(s->st));
     CK(cudaStreamSynchronize(s->st2));
     free_graph(s);  // the captured bulk-pass kernel changes
@@ -1016,7 +1051,8 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         cudaMalloc(&e->d_off, sizeof(long long) * 2 * (n + 1)) != cudaSuccess)
         return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream/event/allocation failed"));
     for (clbm_solver* s : e->s) {   // members' queued work (initialisation) comes first
-        if (cudaEventRecord(e->ev_sync, s->st) != cudaSuccess ||
+        if (join_bulk(s) != CLBM_OK ||
+            cudaEventRecord(e->ev_sync, s->st) != cudaSuccess ||
             cudaStreamWaitEvent(e->st, e->ev_sync, 0) != cudaSuccess)
             return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream ordering failed"));
     }
@@ -1058,7 +1094,7 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
             }
             if (err != cudaSuccess)
                 return fail(CLBM_ERR_CUDA, "clbm_ensemble_run: capture failed: %s", cudaGetErrorString(err));
-            err = cudaGraphInstantiate(&e->gexec, g, 0);
+            err = cudaGraphInstantiateWithFlags(&e->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (err != cudaSuccess)
                 return fail(CLBM_ERR_CUDA, "clbm_ensemble_run: instantiate failed: %s", cudaGetErrorString(err));

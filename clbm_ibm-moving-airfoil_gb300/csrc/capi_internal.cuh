@@ -56,6 +56,9 @@ struct clbm_solver {
     cudaStream_t st = nullptr;     // high priority: IBM chain, box pass, transfers
     cudaStream_t st2 = nullptr;    // low priority: bulk stream-collide of IBM steps
     cudaEvent_t ev_bulk = nullptr; // end of the bulk pass (joined into st)
+    bool bulk_pending = false;     // the last bulk pass is not yet joined into st: the next
+                                   // compute_force's marker kernel runs beside it, and every
+                                   // other call joins it first
     cudaEvent_t ev_fork = nullptr; // fork point of a bulk pass without a fresh box event
     long long version = 0;         // bumped whenever f[cur] changes
     long long launches = 0;
@@ -69,6 +72,7 @@ struct clbm_solver {
     size_t ev_used = 0;
     // cached two-step graph of the time loop
     cudaGraphExec_t gexec = nullptr;
+    int g_slot = -1;               // box slot parity the cached graph was captured at
     const clbm_ibm* g_ibm = nullptr;
     clbm_motion g_m{};
     int g_cur = -1;

@@ -237,7 +237,10 @@ struct ForceArgs {
     const float* fz;
     const long long* qx;   // band mode: fixed-point IBM fields, padded layout
     const long long* qy;
-    const IbmDev* dev;     // band mode: box of the last compute_force
+    const IbmDev* dev;     // band mode: boxes of the compute_force calls
+    int slot;              // band mode: box slot of the call this step applies (call index & 1),
+                           // passed by the host so the next call's marker kernel may run
+                           // while this step's bulk pass still reads it
 };
 
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);

@@ -411,7 +411,7 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
                                                     const ForceArgs& fa, int x, int y, int z) {
     if (FMODE == kForceSkipBand) {
         // bulk pass of an IBM step: the cells of the force box are done by the box pass
-        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
         if (in_band(b, x, y, z, g.ny, g.nz)) return;
     }
     // shifted storage: the collision works on the deviations (no per-population shift)
@@ -425,7 +425,7 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
         const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
         collide<true, DEV>(f, c, fa.fx[cell], fa.fy[cell], Fz);
     } else {
-        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
         if (in_band(b, x, y, z, g.ny, g.nz)) {
             // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
             // fz is always zero there.
@@ -463,7 +463,7 @@ __device__ __forceinline__ void box_pass_body(const typename Pop<S>::T* __restri
                                               typename Pop<S>::T* __restrict__ fout,
                                               const Grid& g, const Coef& c, const ForceArgs& fa,
                                               int bx, int nbx) {
-    const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+    const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
     const int cells = b.ilen * b.jlen * b.klen;
     for (int t = bx * blockDim.x + threadIdx.x; t < cells; t += nbx * blockDim.x)
         box_pass_cell<S, PULL>(fin, fout, g, c, fa, b, t);

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair
     const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
     bool in0 = false, in1 = false;
     if (FMODE == kForceSkipBand || FMODE == kForceBand) {
-        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
         in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
         in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
     }
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) k_stream_collide_tma(const typename Stg<S
     const bool act1 = x0 + 1 < g.nx;
     bool in0 = false, in1 = false;
     if (FMODE == kForceSkipBand || FMODE == kForceBand) {
-        const Band b = band_from_box(fa.dev->box[fa.dev->cur & 1], g.nx, g.ny, g.nz);
+        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
         in0 = in_band(b, x0, y, z, g.ny, g.nz);
         in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
     }

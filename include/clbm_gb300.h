@@ -139,8 +139,9 @@ int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t nx, int32_t
                            double* out);
 
 /* The driver loop of main_moving.py:116-122 for nsteps steps: per step
- * ibm_compute_force_motion then clbm_step, captured once into a CUDA graph and replayed
- * when use_graph != 0. ibm may be NULL (zero force). */
+ * ibm_compute_force_motion then clbm_step. use_graph != 0: eight steps are captured once
+ * into a CUDA graph (motion law on the device) and replayed; a remainder below eight runs as
+ * direct launches (motion law on the host). ibm may be NULL (zero force). */
 int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps,
              int32_t use_graph);
 
@@ -176,7 +177,11 @@ int clbm_synchronize(clbm_solver* s);
 int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit);
 
 /* The solver's CUDA stream (cudaStream_t), for callers that record events or order their
- * own work against the solver. The stream stays owned by the solver. */
+ * own work against the solver. The stream stays owned by the solver. An IBM step runs its
+ * bulk pass on a second stream and leaves it running there, so the next compute_force's
+ * marker kernel overlaps it; every later call on the solver or its IBMs, the end of
+ * clbm_run, clbm_synchronize and this call join it into the solver stream first, so work
+ * queued before this call is complete on the returned stream. */
 int clbm_stream(const clbm_solver* s, void** out);
 
 /* Kernel timing for roofline reporting: while enabled, each fused stream-collide launch is
