@@ -171,8 +171,10 @@ def measure_form(pkg, torch, device, storage, closure=None, steps=200, warmup=10
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
+    variant = sim.solver.kernel_variant()
     sim.close()
-    return {"value": cfg.cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "steps": steps}
+    return {"value": cfg.cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps, "steps": steps,
+            "variant": variant["variant"], "variant_autotune_us": variant["us_per_launch"]}
 
 
 def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):

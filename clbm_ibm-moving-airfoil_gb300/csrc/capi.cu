@@ -107,6 +107,17 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         // the low-priority stream while the IBM chain still computes the forces; the box
         // pass follows the IBM chain on the main stream; the main stream then joins the
         // bulk pass. The fork is valid only while the state is the one compute_force saw.
+        static const int serial = knob("CLBM_SERIAL", 0);
+        if (serial) {
+            if (int rc = sc_timed(s, kForceSkipBand, fa, s->st, false, 0)) return rc;
+            const long long bc = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
+            if (int rc = sc_timed(s, kForceBand, fa, s->st, true, bc)) return rc;
+            s->cur = 1 - s->cur;
+            s->local = false;
+            s->macro_full = false;
+            s->version += 1;
+            return CLBM_OK;
+        }
         if (ibm->box_version == s->version) {
             CK(cudaStreamWaitEvent(s->st2, ibm->ev_box, 0));
         } else {
@@ -844,7 +855,7 @@ int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_la
     if (!s || !variant) return fail(CLBM_ERR_ARG, "clbm_kernel_variant: invalid argument");
     *variant = s->variant;
     if (ms_per_launch)
-        for (int v = 0; v < 3; ++v) ms_per_launch[v] = s->variant_ms[v];
+        for (int v = 0; v < kVariants; ++v) ms_per_launch[v] = s->variant_ms[v];
     return CLBM_OK;
 }
 

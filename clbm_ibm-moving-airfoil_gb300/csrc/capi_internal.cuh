@@ -62,8 +62,8 @@ struct clbm_solver {
     cudaEvent_t ev_fork = nullptr; // fork point of a bulk pass without a fresh box event
     long long version = 0;         // bumped whenever f[cur] changes
     long long launches = 0;
-    int variant = kVariantStaged;  // full-grid stream-collide kernel (chosen at create)
-    float variant_ms[3] = {0.f, 0.f, 0.f};  // autotune time per launch of each variant (0: not timed)
+    int variant = clbm::kVariantStaged;  // full-grid stream-collide kernel (chosen at create)
+    float variant_ms[clbm::kVariants] = {};  // autotune time per launch of each variant (0: not timed)
     unsigned int* status = nullptr;
     // profiling of the fused kernel
     bool prof = false;

@@ -106,7 +106,11 @@ struct IbmDev {
                            // force-sum kernel has advanced `step` still finds the right box
     int box[2][6];         // slot (call index & 1): imin, -imax, jmin, -jmax, kmin, -kmax
     unsigned int ticket;   // last-block detection of the force-sum kernel
-    int pad;
+    unsigned int mticket;  // last-block detection of the marker kernel
+    // slot: the Band of box[slot] (i0, ilen, j0, jlen, k0, klen, 0, 0), written by the last
+    // block of the marker kernel once the box is complete, so the passes that test cells
+    // against the box read six integers instead of converting the box in every thread
+    alignas(16) int band[2][8];
 };
 
 // Box in lattice coordinates with periodic y/z: x in [i0, i0 + ilen), y in
@@ -116,6 +120,8 @@ struct Band {
 };
 
 __host__ __device__ inline int pmod(int a, int m) {
+    if (a >= 0 && a < m) return a;          // the usual cases need no division
+    if (a < 0 && a >= -m) return a + m;
     int r = a % m;
     return r < 0 ? r + m : r;
 }
@@ -143,6 +149,12 @@ __device__ inline bool in_band(const Band& b, int x, int y, int z, int ny, int n
     int oy = y - b.j0; if (oy < 0) oy += ny;
     int oz = z - b.k0; if (oz < 0) oz += nz;
     return (unsigned)(x - b.i0) < (unsigned)b.ilen && oy < b.jlen && oz < b.klen;
+}
+
+__device__ __forceinline__ Band load_band(const IbmDev* dev, int slot) {
+    const int4 a = *reinterpret_cast<const int4*>(dev->band[slot]);
+    const int2 b = *reinterpret_cast<const int2*>(dev->band[slot] + 4);
+    return Band{a.x, a.y, a.z, a.w, b.x, b.y};
 }
 
 // Cell t (0 <= t < ilen * jlen * klen) of a band box, x fastest.
@@ -243,12 +255,14 @@ struct ForceArgs {
                            // while this step's bulk pass still reads it
 };
 
+int knob(const char* name, int def);  // integer tuning parameter from the environment
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
 // Stream-collide kernel variants for the full-grid pass:
 //   kVariantCell    one cell per thread, direct loads (float32 parity kernel)
 //   kVariantPair    two cells per thread, half2 loads, warp-shuffle x shifts (16-bit only)
 //   kVariantStaged  two cells per thread, rows staged in shared memory by bulk TMA copies
 enum Variant { kVariantCell = 0, kVariantPair = 1, kVariantStaged = 2 };
+constexpr int kVariants = 3;
 void launch_stream_collide(int storage, bool pull, int fmode, int variant, const void* fin,
                            void* fout, const Grid& g, const Coef& c, const ForceArgs& fa,
                            cudaStream_t st);

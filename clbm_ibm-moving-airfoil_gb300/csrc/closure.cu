@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
     const float nu = (1.0f / (1.0f - c.one_m_sv) - 0.5f) * (1.0f / 3.0f);  // solver viscosity
     uint32_t phase = 0;
     bool ok = true;
-    const Band band = (FMODE == kForceSkipBand) ? band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz)
+    const Band band = (FMODE == kForceSkipBand) ? load_band(fa.dev, fa.slot)
                                                 : Band{};
     for (long long tile = blockIdx.x; tile < ca.tiles; tile += gridDim.x) {
         const long long i = tile * 128 + tid;

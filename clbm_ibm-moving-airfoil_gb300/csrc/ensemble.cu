@@ -51,8 +51,8 @@ __global__ void __launch_bounds__(1024) kb_box_scan(const EnsDesc* __restrict__ 
         int a = 0, b = 0;
         if (D.has_ibm) {
             const long long s = D.a.dev->step + 1;
-            const Band nb = band_from_box(D.a.dev->box[s & 1], D.g.nx, D.g.ny, D.g.nz);
-            const Band ob = band_from_box(D.a.dev->box[(s - 1) & 1], D.g.nx, D.g.ny, D.g.nz);
+            const Band nb = load_band(D.a.dev, (int)(s & 1));
+            const Band ob = load_band(D.a.dev, (int)((s - 1) & 1));
             a = nb.ilen * nb.jlen * nb.klen;
             b = ob.ilen * ob.jlen * ob.klen;
         }
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) kb_band_prepare_flat(const EnsDesc* __res
         const int i = member_of(off_old, n, t);
         const EnsDesc& D = d[i];
         const long long s = D.a.dev->step + 1;
-        const Band ob = band_from_box(D.a.dev->box[(s - 1) & 1], D.g.nx, D.g.ny, D.g.nz);
+        const Band ob = load_band(D.a.dev, (int)((s - 1) & 1));
         band_zero_cell(D.g, D.a.fx, D.a.fy, ob, (int)(t - off_old[i]));
     }
     if (!compute_macro) return;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) kb_band_prepare_flat(const EnsDesc* __res
         const int i = member_of(off_new, n, t);
         const EnsDesc& D = d[i];
         const long long s = D.a.dev->step + 1;
-        const Band nb = band_from_box(D.a.dev->box[s & 1], D.g.nx, D.g.ny, D.g.nz);
+        const Band nb = load_band(D.a.dev, (int)(s & 1));
         band_macro_cell<S, PULL>((const typename Pop<S>::T*)D.f[parity], D.g, D.c, D.rho, D.ux, D.uy,
                                  D.uz, nb, (int)(t - off_new[i]));
     }
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) kb_box_flat(const EnsDesc* __restrict__ d
         fa.qx = D.a.fx;
         fa.qy = D.a.fy;
         fa.dev = D.a.dev;
-        const Band b = band_from_box(D.a.dev->box[D.a.dev->cur & 1], D.g.nx, D.g.ny, D.g.nz);
+        const Band b = load_band(D.a.dev, (int)(D.a.dev->cur & 1));
         box_pass_cell<S, PULL>((const T*)D.f[parity], (T*)D.f[parity ^ 1], D.g, D.c, fa, b,
                                (int)(t - off_new[i]));
     }
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
         Band band{};
-        if (D.has_ibm) band = band_from_box(D.a.dev->box[D.a.dev->cur & 1], g.nx, g.ny, g.nz);
+        if (D.has_ibm) band = load_band(D.a.dev, (int)(D.a.dev->cur & 1));
         // tiles run over the instance's cells in x-fastest order across row ends, so no
         // lane idles at the end of a row that is not a multiple of the tile width
         int x[K], y[K], z[K];

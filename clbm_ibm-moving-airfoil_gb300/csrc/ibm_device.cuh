@@ -73,6 +73,24 @@ __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid&
         int v = sbox[0][threadIdx.x];
         for (int w = 1; w < kMarkerBlock / 32; ++w) v = min(v, sbox[w][threadIdx.x]);
         if (v != kBoxEmpty) atomicMin(&a.dev->box[s & 1][threadIdx.x], v);
+        __threadfence();
+    }
+    // the last of the launch's ceil(n / 256) blocks converts the finished box to its band
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int nbx = (unsigned int)((a.n + kMarkerBlock - 1) / kMarkerBlock);
+        last = atomicAdd(&a.dev->mticket, 1u) == nbx - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        int bx6[6];
+        for (int e = 0; e < 6; ++e) bx6[e] = atomicAdd(&a.dev->box[s & 1][e], 0);
+        const Band b = band_from_box(bx6, g.nx, g.ny, g.nz);
+        int* o = a.dev->band[s & 1];
+        o[0] = b.i0; o[1] = b.ilen; o[2] = b.j0; o[3] = b.jlen; o[4] = b.k0; o[5] = b.klen;
+        a.dev->mticket = 0u;
     }
 }
 
@@ -143,7 +161,7 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     __shared__ bool last;
     IbmDev* dev = a.dev;
     const long long s = dev->step + 1;
-    const Band b = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
+    const Band b = load_band(dev, (int)(s & 1));
     const int cells = b.ilen * b.jlen * b.klen;
     const int stride = nbx * kFinishBlock;
     double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;

@@ -409,15 +409,16 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
                                                     typename Pop<S>::T* __restrict__ fout,
                                                     const Grid& g, const Coef& c,
                                                     const ForceArgs& fa, int x, int y, int z) {
-    if (FMODE == kForceSkipBand) {
-        // bulk pass of an IBM step: the cells of the force box are done by the box pass
-        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
-        if (in_band(b, x, y, z, g.ny, g.nz)) return;
-    }
     // shifted storage: the collision works on the deviations (no per-population shift)
     constexpr bool DEV = Pop<S>::kShifted;
     float f[19];
     gather<S, PULL, true>(fin, g, c, x, y, z, f);
+    if (FMODE == kForceSkipBand) {
+        // bulk pass of an IBM step: the cells of the force box are done by the box pass.
+        // Tested after the gather, so the box read does not delay the population loads.
+        const Band b = load_band(fa.dev, fa.slot);
+        if (in_band(b, x, y, z, g.ny, g.nz)) return;
+    }
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
     if (FMODE == kForceNone || FMODE == kForceSkipBand) {
         collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
@@ -425,7 +426,7 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
         const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
         collide<true, DEV>(f, c, fa.fx[cell], fa.fy[cell], Fz);
     } else {
-        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
+        const Band b = load_band(fa.dev, fa.slot);
         if (in_band(b, x, y, z, g.ny, g.nz)) {
             // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
             // fz is always zero there.
@@ -463,7 +464,7 @@ __device__ __forceinline__ void box_pass_body(const typename Pop<S>::T* __restri
                                               typename Pop<S>::T* __restrict__ fout,
                                               const Grid& g, const Coef& c, const ForceArgs& fa,
                                               int bx, int nbx) {
-    const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
+    const Band b = load_band(fa.dev, fa.slot);
     const int cells = b.ilen * b.jlen * b.klen;
     for (int t = bx * blockDim.x + threadIdx.x; t < cells; t += nbx * blockDim.x)
         box_pass_cell<S, PULL>(fin, fout, g, c, fa, b, t);
@@ -514,8 +515,8 @@ __device__ __forceinline__ void band_prepare_body(const typename Pop<S>::T* __re
                                                   bool compute_macro, int bx, int nbx) {
     // Box of this compute_force call (slot s & 1) and of the previous one (slot (s-1) & 1).
     const long long s = dev->step + 1;
-    const Band nb = band_from_box(dev->box[s & 1], g.nx, g.ny, g.nz);
-    const Band ob = band_from_box(dev->box[(s - 1) & 1], g.nx, g.ny, g.nz);
+    const Band nb = load_band(dev, (int)(s & 1));
+    const Band ob = load_band(dev, (int)((s - 1) & 1));
     const int stride = nbx * blockDim.x;
     const int ocells = ob.ilen * ob.jlen * ob.klen;
     for (int t = bx * blockDim.x + threadIdx.x; t < ocells; t += stride) band_zero_cell(g, fx, fy, ob, t);

@@ -17,6 +17,7 @@
 // Algorithmic traffic: 19 loads + 19 stores per cell (152 B/cell float32, 76 B/cell for
 // the 16-bit shifted forms); the force fields add 8 B per cell inside the IBM band only.
 #include <algorithm>
+#include <cstdlib>
 
 #include "lbm_device.cuh"
 
@@ -81,7 +82,7 @@ template <> struct Pair<CLBM_STORE_BF16S> {
 constexpr int kPX = 128;  // threads per block of the pair kernel (256 cells along x)
 
 template <int S, bool PULL, int FMODE>
-__global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
+__global__ void __launch_bounds__(kPX, 8) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
                                                              typename Pair<S>::T* __restrict__ fout,
                                                              Grid g, Coef c, ForceArgs fa) {
     using P = Pair<S>;
@@ -90,16 +91,8 @@ __global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair
     const int y = blockIdx.y, z = blockIdx.z;
     const int lane = threadIdx.x & 31;
     const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
-    bool in0 = false, in1 = false;
-    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
-        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
-        in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
-        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
-    }
-    const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
-    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
     // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
-    if (__all_sync(kFull, !use0 && !use1)) return;
+    if (__all_sync(kFull, !act0)) return;
     const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
     const long long row = ((long long)z * g.ny + y) * g.pitch;
     float h0[19], h1[19];
@@ -158,6 +151,16 @@ __global__ void __launch_bounds__(kPX) k_stream_collide_pair(const typename Pair
             }
         }
     }
+    // cells of the IBM force box: tested after the loads, so the box read does not delay them
+    bool in0 = false, in1 = false;
+    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
+        const Band b = load_band(fa.dev, fa.slot);
+        in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
+        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
+    }
+    const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
+    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
+    if (!use0 && !use1) return;
     // body force per cell
     float F0x = 0.f, F0y = 0.f, F0z = 0.f, F1x = 0.f, F1y = 0.f, F1z = 0.f;
     bool frc0 = false, frc1 = false;
@@ -291,7 +294,7 @@ __global__ void __launch_bounds__(256) k_stream_collide_tma(const typename Stg<S
     const bool act1 = x0 + 1 < g.nx;
     bool in0 = false, in1 = false;
     if (FMODE == kForceSkipBand || FMODE == kForceBand) {
-        const Band b = band_from_box(fa.dev->box[fa.slot], g.nx, g.ny, g.nz);
+        const Band b = load_band(fa.dev, fa.slot);
         in0 = in_band(b, x0, y, z, g.ny, g.nz);
         in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
     }
@@ -650,9 +653,15 @@ void launch_stream_collide(int storage, bool pull, int fmode, int variant, const
     });
 }
 
+int knob(const char* name, int def) {
+    const char* e = std::getenv(name);
+    return e ? std::atoi(e) : def;
+}
+
 static int box_blocks(long long max_cells, int block) {
+    static const int bps = knob("CLBM_CHAIN_BPS", 4);
     const long long b = (max_cells + block - 1) / block;
-    return (int)std::max<long long>(1, std::min<long long>(b, 4 * 152));
+    return (int)std::max<long long>(1, std::min<long long>(b, bps * 152));
 }
 
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,

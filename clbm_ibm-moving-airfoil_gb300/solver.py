@@ -209,7 +209,7 @@ class Solver:
         """Full-grid kernel chosen at creation and the autotune time per launch of each
         variant in microseconds (absent: not timed)."""
         v = ctypes.c_int32()
-        ms = (ctypes.c_float * 3)()
+        ms = (ctypes.c_float * len(self.VARIANTS))()
         check(lib().clbm_kernel_variant(self._h, ctypes.byref(v), ms))
         return dict(variant=self.VARIANTS[v.value],
                     us_per_launch={n: round(ms[i] * 1e3, 2) for i, n in enumerate(self.VARIANTS)

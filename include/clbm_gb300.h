@@ -201,8 +201,9 @@ int clbm_profile_read_split(clbm_solver* s, double* bulk_ms, int64_t* bulk_launc
 int clbm_device_bytes(const clbm_solver* s, int64_t* out);
 
 /* Full-grid stream-collide kernel chosen at creation (0 one cell per thread, 1 two cells
- * per thread, 2 rows staged in shared memory) and, when ms_per_launch is not NULL, the
- * autotune time per launch of each variant in milliseconds (0 for variants not timed:
+ * per thread, 2 rows staged in shared memory) and, when ms_per_launch is not NULL (3
+ * entries), the autotune time per launch of each variant in milliseconds (0 for variants
+ * not timed:
  * lattices below 2^20 cells and forced choices skip the timing). No reference
  * counterpart: the reference has one kernel per phase (clbm_moving.py:326-343). */
 int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_launch);
