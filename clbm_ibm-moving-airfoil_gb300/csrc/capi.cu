@@ -107,6 +107,8 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         // the low-priority stream while the IBM chain still computes the forces; the box
         // pass follows the IBM chain on the main stream; the main stream then joins the
         // bulk pass. The fork is valid only while the state is the one compute_force saw.
+        // CLBM_SERIAL=1: both passes on the main stream after the IBM chain, one after the
+        // other (the bulk pass then runs alone: its isolated time for measurements)
         static const int serial = knob("CLBM_SERIAL", 0);
         if (serial) {
             if (int rc = sc_timed(s, kForceSkipBand, fa, s->st, false, 0)) return rc;

@@ -29,9 +29,9 @@ __global__ void __launch_bounds__(kMarkerBlock) k_ibm_markers(IbmArrays a, Grid 
 }
 
 __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a, Grid g) {
-    const int nw = gridDim.x * (kSpreadBlock / 32);
-    for (int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5; m < a.n; m += nw)
-        ibm_interp_spread_body(a, g, m, threadIdx.x & 31);  // whole warps iterate together
+    const int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5;
+    if (m >= a.n) return;  // whole warp leaves together
+    ibm_interp_spread_body(a, g, m, threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g) {
@@ -49,17 +49,14 @@ void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
 
 void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st) {
     const long long threads = (long long)a.n * 32;
-    int blocks = (int)((threads + kSpreadBlock - 1) / kSpreadBlock);
+    const int blocks = (int)((threads + kSpreadBlock - 1) / kSpreadBlock);
     if (blocks == 0) return;
-    static const int bps = knob("CLBM_SPREAD_BPS", 0);
-    if (bps > 0) blocks = std::min(blocks, bps * 152);
     k_ibm_interp_spread<<<blocks, kSpreadBlock, 0, st>>>(a, g);
 }
 
 void launch_ibm_finish(const IbmArrays& a, const Grid& g, cudaStream_t st) {
     const long long work = std::max<long long>((long long)a.max_bx * a.max_by * a.max_bz, a.n);
-    static const int fb = std::min(std::max(knob("CLBM_FINISH_BLOCKS", kFinishBlocks), 1), kFinishBlocks);
-    int blocks = (int)std::min<long long>((work + kFinishBlock - 1) / kFinishBlock, fb);
+    int blocks = (int)std::min<long long>((work + kFinishBlock - 1) / kFinishBlock, kFinishBlocks);
     if (blocks < 1) blocks = 1;
     k_ibm_finish<<<blocks, kFinishBlock, 0, st>>>(a, g);
 }

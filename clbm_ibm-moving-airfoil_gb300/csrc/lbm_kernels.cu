@@ -659,9 +659,8 @@ int knob(const char* name, int def) {
 }
 
 static int box_blocks(long long max_cells, int block) {
-    static const int bps = knob("CLBM_CHAIN_BPS", 4);
     const long long b = (max_cells + block - 1) / block;
-    return (int)std::max<long long>(1, std::min<long long>(b, bps * 152));
+    return (int)std::max<long long>(1, std::min<long long>(b, 4 * 152));
 }
 
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
