@@ -920,9 +920,12 @@ int ens_upload(clbm_ensemble* e, int bx) {
         D.cells = s->g.nx * s->g.ny * s->g.nz;
         D.tile0 = tiles;
         t0[i] = tiles;
-        // the 16-bit forms take two cells per thread
-        const int tile_cells = e->storage == CLBM_STORE_F32 ? bx : 2 * bx;
-        tiles += (D.cells + tile_cells - 1) / tile_cells;
+        // a tile is a run of bx consecutive cells (float32) or a segment of bx cells of one
+        // row (16-bit forms: the two cells of a thread and a warp's rows stay in one row)
+        if (e->storage != CLBM_STORE_F32)
+            tiles += (long long)((s->g.nx + bx - 1) / bx) * s->g.ny * s->g.nz;
+        else
+            tiles += (D.cells + bx - 1) / bx;
     }
     CK(cudaMemcpyAsync(e->d_desc, h.data(), sizeof(EnsDesc) * e->n, cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->d_tile0, t0.data(), sizeof(long long) * e->n, cudaMemcpyHostToDevice, e->st));

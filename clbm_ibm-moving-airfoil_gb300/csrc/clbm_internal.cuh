@@ -341,7 +341,7 @@ struct EnsDesc {
     IbmArrays a;
     clbm_motion m;
     long long tile0;   // first bulk tile of this instance in the flat tile list
-    int cells;         // nx * ny * nz; a tile is a run of consecutive cells in x-fastest order
+    int cells;         // nx * ny * nz
     int has_ibm;
 };
 

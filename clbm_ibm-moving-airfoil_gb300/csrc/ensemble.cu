@@ -6,8 +6,8 @@
 // as it needs, the rest leave); band-prepare and the box pass run one thread per force-box
 // cell over a flat list of all instances' boxes. The bulk stream-collide pass runs
 // persistent blocks over one flat list of tiles (runs of consecutive cells) of all
-// instances, so lattices of different sizes share the GPU without tail effects;
-// the tile width and the number of persistent blocks are picked by timing at creation.
+// instances, so lattices of different sizes share the GPU without tail effects; the tile
+// width and the number of persistent blocks are picked by timing at creation.
 // Every per-cell and per-marker computation is the single-lattice code (lbm_device.cuh,
 // ibm_device.cuh), so an instance gives the same bits as when it is stepped alone.
 #include <algorithm>
@@ -130,16 +130,18 @@ __global__ void __launch_bounds__(256) kb_box_flat(const EnsDesc* __restrict__ d
     }
 }
 
-// Bulk pass over the flat tile list. Float32: one cell per thread, tiles of BX cells.
-// 16-bit shifted forms: two cells per thread (t and BX + t of a tile of 2 BX cells), the
-// collision of both in packed f32x2 arithmetic (the same bits as the one-cell form).
-template <int S, bool PULL, int BX>
-__global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
-                                              const long long* __restrict__ tile0, int n,
-                                              long long ntiles, int parity) {
+// Bulk pass over the flat tile list: tile t of instance i is tile (t - tile0[i]) of that
+// instance, W cells each. Float32 (one cell per thread) takes runs of W consecutive cells in
+// x-fastest order across row ends, so no lane idles at the end of a row; the 16-bit forms
+// (two neighbouring cells of one row per thread) take segments of W cells of one row, so a
+// warp's rows and their neighbour rows are the same for all its lanes. Each thread runs the
+// single-lattice bodies (stream_collide_cell; pair_body: half2 loads, warp-shuffle x
+// shifts), so an instance gives the same bits as when it is stepped alone.
+template <int S, bool PULL, int W>
+__global__ void __launch_bounds__(S == CLBM_STORE_F32 ? W : W / 2, S == CLBM_STORE_F32 ? 1024 / W : 2048 / W)
+kb_bulk(const EnsDesc* __restrict__ d, const long long* __restrict__ tile0, int n, long long ntiles,
+        int parity) {
     using T = typename Pop<S>::T;
-    constexpr bool DEV = Pop<S>::kShifted;
-    constexpr int K = DEV ? 2 : 1;  // cells per thread
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         // instance of tile t: the last i with tile0[i] <= t
         int lo = 0, hi = n - 1;
@@ -150,38 +152,32 @@ __global__ void __launch_bounds__(BX) kb_bulk(const EnsDesc* __restrict__ d,
         }
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
+        const Coef c = D.c;
+        const unsigned local = (unsigned)(t - D.tile0);
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
-        Band band{};
-        if (D.has_ibm) band = load_band(D.a.dev, (int)(D.a.dev->cur & 1));
-        // tiles run over the instance's cells in x-fastest order across row ends, so no
-        // lane idles at the end of a row that is not a multiple of the tile width
-        int x[K], y[K], z[K];
-        bool use[K];
-        float h[K][19];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const unsigned i = (unsigned)(t - D.tile0) * (BX * K) + k * BX + threadIdx.x;
-            use[k] = i < (unsigned)D.cells;
-            x[k] = y[k] = z[k] = 0;
-            if (use[k]) {
+        ForceArgs fa{};
+        if (D.has_ibm) {
+            fa.dev = D.a.dev;
+            fa.slot = (int)(D.a.dev->cur & 1);
+        }
+        if constexpr (S == CLBM_STORE_F32) {
+            const unsigned i = local * W + threadIdx.x;
+            if (i < (unsigned)D.cells) {
                 const unsigned row = i / (unsigned)g.nx;
-                x[k] = (int)(i - row * (unsigned)g.nx);
-                y[k] = (int)(row % (unsigned)g.ny);
-                z[k] = (int)(row / (unsigned)g.ny);
-                if (D.has_ibm && in_band(band, x[k], y[k], z[k], g.ny, g.nz)) use[k] = false;
+                const int x = (int)(i - row * (unsigned)g.nx);
+                const int y = (int)(row % (unsigned)g.ny), z = (int)(row / (unsigned)g.ny);
+                if (D.has_ibm) stream_collide_cell<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, x, y, z);
+                else stream_collide_cell<S, PULL, kForceNone>(fin, fout, g, c, fa, x, y, z);
             }
-            if (use[k]) gather<S, PULL, true>(fin, g, D.c, x[k], y[k], z[k], h[k]);
+        } else {
+            const int nseg = (g.nx + W - 1) / W;
+            const int r = (int)local / nseg;   // row z * ny + y
+            const int x0 = ((int)local - r * nseg) * W + 2 * threadIdx.x;
+            const int y = r % g.ny, z = r / g.ny;
+            if (D.has_ibm) pair_body<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, x0, y, z);
+            else pair_body<S, PULL, kForceNone>(fin, fout, g, c, fa, x0, y, z);
         }
-        if (K == 2) {
-            collide_pair<DEV>(h[0], h[K - 1], D.c, use[0], use[K - 1], false, false, 0.f, 0.f, 0.f,
-                              0.f, 0.f, 0.f);
-        } else if (use[0]) {
-            collide<false, DEV>(h[0], D.c, 0.f, 0.f, 0.f);
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (use[k]) store_raw<S>(fout, g, ((long long)z[k] * g.ny + y[k]) * g.pitch + x[k], h[k]);
     }
 }
 
@@ -230,8 +226,9 @@ void launch_ens_box_flat(int storage, bool pull, const EnsDesc* d, int n, const 
 template <int S, bool PULL>
 static void ens_bulk(int bx, const EnsDesc* d, const long long* tile0, int n, long long ntiles,
                      int parity, int grid, cudaStream_t st) {
-    if (bx == 256) kb_bulk<S, PULL, 256><<<grid, 256, 0, st>>>(d, tile0, n, ntiles, parity);
-    else kb_bulk<S, PULL, 128><<<grid, 128, 0, st>>>(d, tile0, n, ntiles, parity);
+    constexpr int kDiv = S == CLBM_STORE_F32 ? 1 : 2;  // cells per thread
+    if (bx == 256) kb_bulk<S, PULL, 256><<<grid, 256 / kDiv, 0, st>>>(d, tile0, n, ntiles, parity);
+    else kb_bulk<S, PULL, 128><<<grid, 128 / kDiv, 0, st>>>(d, tile0, n, ntiles, parity);
 }
 
 void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,

@@ -403,6 +403,165 @@ __device__ __forceinline__ void collide_pair(float (&h0)[19], float (&h1)[19], c
     }
 }
 
+// ------------------------------------------------------------------ 16-bit pair kernel
+// Shifted 16-bit storage moves half the bytes of float32, so the one-cell kernel becomes
+// issue-bound. This variant gives each thread two neighbouring cells (x0, x0 + 1), x0 even:
+// every population is one aligned 32-bit load/store of a half2 (or bf16x2); the x-shifted
+// pulls take the neighbour element from the adjacent lane with a warp shuffle (the lanes at
+// the two warp edges load that one element themselves); the collision works on the
+// deviations directly (collide<.., DEV = true>), both cells at once in packed f32x2.
+template <int S> struct Pair;
+template <> struct Pair<CLBM_STORE_F16S> {
+    using T = __half;
+    static __device__ __forceinline__ float2 ld2(const T* p) {
+        return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    }
+    static __device__ __forceinline__ float ld1(const T* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) {
+        const __half2 h = __floats2half2_rn(a, b);
+        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+    }
+    static __device__ __forceinline__ void st1(T* p, float a) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(a)));
+    }
+};
+template <> struct Pair<CLBM_STORE_BF16S> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ float2 ld2(const T* p) {
+        return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)));
+    }
+    static __device__ __forceinline__ float ld1(const T* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ void st2(T* p, float a, float b) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+    }
+    static __device__ __forceinline__ void st1(T* p, float a) {
+        __stcs(reinterpret_cast<unsigned short*>(p), __bfloat16_as_ushort(__float2bfloat16_rn(a)));
+    }
+};
+
+// Cells (x0, x0 + 1) of row (y, z), x0 even, for a warp of consecutive pairs of one row
+// (lanes past the lattice edge take part in the shuffles and store nothing).
+template <int S, bool PULL, int FMODE>
+__device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
+                                          typename Pair<S>::T* __restrict__ fout, const Grid& g,
+                                          const Coef& c, const ForceArgs& fa, int x0, int y, int z) {
+    using P = Pair<S>;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
+    // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
+    if (__all_sync(kFull, !act0)) return;
+    const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
+    const long long row = ((long long)z * g.ny + y) * g.pitch;
+    float h0[19], h1[19];
+    if (!PULL) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const float2 p = P::ld2(fin + q * g.plane + row + x0c);
+            h0[q] = p.x;
+            h1[q] = p.y;
+        }
+    } else {
+        const int ym = (y == 0) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1) ? 0 : z + 1;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+            const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+            const typename P::T* rp = fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch;
+            const float2 p = P::ld2(rp + x0c);
+            if (ex(q) == 0) {
+                h0[q] = p.x;
+                h1[q] = p.y;
+            } else if (ex(q) == 1) {  // pull from x - 1
+                float up = __shfl_up_sync(kFull, p.y, 1);
+                if (lane == 0) up = (x0 >= 1 && x0 - 1 < g.nx) ? P::ld1(rp + (x0 - 1)) : 0.0f;
+                h0[q] = up;   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
+                h1[q] = p.x;
+            } else {                  // pull from x + 1
+                float dn = __shfl_down_sync(kFull, p.x, 1);
+                if (lane == 31) dn = (x0 + 2 < g.nx) ? P::ld1(rp + (x0 + 2)) : 0.0f;
+                h0[q] = p.y;
+                h1[q] = dn;
+            }
+        }
+        if (x0 == 0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h0[q] += wq(q);
+            zou_he(h0, c);
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h0[q] -= wq(q);
+        }
+        if (x0 + 1 == g.nx - 1) {
+            // outlet column Nx-1 is a copy of column Nx-2 = x0 (clbm_moving.py:296-300)
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h1[q] = h0[q];
+        } else if (x0 == g.nx - 1) {
+            // odd Nx: the outlet is the first cell of the last pair; pull like column Nx-2
+            const int xe = g.nx - 2;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+                const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+                h0[q] = P::ld1(fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + (xe - ex(q)));
+            }
+        }
+    }
+    // cells of the IBM force box: tested after the loads, so the box read does not delay them
+    bool in0 = false, in1 = false;
+    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
+        const Band b = load_band(fa.dev, fa.slot);
+        in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
+        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
+    }
+    const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
+    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
+    if (!use0 && !use1) return;
+    // body force per cell
+    float F0x = 0.f, F0y = 0.f, F0z = 0.f, F1x = 0.f, F1y = 0.f, F1z = 0.f;
+    bool frc0 = false, frc1 = false;
+    if (FMODE == kForceBand) {
+        frc0 = in0;
+        frc1 = in1;
+        if (in0) {
+            F0x = fminf(fmaxf(qforce(fa.qx[row + x0]), -0.05f), 0.05f);
+            F0y = fminf(fmaxf(qforce(fa.qy[row + x0]), -0.05f), 0.05f);
+        }
+        if (in1) {
+            F1x = fminf(fmaxf(qforce(fa.qx[row + x0 + 1]), -0.05f), 0.05f);
+            F1y = fminf(fmaxf(qforce(fa.qy[row + x0 + 1]), -0.05f), 0.05f);
+        }
+    } else if (FMODE == kForceDense) {
+        frc0 = act0;
+        frc1 = act1;
+        if (act0) {
+            F0x = fa.fx[row + x0]; F0y = fa.fy[row + x0]; F0z = fa.fz ? fa.fz[row + x0] : 0.f;
+        }
+        if (act1) {
+            F1x = fa.fx[row + x0 + 1]; F1y = fa.fy[row + x0 + 1];
+            F1z = fa.fz ? fa.fz[row + x0 + 1] : 0.f;
+        }
+    }
+    collide_pair<true>(h0, h1, c, use0, use1, frc0, frc1, F0x, F0y, F0z, F1x, F1y, F1z);
+    if (use0 && use1) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) P::st2(fout + q * g.plane + row + x0, h0[q], h1[q]);
+    } else {
+        if (use0) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0, h0[q]);
+        }
+        if (use1) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0 + 1, h1[q]);
+        }
+    }
+}
+
+
 // One cell of the full-grid pass: gather, force (per FMODE), collide, store.
 template <int S, bool PULL, int FMODE>
 __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __restrict__ fin,

@@ -9,20 +9,24 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 SMALL = ((48, 24, 4), (64, 20, 6), (40, 16, 3))
+# odd and even widths (the 16-bit bulk pass tiles by row segments, float32 by runs across
+# row ends)
+MIXED = ((47, 20, 4), (64, 20, 6), (41, 16, 3))
 
 
-def _cases(pkg, storage, n=5):
-    return [pkg.config.ensemble_case(seed, storage=storage, lattices=SMALL) for seed in range(n)]
+def _cases(pkg, storage, n=5, lattices=SMALL):
+    return [pkg.config.ensemble_case(seed, storage=storage, lattices=lattices) for seed in range(n)]
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", ["cell", "pair"])
-def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant):
+@pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
+def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant, lattices):
     """The single runs use either full-grid kernel; all variants give the same bits."""
     pkg = built_pkg
     monkeypatch.setenv("CLBM_KERNEL", variant)
-    cases = _cases(pkg, storage)
+    cases = _cases(pkg, storage, lattices=lattices)
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
     t = ens.tuning()
