@@ -203,6 +203,29 @@ def compare(fine, coarse):
                 wall_ratio=fine["wall_s"] / max(coarse["wall_s"], 1e-9))
 
 
+def span_sweep(net_path, fine_json, scales, coarse_steps, log, base=BASE, re=2000.0):
+    """A trained network with its output range (span) scaled at inference, each scale one
+    coarse run, compared with the fine run's statistics saved by an earlier study."""
+    with open(fine_json) as fh:
+        fine = json.load(fh)["fine"]
+    out = []
+    for m in scales:
+        net = closure.ClosureNet.load(net_path)
+        net.view("span")[:] *= m
+        r = run_coarse(net, coarse_steps, 1, log, base=base, re=re)
+        row = dict(span_scale=m, span=float(net.view("span")[0]), wall_s=r["wall_s"])
+        if "stats" in r:
+            f, c = fine["stats"], r["stats"]
+            row.update({k: c[k] for k in ("cl_mean", "cd_mean", "cl_rms", "cd_rms")})
+            row.update({k + "_err": abs(c[k] - f[k]) / abs(f[k])
+                        for k in ("cl_mean", "cd_mean", "cl_rms", "cd_rms")})
+        else:
+            row["diverged"] = r.get("diverged")
+        log(f"span x{m}: {row}")
+        out.append(row)
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--coarse-steps", type=int, default=20000)
@@ -226,9 +249,24 @@ def main(argv=None):
                     help="coarse nx ny nz chord (the fine lattice doubles each)")
     ap.add_argument("--save-net", default=None)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--span-sweep", type=float, nargs="+", default=None,
+                    help="no fine run or training: scale the output range of --load-net by "
+                         "each factor and compare coarse runs with the fine statistics of "
+                         "--fine-json (an earlier --out file)")
+    ap.add_argument("--load-net", default=None)
+    ap.add_argument("--fine-json", default=None)
     args = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)
     base = tuple(args.base)
+    if args.span_sweep:
+        rows = span_sweep(args.load_net, args.fine_json, args.span_sweep, args.coarse_steps, log,
+                          base=base, re=args.re)
+        text = json.dumps(dict(span_sweep=rows, net=args.load_net), indent=1, default=float)
+        print(text)
+        if args.out:
+            with open(args.out, "w") as fh:
+                fh.write(text + "\n")
+        return rows
     fine, trainer = run_fine(args.coarse_steps, args.sample_every, args.sample_start,
                              args.cells_per_snapshot, args.seed, args.spectra, log, base=base,
                              re=args.re)
