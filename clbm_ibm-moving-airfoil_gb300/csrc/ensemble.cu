@@ -199,7 +199,9 @@ void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t 
 }
 
 void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st) {
-    kb_finish<<<dim3(kFinishBlocks, n), kFinishBlock, 0, st>>>(d);
+    // a quarter of the single-lattice blocks per member: the members' boxes are small and
+    // the blocks of all members fill the GPU (fewer block reductions)
+    kb_finish<<<dim3(kFinishBlocks / 4, n), kFinishBlock, 0, st>>>(d);
 }
 
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st) {

@@ -164,19 +164,32 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     const Band b = load_band(dev, (int)(s & 1));
     const int cells = b.ilen * b.jlen * b.klen;
     const int stride = nbx * kFinishBlock;
-    double sx = 0.0, sy = 0.0, mx = 0.0, my = 0.0;
+    // Every clipped Eulerian value is an integer multiple of 2^-40 (a float of the int64
+    // field times 2^-40, or the float 0.05f = 13421773 * 2^-28) of magnitude <= 0.05. The
+    // integers k = value * 2^40 are summed exactly in int64 and converted once: the exact
+    // sum rounded to double, which is also what adding the values in double gives, in any
+    // order, while the partial sums stay below 2^13 (every add is then exact); this keeps
+    // the slow double-precision adds of this part to one per block.
+    long long kx = 0, ky = 0;
+    double mx = 0.0, my = 0.0;
     for (int t = bx * kFinishBlock + threadIdx.x; t < cells; t += stride) {
         int x, y, z;
         box_cell(b, g.ny, g.nz, t, x, y, z);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
-        sx += (double)fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f);
-        sy += (double)fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f);
+        kx += (long long)(fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f) * kForceScale);
+        ky += (long long)(fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f) * kForceScale);
     }
     for (int t = bx * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
         mx += (double)a.FXk[t];
         my += (double)a.FYk[t];
     }
-    sx = warp_sum(sx); sy = warp_sum(sy); mx = warp_sum(mx); my = warp_sum(my);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        kx += __shfl_xor_sync(0xffffffffu, kx, o);
+        ky += __shfl_xor_sync(0xffffffffu, ky, o);
+    }
+    const double sx = (double)kx * (double)kForceInvScale, sy = (double)ky * (double)kForceInvScale;
+    mx = warp_sum(mx); my = warp_sum(my);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) { red[warp][0] = sx; red[warp][1] = sy; red[warp][2] = mx; red[warp][3] = my; }
     __syncthreads();
