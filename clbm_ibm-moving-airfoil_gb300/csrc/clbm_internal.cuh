@@ -256,6 +256,7 @@ struct ForceArgs {
 };
 
 int knob(const char* name, int def);  // integer tuning parameter from the environment
+bool spread_tiled();                  // IBM spreading through shared-memory tiles (CLBM_SPREAD)
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
 // Stream-collide kernel variants for the full-grid pass:
 //   kVariantCell    one cell per thread, direct loads (float32 parity kernel)

@@ -30,6 +30,12 @@ __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread(const EnsDesc* 
     ibm_interp_spread_body(D.a, D.g, m, threadIdx.x & 31);
 }
 
+__global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread_tiled(const EnsDesc* __restrict__ d) {
+    const EnsDesc& D = d[blockIdx.y];
+    if (!D.has_ibm || (int)blockIdx.x * kTileMarkers >= D.a.n) return;  // whole block
+    ibm_interp_spread_tiled_body(D.a, D.g, blockIdx.x);
+}
+
 __global__ void __launch_bounds__(kFinishBlock) kb_finish(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
     if (!D.has_ibm) return;
@@ -195,6 +201,11 @@ void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
 
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     if (blocks < 1) return;
+    if (spread_tiled()) {
+        // blocks of the warp-per-marker form cover 8 markers; a tiled block covers 32
+        kb_interp_spread_tiled<<<dim3((blocks + 3) / 4, n), kSpreadBlock, 0, st>>>(d);
+        return;
+    }
     kb_interp_spread<<<dim3(blocks, n), kSpreadBlock, 0, st>>>(d);
 }
 

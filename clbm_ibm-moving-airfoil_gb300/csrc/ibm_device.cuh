@@ -94,15 +94,21 @@ __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid&
     }
 }
 
+// Stencil taps of one marker held by a lane (two of the 64), with the marker's force.
+struct MarkerTaps {
+    float wt[2];      // Peskin weight of tap h
+    int ii[2];        // x index (clamped)
+    int jr[2], kr[2]; // y, z index before the periodic wrap
+    float fx, fy;     // clipped marker force
+};
+
 // One warp per marker m: Peskin interpolation of the current velocity (two stencil taps
-// per lane, warp-shuffle sums; airfoil_moving.py:142-170), marker force clip
-// (airfoil_moving.py:175-183) and spreading in 64-bit fixed point (airfoil_moving.py:188-214).
-__device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const Grid& g, int m,
-                                                       int lane) {
+// per lane, warp-shuffle sums; airfoil_moving.py:142-170) and the marker force clip
+// (airfoil_moving.py:175-183); the taps are kept for spreading.
+__device__ __forceinline__ void ibm_interp_marker(const IbmArrays& a, const Grid& g, int m, int lane,
+                                                  MarkerTaps& tp) {
     const float xk = a.X[m], yk = a.Y[m], zk = a.Z[m];
     const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
-    float wt[2];
-    long long cell[2];
     float us = 0.f, vs = 0.f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
@@ -114,8 +120,10 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
         const int kk = pmod(kb + dk, g.nz);              // uses the wrapped index, as there
         const float w = phi1d((float)ii - xk) * phi1d((float)jj - yk) * phi1d((float)kk - zk);
         const long long c = ((long long)kk * g.ny + jj) * g.pitch + ii;
-        wt[h] = w;
-        cell[h] = c;
+        tp.wt[h] = w;
+        tp.ii[h] = ii;
+        tp.jr[h] = jb + dj;
+        tp.kr[h] = kb + dk;
         if (w != 0.0f) {
             us += a.ux[c] * w;
             vs += a.uy[c] * w;
@@ -126,24 +134,123 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
         us += __shfl_xor_sync(0xffffffffu, us, o);
         vs += __shfl_xor_sync(0xffffffffu, vs, o);
     }
-    const float fxk = fmaxf(-0.05f, fminf(0.05f, -(us - a.VX[m])));
-    const float fyk = fmaxf(-0.05f, fminf(0.05f, -(vs - a.VY[m])));
+    tp.fx = fmaxf(-0.05f, fminf(0.05f, -(us - a.VX[m])));
+    tp.fy = fmaxf(-0.05f, fminf(0.05f, -(vs - a.VY[m])));
     if (lane == 0) {
         a.Uk[m] = us;
         a.Vk[m] = vs;
-        a.FXk[m] = fxk;
-        a.FYk[m] = fyk;
+        a.FXk[m] = tp.fx;
+        a.FYk[m] = tp.fy;
     }
-    // spreading: the float32 contribution fxk * w (airfoil_moving.py:212-214) is added in
-    // 64-bit fixed point, so the sum does not depend on the order of the atomics
+}
+
+// Spreading contribution of tap h in 64-bit fixed point: the float32 product f * w
+// (airfoil_moving.py:212-214) scaled by 2^40, so sums do not depend on their order.
+__device__ __forceinline__ long long spread_q(float f, float w) {
+    return __float2ll_rn(f * w * kForceScale);
+}
+
+// One warp per marker: interpolation, then spreading with one global atomic per tap and
+// component.
+__device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const Grid& g, int m,
+                                                       int lane) {
+    MarkerTaps tp;
+    ibm_interp_marker(a, g, m, lane, tp);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        if (wt[h] != 0.0f) {
-            atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + cell[h]),
-                      (unsigned long long)__float2ll_rn(fxk * wt[h] * kForceScale));
-            atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + cell[h]),
-                      (unsigned long long)__float2ll_rn(fyk * wt[h] * kForceScale));
+        if (tp.wt[h] != 0.0f) {
+            const long long c = ((long long)pmod(tp.kr[h], g.nz) * g.ny + pmod(tp.jr[h], g.ny)) * g.pitch + tp.ii[h];
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)spread_q(tp.fx, tp.wt[h]));
+            atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)spread_q(tp.fy, tp.wt[h]));
         }
+    }
+}
+
+// Spreading through a shared-memory tile: a block of 8 warps takes kTileMarkers
+// consecutive markers (a body's markers are stored in surface order, so they lie close
+// together), interpolates them (a warp per marker, as above), accumulates their int64
+// contributions in a tile over the box their stencils cover (y, z before the wrap) and
+// adds each touched cell to the global fields once. The sums are the same integers as with
+// one global atomic per tap. A chunk whose box exceeds the tile (or spans the lattice in
+// y or z) spreads with direct global atomics.
+constexpr int kTileMarkers = 32;
+constexpr int kTileCells = 2048;   // two int64 per cell: 32 KB of shared memory
+constexpr int kTileMarkersPerWarp = kTileMarkers / (kSpreadBlock / 32);
+
+__device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a, const Grid& g, int chunk) {
+    __shared__ long long tfx[kTileCells], tfy[kTileCells];
+    __shared__ int sb[6];   // box, inclusive: imin, -imax, jmin, -jmax, kmin, -kmax
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 6) sb[threadIdx.x] = 0x7fffffff;
+    __syncthreads();
+    MarkerTaps tp[kTileMarkersPerWarp];
+    bool has[kTileMarkersPerWarp];
+#pragma unroll
+    for (int i = 0; i < kTileMarkersPerWarp; ++i) {
+        const int m = chunk * kTileMarkers + warp * kTileMarkersPerWarp + i;
+        has[i] = m < a.n;   // warp-uniform
+        if (has[i]) {
+            ibm_interp_marker(a, g, m, lane, tp[i]);
+            // taps 0 and 63 hold the stencil's corners (di, dj, dk = 0 and 3)
+            if (lane == 0) {
+                atomicMin(&sb[0], tp[i].ii[0]);
+                atomicMin(&sb[2], tp[i].jr[0]);
+                atomicMin(&sb[4], tp[i].kr[0]);
+            } else if (lane == 31) {
+                atomicMin(&sb[1], -tp[i].ii[1]);
+                atomicMin(&sb[3], -tp[i].jr[1]);
+                atomicMin(&sb[5], -tp[i].kr[1]);
+            }
+        }
+    }
+    __syncthreads();
+    const int i0 = sb[0], j0 = sb[2], k0 = sb[4];
+    const int li = -sb[1] - i0 + 1, lj = -sb[3] - j0 + 1, lk = -sb[5] - k0 + 1;
+    const bool tiled = sb[0] != 0x7fffffff && lj < g.ny && lk < g.nz &&
+                       (long long)li * lj * lk <= kTileCells;   // block-uniform
+    if (!tiled) {
+#pragma unroll
+        for (int i = 0; i < kTileMarkersPerWarp; ++i) {
+            if (!has[i]) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (tp[i].wt[h] != 0.0f) {
+                    const long long c = ((long long)pmod(tp[i].kr[h], g.nz) * g.ny + pmod(tp[i].jr[h], g.ny)) * g.pitch + tp[i].ii[h];
+                    atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)spread_q(tp[i].fx, tp[i].wt[h]));
+                    atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)spread_q(tp[i].fy, tp[i].wt[h]));
+                }
+            }
+        }
+        return;
+    }
+    const int vol = li * lj * lk;
+    for (int t = threadIdx.x; t < vol; t += kSpreadBlock) {
+        tfx[t] = 0;
+        tfy[t] = 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kTileMarkersPerWarp; ++i) {
+        if (!has[i]) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (tp[i].wt[h] != 0.0f) {
+                const int l = (tp[i].ii[h] - i0) + li * ((tp[i].jr[h] - j0) + lj * (tp[i].kr[h] - k0));
+                atomicAdd(reinterpret_cast<unsigned long long*>(tfx + l), (unsigned long long)spread_q(tp[i].fx, tp[i].wt[h]));
+                atomicAdd(reinterpret_cast<unsigned long long*>(tfy + l), (unsigned long long)spread_q(tp[i].fy, tp[i].wt[h]));
+            }
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < vol; t += kSpreadBlock) {
+        const long long vx = tfx[t], vy = tfy[t];
+        if (vx == 0 && vy == 0) continue;
+        const int x = i0 + t % li;
+        const int r = t / li;
+        const int y = pmod(j0 + r % lj, g.ny), z = pmod(k0 + r / lj, g.nz);
+        const long long c = ((long long)z * g.ny + y) * g.pitch + x;
+        if (vx) atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)vx);
+        if (vy) atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)vy);
     }
 }
 

@@ -17,6 +17,8 @@
 //                        device call counter. The clip itself (_clip_forces,
 //                        airfoil_moving.py:219-225) is applied where the fields are read.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "ibm_device.cuh"
 
@@ -34,6 +36,10 @@ __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a,
     ibm_interp_spread_body(a, g, m, threadIdx.x & 31);
 }
 
+__global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread_tiled(IbmArrays a, Grid g) {
+    ibm_interp_spread_tiled_body(a, g, blockIdx.x);
+}
+
 __global__ void __launch_bounds__(kFinishBlock) k_ibm_finish(IbmArrays a, Grid g) {
     ibm_finish_body(a, g, blockIdx.x, gridDim.x);
 }
@@ -47,7 +53,20 @@ void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
     else k_ibm_markers<false><<<blocks, kMarkerBlock, 0, st>>>(a, g, mf, m);
 }
 
+// Spreading form: CLBM_SPREAD=tiled accumulates blocks of consecutive markers in
+// shared-memory tiles; the default spreads with one global atomic per tap (faster at the
+// marker counts measured, see the design notes).
+bool spread_tiled() {
+    const char* e = std::getenv("CLBM_SPREAD");   // read at every launch (graphs keep theirs)
+    return e && !std::strcmp(e, "tiled");
+}
+
 void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st) {
+    if (spread_tiled()) {
+        const int blocks = (a.n + kTileMarkers - 1) / kTileMarkers;
+        if (blocks > 0) k_ibm_interp_spread_tiled<<<blocks, kSpreadBlock, 0, st>>>(a, g);
+        return;
+    }
     const long long threads = (long long)a.n * 32;
     const int blocks = (int)((threads + kSpreadBlock - 1) / kSpreadBlock);
     if (blocks == 0) return;
