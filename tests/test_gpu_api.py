@@ -207,7 +207,13 @@ def test_shifted_storage_error_against_fp64_oracle(gpkg, oracle_mod, storage, to
     rho, ux, uy, _ = ref.macro()
     e_rho = rel_l2(got["rho"] - 1.0, rho - 1.0)
     e_u = rel_l2(got["ux"], ux)
-    e_f = rel_l2(sim.ibm.force_history(300), ref_hist)
-    print(f"{storage}: rel L2 (rho-1) {e_rho:.2e}, ux {e_u:.2e}, force history {e_f:.2e}")
+    hist = sim.ibm.force_history(300)
+    e_f = rel_l2(hist, ref_hist)
+    # mean C_L and C_D over the run (the precision form's target: within 1 % of FP64)
+    cg, cr = gpkg.force_coefficients(hist, cfg), gpkg.force_coefficients(ref_hist, cfg)
+    e_mean = {k: abs(np.mean(cg[k]) - np.mean(cr[k])) / abs(np.mean(cr[k])) for k in ("cl", "cd")}
+    print(f"{storage}: rel L2 (rho-1) {e_rho:.2e}, ux {e_u:.2e}, force history {e_f:.2e}, "
+          f"mean C_L {e_mean['cl']:.2e}, mean C_D {e_mean['cd']:.2e}")
     assert e_u < tol and e_f < 10 * tol
+    assert e_mean["cl"] < 1e-2 and e_mean["cd"] < 1e-2
     sim.close()
