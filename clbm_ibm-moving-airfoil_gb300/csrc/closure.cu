@@ -95,10 +95,17 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
         bool use = i < ca.cells;
         int x = 0, y = 0, z = 0;
         if (use) {
-            const long long row = i / g.nx;
-            x = (int)(i - row * g.nx);
-            y = (int)(row % g.ny);
-            z = (int)(row / g.ny);
+            if (ca.cells <= 0xffffffffLL) {   // 32-bit divisions (64-bit ones are far slower)
+                const unsigned ui = (unsigned)i, row = ui / (unsigned)g.nx;
+                x = (int)(ui - row * (unsigned)g.nx);
+                y = (int)(row % (unsigned)g.ny);
+                z = (int)(row / (unsigned)g.ny);
+            } else {
+                const long long row = i / g.nx;
+                x = (int)(i - row * g.nx);
+                y = (int)(row % g.ny);
+                z = (int)(row / g.ny);
+            }
             if (FMODE == kForceSkipBand && in_band(band, x, y, z, g.ny, g.nz)) use = false;
         }
         float f[19];
