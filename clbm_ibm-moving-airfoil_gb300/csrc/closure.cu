@@ -65,7 +65,7 @@ __device__ __forceinline__ void tc_sync() {
 // layer on the CUDA cores, collision with s_h, store. Cells of the IBM force box (SkipBand)
 // are left to the box pass, which uses the plain collision with forcing; the inlet and
 // outlet columns (x = 0, nx - 1) keep the plain rates.
-template <int S, bool PULL, int FMODE>
+template <int S, bool PULL, int FMODE, bool IDX32>
 __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typename Pop<S>::T* __restrict__ fin,
                                                                 typename Pop<S>::T* __restrict__ fout,
                                                                 Grid g, Coef c, ForceArgs fa,
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
         float f[19];
         float v[32];
         if (use) {
-            gather<S, PULL, true>(fin, g, c, x, y, z, f);
+            gather<S, PULL, true, IDX32>(fin, g, c, x, y, z, f);
             CMom m;
             moments_full<DEV>(f, m);
             standardise(m, net, v);
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
                 higher_order_post(m, sh, ho);
                 collide_ho<DEV>(f, c, ho);
             }
-            store_raw<S>(fout, g, ((long long)z * g.ny + y) * g.pitch + x, f);
+            store_raw<S, IDX32>(fout, g, ((long long)z * g.ny + y) * g.pitch + x, f);
         }
     }
     if (!ok) {
@@ -198,10 +198,17 @@ template <int S, bool PULL>
 static void closure_sc(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
                        const ForceArgs& fa, const ClosureArgs& ca, int grid, cudaStream_t st) {
     using T = typename Pop<S>::T;
+    if (19LL * g.plane <= 0xffffffffLL) {   // every element index fits 32 bits
+        if (fmode == kForceSkipBand)
+            k_closure_stream_collide<S, PULL, kForceSkipBand, true><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        else
+            k_closure_stream_collide<S, PULL, kForceNone, true><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        return;
+    }
     if (fmode == kForceSkipBand)
-        k_closure_stream_collide<S, PULL, kForceSkipBand><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        k_closure_stream_collide<S, PULL, kForceSkipBand, false><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
     else
-        k_closure_stream_collide<S, PULL, kForceNone><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        k_closure_stream_collide<S, PULL, kForceNone, false><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
 }
 
 // Persistent grid: the blocks that fit on an SM by registers (65,536 per SM) and by
@@ -212,7 +219,7 @@ int closure_grid(int storage) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncAttributes fa{};
     CLBM_CL_STORE(storage, {
-        if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand>) == cudaSuccess)
+        if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand, true>) == cudaSuccess)
             regs = fa.numRegs;
     });
     cudaGetLastError();

@@ -30,16 +30,20 @@ __device__ __forceinline__ void zou_he(float (&v)[19], const Coef& c) {
 // RAW: return the stored values themselves (the deviations h = f - w of the shifted forms,
 // for collide<.., DEV = true>); the Zou-He inlet is applied to f = h + w and shifted back.
 // For float32 storage RAW changes nothing.
-template <int S, bool PULL, bool RAW = false>
+// IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32),
+// one wide multiply-add per address instead of 64-bit index arithmetic.
+template <int S, bool PULL, bool RAW = false, bool IDX32 = false>
 __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f, const Grid& g,
                                        const Coef& c, int x, int y, int z, float (&v)[19]) {
     using P = Pop<S>;
+    using I = typename std::conditional<IDX32, unsigned, long long>::type;
     constexpr bool kRaw = RAW && P::kShifted;
+    const I plane = (I)g.plane;
     if (!PULL) {
-        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        const I cell = ((I)z * (I)g.ny + (I)y) * (I)g.pitch + (I)x;
 #pragma unroll
         for (int q = 0; q < 19; ++q)
-            v[q] = kRaw ? P::ld_raw(f + q * g.plane + cell) : P::ld(f + q * g.plane + cell, q);
+            v[q] = kRaw ? P::ld_raw(f + ((I)q * plane + cell)) : P::ld(f + ((I)q * plane + cell), q);
         return;
     }
     const int xe = (x == g.nx - 1) ? g.nx - 2 : x;  // outlet: copy of column Nx-2
@@ -55,7 +59,7 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
         if (ex(q) == 1 && xe == 0) {
             v[q] = 0.0f;  // inlet unknown, rebuilt by Zou-He below
         } else {
-            const typename P::T* p = f + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + sx;
+            const typename P::T* p = f + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)sx);
             v[q] = kRaw ? P::ld_raw(p) : P::ld(p, q);
         }
     }
@@ -73,11 +77,12 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
 }
 
 // Store a population vector produced by gather<.., RAW = true> + collide<.., DEV = kShifted>.
-template <int S>
+template <int S, bool IDX32 = false>
 __device__ __forceinline__ void store_raw(typename Pop<S>::T* __restrict__ f, const Grid& g,
                                           long long cell, const float (&v)[19]) {
+    using I = typename std::conditional<IDX32, unsigned, long long>::type;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Pop<S>::st_raw(f + q * g.plane + cell, v[q]);
+    for (int q = 0; q < 19; ++q) Pop<S>::st_raw(f + ((I)q * (I)g.plane + (I)cell), v[q]);
 }
 
 // Zeroth, first and second raw moments of a population vector.
