@@ -32,7 +32,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=400)
+    p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
@@ -77,11 +77,16 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        self.first = []
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # the timed region starts once sampling runs (nvidia-smi takes a while to start)
+            line = self.proc.stdout.readline()
+            if line.strip():
+                self.first.append(line)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -95,7 +100,8 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+            # the sample that signalled the start was taken before the timed region
+            self.lines = [ln for ln in out.splitlines() if ln.strip()] or self.first
         return False
 
     def summary(self):
@@ -192,10 +198,21 @@ def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
+    tuning = ens.tuning()
+    # roofline of the batched bulk pass alone (timed at creation by the autotuner): the
+    # algorithmic bytes of all members' cells (force-box cells included, an upper bound on
+    # the cells it processes) over its time
+    peak, peak_kind = measured_peak()
+    alg = BYTES_PER_CELL[storage] * ens.cells
+    bulk_gbs = alg / (tuning["bulk_us"] * 1e-6) / 1e9 if tuning["bulk_us"] > 0 else None
     out = {"instances": n, "cells": ens.cells, "markers": sum(c.n_markers for c in cases),
            "steps": steps, "ms_per_step": ms / steps,
            "mlups": ens.cells * steps / (ms / 1e3) / 1e6, "storage": storage,
-           "tuning": ens.tuning()}
+           "tuning": tuning,
+           "bulk_roofline": {"achieved": bulk_gbs, "peak": peak, "unit": "GB/s",
+                             "frac": bulk_gbs / peak if bulk_gbs else None,
+                             "algorithmic_bytes": alg, "how": "bulk pass alone at creation, "
+                             "all members' cells"}}
     ens.close()
     return out
 

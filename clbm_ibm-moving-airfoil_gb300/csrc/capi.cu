@@ -888,6 +888,7 @@ struct clbm_ensemble {
     long long ntiles = 0;
     int bx = 128;            // bulk tile width (cells)
     int grid = 0;            // persistent bulk blocks
+    float bulk_ms = 0.f;     // time of one bulk pass of the chosen schedule at creation
     int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
     bool local = true, macro_full = true;
@@ -974,6 +975,7 @@ int ens_tune(clbm_ensemble* e) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     e->grid = best_grid;
+    e->bulk_ms = best / 3.0f;
     return ens_upload(e, best_bx);
 }
 
@@ -1149,11 +1151,12 @@ int clbm_ensemble_stream(const clbm_ensemble* e, void** out) {
 }
 
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
-                         int64_t* tiles) {
+                         int64_t* tiles, float* bulk_ms) {
     if (!e) return fail(CLBM_ERR_ARG, "clbm_ensemble_tuning: null ensemble");
     if (tile_width) *tile_width = e->bx;
     if (blocks) *blocks = e->grid;
     if (tiles) *tiles = e->ntiles;
+    if (bulk_ms) *bulk_ms = e->bulk_ms;
     return CLBM_OK;
 }
 

@@ -338,9 +338,12 @@ class Ensemble:
         return p.value or 0
 
     def tuning(self):
-        w, b, t = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
-        check(lib().clbm_ensemble_tuning(self._h, ctypes.byref(w), ctypes.byref(b), ctypes.byref(t)))
-        return dict(tile_width=w.value, blocks=b.value, tiles=t.value)
+        """Bulk-pass schedule chosen at creation and the time of one bulk pass of all
+        members with it, alone (bulk_us)."""
+        w, b, t, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_float()
+        check(lib().clbm_ensemble_tuning(self._h, ctypes.byref(w), ctypes.byref(b), ctypes.byref(t),
+                                         ctypes.byref(ms)))
+        return dict(tile_width=w.value, blocks=b.value, tiles=t.value, bulk_us=round(ms.value * 1e3, 2))
 
     def synchronize(self):
         for s in self.sims:
