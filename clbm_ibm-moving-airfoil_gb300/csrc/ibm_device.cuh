@@ -144,6 +144,11 @@ __device__ __forceinline__ void ibm_interp_marker(const IbmArrays& a, const Grid
     }
 }
 
+// Fire-and-forget 64-bit add to a global force field (a reduction: no value comes back).
+__device__ __forceinline__ void red_add(long long* p, long long v) {
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // Spreading contribution of tap h in 64-bit fixed point: the float32 product f * w
 // (airfoil_moving.py:212-214) scaled by 2^40, so sums do not depend on their order.
 __device__ __forceinline__ long long spread_q(float f, float w) {
@@ -160,8 +165,8 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
     for (int h = 0; h < 2; ++h) {
         if (tp.wt[h] != 0.0f) {
             const long long c = ((long long)pmod(tp.kr[h], g.nz) * g.ny + pmod(tp.jr[h], g.ny)) * g.pitch + tp.ii[h];
-            atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)spread_q(tp.fx, tp.wt[h]));
-            atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)spread_q(tp.fy, tp.wt[h]));
+            red_add(a.fx + c, spread_q(tp.fx, tp.wt[h]));
+            red_add(a.fy + c, spread_q(tp.fy, tp.wt[h]));
         }
     }
 }
@@ -216,8 +221,8 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
             for (int h = 0; h < 2; ++h) {
                 if (tp[i].wt[h] != 0.0f) {
                     const long long c = ((long long)pmod(tp[i].kr[h], g.nz) * g.ny + pmod(tp[i].jr[h], g.ny)) * g.pitch + tp[i].ii[h];
-                    atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)spread_q(tp[i].fx, tp[i].wt[h]));
-                    atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)spread_q(tp[i].fy, tp[i].wt[h]));
+                    red_add(a.fx + c, spread_q(tp[i].fx, tp[i].wt[h]));
+                    red_add(a.fy + c, spread_q(tp[i].fy, tp[i].wt[h]));
                 }
             }
         }
@@ -249,8 +254,8 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
         const int r = t / li;
         const int y = pmod(j0 + r % lj, g.ny), z = pmod(k0 + r / lj, g.nz);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
-        if (vx) atomicAdd(reinterpret_cast<unsigned long long*>(a.fx + c), (unsigned long long)vx);
-        if (vy) atomicAdd(reinterpret_cast<unsigned long long*>(a.fy + c), (unsigned long long)vy);
+        if (vx) red_add(a.fx + c, vx);
+        if (vy) red_add(a.fy + c, vy);
     }
 }
 
