@@ -1048,7 +1048,8 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         clbm_ibm* b = e->ibm.back();
         if (b) {
             e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + 255) / 256);
-            e->max_spread_blocks = std::max(e->max_spread_blocks, (int)(((long long)b->a.n * 32 + 255) / 256));
+            const long long warps = ((long long)b->a.n + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp;
+            e->max_spread_blocks = std::max(e->max_spread_blocks, (int)((warps * 32 + 255) / 256));
         }
     }
     {

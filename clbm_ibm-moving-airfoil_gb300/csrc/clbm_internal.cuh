@@ -323,6 +323,7 @@ void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
                         const MotionF& mf, const clbm_motion& m, cudaStream_t st);
 // Zero the previous call's force band and compute the macro fields on this call's band.
 constexpr int kFinishBlocks = 64;    // force-sum blocks: few, so they leave the SMs to the bulk pass
+constexpr int kSpreadMarkersPerWarp = 2;   // markers interpolated and spread by one warp
 void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
                          IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,

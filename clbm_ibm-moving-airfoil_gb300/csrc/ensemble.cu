@@ -25,9 +25,9 @@ __global__ void __launch_bounds__(kMarkerBlock) kb_markers(const EnsDesc* __rest
 
 __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
-    const int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5;
-    if (!D.has_ibm || m >= D.a.n) return;  // whole warp
-    ibm_interp_spread_body(D.a, D.g, m, threadIdx.x & 31);
+    const int m0 = ((blockIdx.x * kSpreadBlock + threadIdx.x) >> 5) * kSpreadMarkersPerWarp;
+    if (!D.has_ibm || m0 >= D.a.n) return;  // whole warp
+    ibm_interp_spread_body<kSpreadMarkersPerWarp>(D.a, D.g, m0, threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread_tiled(const EnsDesc* __restrict__ d) {
@@ -202,8 +202,9 @@ void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     if (blocks < 1) return;
     if (spread_tiled()) {
-        // blocks of the warp-per-marker form cover 8 markers; a tiled block covers 32
-        kb_interp_spread_tiled<<<dim3((blocks + 3) / 4, n), kSpreadBlock, 0, st>>>(d);
+        // a block of the direct form covers 8 * kSpreadMarkersPerWarp markers; a tiled block 32
+        kb_interp_spread_tiled<<<dim3((blocks * 8 * kSpreadMarkersPerWarp + kTileMarkers - 1) / kTileMarkers, n),
+                                 kSpreadBlock, 0, st>>>(d);
         return;
     }
     kb_interp_spread<<<dim3(blocks, n), kSpreadBlock, 0, st>>>(d);

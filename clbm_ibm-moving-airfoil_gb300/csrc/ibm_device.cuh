@@ -102,48 +102,6 @@ struct MarkerTaps {
     float fx, fy;     // clipped marker force
 };
 
-// One warp per marker m: Peskin interpolation of the current velocity (two stencil taps
-// per lane, warp-shuffle sums; airfoil_moving.py:142-170) and the marker force clip
-// (airfoil_moving.py:175-183); the taps are kept for spreading.
-__device__ __forceinline__ void ibm_interp_marker(const IbmArrays& a, const Grid& g, int m, int lane,
-                                                  MarkerTaps& tp) {
-    const float xk = a.X[m], yk = a.Y[m], zk = a.Z[m];
-    const int ib = (int)floorf(xk) - 1, jb = (int)floorf(yk) - 1, kb = (int)floorf(zk) - 1;
-    float us = 0.f, vs = 0.f;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        // tap t: di fastest, so four neighbouring lanes read four consecutive x
-        const int t = lane + 32 * h;
-        const int di = t & 3, dj = (t >> 2) & 3, dk = t >> 4;
-        const int ii = min(max(ib + di, 0), g.nx - 1);   // x clamped (airfoil_moving.py:158)
-        const int jj = pmod(jb + dj, g.ny);              // y, z periodic indices; the weight
-        const int kk = pmod(kb + dk, g.nz);              // uses the wrapped index, as there
-        const float w = phi1d((float)ii - xk) * phi1d((float)jj - yk) * phi1d((float)kk - zk);
-        const long long c = ((long long)kk * g.ny + jj) * g.pitch + ii;
-        tp.wt[h] = w;
-        tp.ii[h] = ii;
-        tp.jr[h] = jb + dj;
-        tp.kr[h] = kb + dk;
-        if (w != 0.0f) {
-            us += a.ux[c] * w;
-            vs += a.uy[c] * w;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        us += __shfl_xor_sync(0xffffffffu, us, o);
-        vs += __shfl_xor_sync(0xffffffffu, vs, o);
-    }
-    tp.fx = fmaxf(-0.05f, fminf(0.05f, -(us - a.VX[m])));
-    tp.fy = fmaxf(-0.05f, fminf(0.05f, -(vs - a.VY[m])));
-    if (lane == 0) {
-        a.Uk[m] = us;
-        a.Vk[m] = vs;
-        a.FXk[m] = tp.fx;
-        a.FYk[m] = tp.fy;
-    }
-}
-
 // Fire-and-forget 64-bit add to a global force field (a reduction: no value comes back).
 __device__ __forceinline__ void red_add(long long* p, long long v) {
     asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -155,25 +113,102 @@ __device__ __forceinline__ long long spread_q(float f, float w) {
     return __float2ll_rn(f * w * kForceScale);
 }
 
-// One warp per marker: interpolation, then spreading with one global atomic per tap and
-// component.
-__device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const Grid& g, int m,
-                                                       int lane) {
-    MarkerTaps tp;
-    ibm_interp_marker(a, g, m, lane, tp);
+// Markers m0 .. m0 + K - 1 (those below a.n: has[k], warp-uniform) on one warp: Peskin
+// interpolation of the current velocity (two stencil taps per lane, warp-shuffle sums;
+// airfoil_moving.py:142-170) and the marker force clip (airfoil_moving.py:175-183). The
+// velocity gathers of all K markers are issued before any of their sums, so a warp has K
+// times the loads in flight; the taps are kept for spreading.
+template <int K>
+__device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Grid& g, int m0, int lane,
+                                                   MarkerTaps (&tp)[K], bool (&has)[K]) {
+    float xk[K], yk[K], zk[K], us[K], vs[K], uxv[K][2], uyv[K][2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        if (tp.wt[h] != 0.0f) {
-            const long long c = ((long long)pmod(tp.kr[h], g.nz) * g.ny + pmod(tp.jr[h], g.ny)) * g.pitch + tp.ii[h];
-            red_add(a.fx + c, spread_q(tp.fx, tp.wt[h]));
-            red_add(a.fy + c, spread_q(tp.fy, tp.wt[h]));
+    for (int k = 0; k < K; ++k) {
+        has[k] = m0 + k < a.n;
+        const int m = has[k] ? m0 + k : 0;   // launched only with a.n >= 1
+        xk[k] = a.X[m]; yk[k] = a.Y[m]; zk[k] = a.Z[m];
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int ib = (int)floorf(xk[k]) - 1, jb = (int)floorf(yk[k]) - 1, kb = (int)floorf(zk[k]) - 1;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            // tap t: di fastest, so four neighbouring lanes read four consecutive x
+            const int t = lane + 32 * h;
+            const int di = t & 3, dj = (t >> 2) & 3, dk = t >> 4;
+            const int ii = min(max(ib + di, 0), g.nx - 1);   // x clamped (airfoil_moving.py:158)
+            const int jj = pmod(jb + dj, g.ny);              // y, z periodic indices; the weight
+            const int kk = pmod(kb + dk, g.nz);              // uses the wrapped index, as there
+            const float w = phi1d((float)ii - xk[k]) * phi1d((float)jj - yk[k]) * phi1d((float)kk - zk[k]);
+            const long long c = ((long long)kk * g.ny + jj) * g.pitch + ii;
+            tp[k].wt[h] = w;
+            tp[k].ii[h] = ii;
+            tp[k].jr[h] = jb + dj;
+            tp[k].kr[h] = kb + dk;
+            uxv[k][h] = (w != 0.0f) ? a.ux[c] : 0.0f;
+            uyv[k][h] = (w != 0.0f) ? a.uy[c] : 0.0f;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        us[k] = 0.f;
+        vs[k] = 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (tp[k].wt[h] != 0.0f) {
+                us[k] += uxv[k][h] * tp[k].wt[h];
+                vs[k] += uyv[k][h] * tp[k].wt[h];
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            us[k] += __shfl_xor_sync(0xffffffffu, us[k], o);
+            vs[k] += __shfl_xor_sync(0xffffffffu, vs[k], o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!has[k]) continue;
+        const int m = m0 + k;
+        tp[k].fx = fmaxf(-0.05f, fminf(0.05f, -(us[k] - a.VX[m])));
+        tp[k].fy = fmaxf(-0.05f, fminf(0.05f, -(vs[k] - a.VY[m])));
+        if (lane == 0) {
+            a.Uk[m] = us[k];
+            a.Vk[m] = vs[k];
+            a.FXk[m] = tp[k].fx;
+            a.FYk[m] = tp[k].fy;
+        }
+    }
+}
+
+// K markers per warp: interpolation, then spreading with one global reduction per tap and
+// component.
+template <int K>
+__device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const Grid& g, int m0,
+                                                       int lane) {
+    MarkerTaps tp[K];
+    bool has[K];
+    ibm_interp_markers<K>(a, g, m0, lane, tp, has);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!has[k]) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (tp[k].wt[h] != 0.0f) {
+                const long long c = ((long long)pmod(tp[k].kr[h], g.nz) * g.ny + pmod(tp[k].jr[h], g.ny)) * g.pitch + tp[k].ii[h];
+                red_add(a.fx + c, spread_q(tp[k].fx, tp[k].wt[h]));
+                red_add(a.fy + c, spread_q(tp[k].fy, tp[k].wt[h]));
+            }
         }
     }
 }
 
 // Spreading through a shared-memory tile: a block of 8 warps takes kTileMarkers
 // consecutive markers (a body's markers are stored in surface order, so they lie close
-// together), interpolates them (a warp per marker, as above), accumulates their int64
+// together), interpolates them (four per warp, as above), accumulates their int64
 // contributions in a tile over the box their stencils cover (y, z before the wrap) and
 // adds each touched cell to the global fields once. The sums are the same integers as with
 // one global atomic per tap. A chunk whose box exceeds the tile (or spans the lattice in
@@ -190,12 +225,11 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
     __syncthreads();
     MarkerTaps tp[kTileMarkersPerWarp];
     bool has[kTileMarkersPerWarp];
+    ibm_interp_markers<kTileMarkersPerWarp>(a, g, chunk * kTileMarkers + warp * kTileMarkersPerWarp,
+                                            lane, tp, has);
 #pragma unroll
     for (int i = 0; i < kTileMarkersPerWarp; ++i) {
-        const int m = chunk * kTileMarkers + warp * kTileMarkersPerWarp + i;
-        has[i] = m < a.n;   // warp-uniform
         if (has[i]) {
-            ibm_interp_marker(a, g, m, lane, tp[i]);
             // taps 0 and 63 hold the stencil's corners (di, dj, dk = 0 and 3)
             if (lane == 0) {
                 atomicMin(&sb[0], tp[i].ii[0]);

@@ -31,9 +31,9 @@ __global__ void __launch_bounds__(kMarkerBlock) k_ibm_markers(IbmArrays a, Grid 
 }
 
 __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a, Grid g) {
-    const int m = (blockIdx.x * kSpreadBlock + threadIdx.x) >> 5;
-    if (m >= a.n) return;  // whole warp leaves together
-    ibm_interp_spread_body(a, g, m, threadIdx.x & 31);
+    const int m0 = ((blockIdx.x * kSpreadBlock + threadIdx.x) >> 5) * kSpreadMarkersPerWarp;
+    if (m0 >= a.n) return;  // whole warp leaves together
+    ibm_interp_spread_body<kSpreadMarkersPerWarp>(a, g, m0, threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread_tiled(IbmArrays a, Grid g) {
@@ -67,7 +67,7 @@ void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st
         if (blocks > 0) k_ibm_interp_spread_tiled<<<blocks, kSpreadBlock, 0, st>>>(a, g);
         return;
     }
-    const long long threads = (long long)a.n * 32;
+    const long long threads = (long long)(a.n + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp * 32;
     const int blocks = (int)((threads + kSpreadBlock - 1) / kSpreadBlock);
     if (blocks == 0) return;
     k_ibm_interp_spread<<<blocks, kSpreadBlock, 0, st>>>(a, g);
