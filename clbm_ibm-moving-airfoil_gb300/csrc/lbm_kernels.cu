@@ -44,14 +44,34 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
 
 // ------------------------------------------------------------------ 16-bit pair kernel
 // Two cells per thread (Pair, pair_body in lbm_device.cuh).
-constexpr int kPX = 128;  // threads per block of the pair kernel (256 cells along x)
-
-template <int S, bool PULL, int FMODE>
-__global__ void __launch_bounds__(kPX, 8) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
-                                                             typename Pair<S>::T* __restrict__ fout,
-                                                             Grid g, Coef c, ForceArgs fa) {
-    pair_body<S, PULL, FMODE>(fin, fout, g, c, fa, 2 * (blockIdx.x * kPX + threadIdx.x), blockIdx.y,
+// PX threads per block (2 PX cells along x): 64 or 128, whichever leaves fewer idle lanes
+// at the row ends (pair_threads).
+template <int S, bool PULL, int FMODE, int PX>
+__global__ void __launch_bounds__(PX, 1024 / PX) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
+                                                                    typename Pair<S>::T* __restrict__ fout,
+                                                                    Grid g, Coef c, ForceArgs fa) {
+    pair_body<S, PULL, FMODE>(fin, fout, g, c, fa, 2 * (blockIdx.x * PX + threadIdx.x), blockIdx.y,
                               blockIdx.z);
+}
+
+static int pair_threads(int nx) {
+    const int w64 = (nx + 127) / 128 * 128 - nx, w128 = (nx + 255) / 256 * 256 - nx;
+    return w64 < w128 ? 64 : 128;
+}
+
+template <int S, bool PULL, int PX>
+static void pair_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                        const ForceArgs& fa, cudaStream_t st) {
+    using T = typename Pair<S>::T;
+    const dim3 grid((g.nx + 2 * PX - 1) / (2 * PX), g.ny, g.nz);
+    if (fmode == kForceNone)
+        k_stream_collide_pair<S, PULL, kForceNone, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceBand)
+        k_stream_collide_pair<S, PULL, kForceBand, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceSkipBand)
+        k_stream_collide_pair<S, PULL, kForceSkipBand, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else
+        k_stream_collide_pair<S, PULL, kForceDense, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
 }
 
 // ------------------------------------------------------------------ TMA-staged kernel
@@ -475,15 +495,8 @@ static void sc_launch(int fmode, int variant, const void* fin, void* fout, const
         return;
     }
     if constexpr (S != CLBM_STORE_F32) if (variant == kVariantPair) {
-        const dim3 grid((g.nx + 2 * kPX - 1) / (2 * kPX), g.ny, g.nz);
-        if (fmode == kForceNone)
-            k_stream_collide_pair<S, PULL, kForceNone><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-        else if (fmode == kForceBand)
-            k_stream_collide_pair<S, PULL, kForceBand><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-        else if (fmode == kForceSkipBand)
-            k_stream_collide_pair<S, PULL, kForceSkipBand><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-        else
-            k_stream_collide_pair<S, PULL, kForceDense><<<grid, kPX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        if (pair_threads(g.nx) == 64) pair_launch<S, PULL, 64>(fmode, fin, fout, g, c, fa, st);
+        else pair_launch<S, PULL, 128>(fmode, fin, fout, g, c, fa, st);
         return;
     }
     if (fmode == kForceNone)
