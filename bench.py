@@ -125,6 +125,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x, dist):
+    """The largest value of x over all ranks (the slowest replica times the job); x itself
+    without a process group. NCCL reduces on the rank's GPU, gloo on the host."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_mlups(cells, steps, world, ms):
+    """Whole-job MLUPS: every rank steps its own replica of `cells` cells; `ms` is the
+    slowest rank's time for `steps` steps."""
+    return cells * steps * world / (ms / 1e3) / 1e6
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -296,11 +314,8 @@ def run_gpu(args, rank, world, local):
     prof = solver.profile_read()
     solver.profile(False)
     gpu_launches = prof["total_launches"] - launches0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cfg.cells * args.steps * world / (ms / 1e3) / 1e6
+    ms = max_over_ranks(ms, dist)
+    value = aggregate_mlups(cfg.cells, args.steps, world, ms)
     st = solver.check()
 
     # ---- graph-replayed loop (same work, one graph launch per eight steps)
