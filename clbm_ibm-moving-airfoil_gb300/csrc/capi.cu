@@ -888,6 +888,17 @@ struct clbm_ensemble {
     long long ntiles = 0;
     int bx = 128;            // bulk tile width (cells)
     int grid = 0;            // persistent bulk blocks
+    // 16-bit forms: instances grouped by row width, one row per block (rows = true when
+    // the autotuner chose it)
+    struct Group {
+        EnsDesc* d = nullptr;
+        long long* tile0 = nullptr;
+        int n = 0;
+        long long ntiles = 0;
+        int threads = 0;
+    };
+    std::vector<Group> groups;
+    bool rows = false;
     float bulk_ms = 0.f;     // time of one bulk pass of the chosen schedule at creation
     int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
@@ -901,6 +912,69 @@ struct clbm_ensemble {
 
 namespace {
 
+// Descriptor of member i (tile0 left to the caller).
+EnsDesc member_desc(const clbm_ensemble* e, int i) {
+    const clbm_solver* s = e->s[i];
+    EnsDesc D{};
+    D.g = s->g;
+    D.c = s->c;
+    D.f[0] = s->f[0];
+    D.f[1] = s->f[1];
+    D.rho = s->rho; D.ux = s->ux; D.uy = s->uy; D.uz = s->uz;
+    D.has_ibm = e->ibm[i] != nullptr;
+    if (D.has_ibm) D.a = e->ibm[i]->a;
+    D.m = e->m[i];
+    D.cells = s->g.nx * s->g.ny * s->g.nz;
+    return D;
+}
+
+// 16-bit forms: members grouped by the threads a whole row needs (two cells each, a
+// multiple of 32, rows up to 512 cells); each group's descriptors list its members with
+// tiles = rows. No groups when a row is wider.
+int ens_groups(clbm_ensemble* e) {
+    if (e->storage == CLBM_STORE_F32) return CLBM_OK;
+    std::vector<int> th(e->n);
+    for (int i = 0; i < e->n; ++i) {
+        const int nx = e->s[i]->g.nx;
+        if (nx > 512) return CLBM_OK;
+        th[i] = (nx + 63) / 64 * 32;
+    }
+    std::vector<int> widths(th);
+    std::sort(widths.begin(), widths.end());
+    widths.erase(std::unique(widths.begin(), widths.end()), widths.end());
+    for (int w : widths) {
+        std::vector<EnsDesc> h;
+        std::vector<long long> t0;
+        long long tiles = 0;
+        for (int i = 0; i < e->n; ++i) {
+            if (th[i] != w) continue;
+            EnsDesc D = member_desc(e, i);
+            D.tile0 = tiles;
+            t0.push_back(tiles);
+            tiles += (long long)D.g.ny * D.g.nz;
+            h.push_back(D);
+        }
+        clbm_ensemble::Group gr;
+        gr.n = (int)h.size();
+        gr.ntiles = tiles;
+        gr.threads = w;
+        e->groups.push_back(gr);
+        clbm_ensemble::Group& G = e->groups.back();
+        CK(cudaMalloc(&G.d, sizeof(EnsDesc) * G.n));
+        CK(cudaMalloc(&G.tile0, sizeof(long long) * G.n));
+        CK(cudaMemcpyAsync(G.d, h.data(), sizeof(EnsDesc) * G.n, cudaMemcpyHostToDevice, e->st));
+        CK(cudaMemcpyAsync(G.tile0, t0.data(), sizeof(long long) * G.n, cudaMemcpyHostToDevice, e->st));
+    }
+    CK(cudaStreamSynchronize(e->st));
+    return CLBM_OK;
+}
+
+void ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
+    for (const auto& G : e->groups)
+        launch_ens_bulk_rows(e->storage, pull, G.threads, G.d, G.tile0, G.n, G.ntiles, e->cur,
+                             (int)std::min<long long>(G.ntiles, 1LL << 30), st);
+}
+
 // Device descriptors for tile width bx; returns the number of bulk tiles.
 int ens_upload(clbm_ensemble* e, int bx) {
     std::vector<EnsDesc> h(e->n);
@@ -909,16 +983,7 @@ int ens_upload(clbm_ensemble* e, int bx) {
     for (int i = 0; i < e->n; ++i) {
         clbm_solver* s = e->s[i];
         EnsDesc& D = h[i];
-        D = EnsDesc{};
-        D.g = s->g;
-        D.c = s->c;
-        D.f[0] = s->f[0];
-        D.f[1] = s->f[1];
-        D.rho = s->rho; D.ux = s->ux; D.uy = s->uy; D.uz = s->uz;
-        D.has_ibm = e->ibm[i] != nullptr;
-        if (D.has_ibm) D.a = e->ibm[i]->a;
-        D.m = e->m[i];
-        D.cells = s->g.nx * s->g.ny * s->g.nz;
+        D = member_desc(e, i);
         D.tile0 = tiles;
         t0[i] = tiles;
         // a tile is a run of bx consecutive cells (float32) or a segment of bx cells of one
@@ -972,10 +1037,27 @@ int ens_tune(clbm_ensemble* e) {
             }
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     e->grid = best_grid;
     e->bulk_ms = best / 3.0f;
+    e->rows = false;
+    if (int rc = ens_groups(e)) return rc;
+    if (!e->groups.empty()) {   // one row per block, instances grouped by row width
+        ens_bulk_rows(e, true, e->st);
+        CK(cudaEventRecord(e0, e->st));
+        for (int k = 0; k < 3; ++k) ens_bulk_rows(e, true, e->st);
+        CK(cudaEventRecord(e1, e->st));
+        CK(cudaEventSynchronize(e1));
+        CK_LAUNCH();
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        e->launches += 4 * (long long)e->groups.size();
+        if (ms < best) {
+            e->rows = true;
+            e->bulk_ms = ms / 3.0f;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     return ens_upload(e, best_bx);
 }
 
@@ -991,8 +1073,9 @@ int ens_step(clbm_ensemble* e) {
     launch_ens_interp_spread(e->d_desc, e->n, e->max_spread_blocks, e->st);
     launch_ens_finish(e->d_desc, e->n, e->st);
     CK(cudaStreamWaitEvent(e->st2, e->ev_box, 0));
-    launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
-                    e->grid, e->st2);
+    if (e->rows) ens_bulk_rows(e, pull, e->st2);
+    else launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
+                         e->grid, e->st2);
     CK(cudaEventRecord(e->ev_bulk, e->st2));
     launch_ens_box_flat(e->storage, pull, e->d_desc, e->n, off_new, e->cur, e->flat_grid, e->st);
     CK(cudaStreamWaitEvent(e->st, e->ev_bulk, 0));
@@ -1154,9 +1237,11 @@ int clbm_ensemble_stream(const clbm_ensemble* e, void** out) {
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
                          int64_t* tiles, float* bulk_ms) {
     if (!e) return fail(CLBM_ERR_ARG, "clbm_ensemble_tuning: null ensemble");
-    if (tile_width) *tile_width = e->bx;
-    if (blocks) *blocks = e->grid;
-    if (tiles) *tiles = e->ntiles;
+    long long rows = 0;
+    for (const auto& G : e->groups) rows += G.ntiles;
+    if (tile_width) *tile_width = e->rows ? 0 : e->bx;
+    if (blocks) *blocks = e->rows ? (int)std::min<long long>(rows, 1LL << 30) : e->grid;
+    if (tiles) *tiles = e->rows ? rows : e->ntiles;
     if (bulk_ms) *bulk_ms = e->bulk_ms;
     return CLBM_OK;
 }
@@ -1167,6 +1252,10 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     if (e->st2) cudaStreamSynchronize(e->st2);
     ens_free_graph(e);
     if (e->d_desc) cudaFree(e->d_desc);
+    for (auto& G : e->groups) {
+        if (G.d) cudaFree(G.d);
+        if (G.tile0) cudaFree(G.tile0);
+    }
     if (e->d_tile0) cudaFree(e->d_tile0);
     if (e->d_off) cudaFree(e->d_off);
     cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};

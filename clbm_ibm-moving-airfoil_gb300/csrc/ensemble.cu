@@ -187,6 +187,52 @@ kb_bulk(const EnsDesc* __restrict__ d, const long long* __restrict__ tile0, int 
     }
 }
 
+// 16-bit forms, one row per block: tile t of a group is row (t - tile0[i]) of instance i
+// (y fastest), the block's warps cover the row with two cells per thread (blockDim.x >=
+// Nx / 2, the smallest multiple of 32). Instances are grouped by that width, one launch per
+// group, so a 150-, 200- or 300-cell row costs 3, 4 or 5 warps and the row (y, z) stays
+// uniform across the block.
+template <int S, bool PULL>
+__global__ void __launch_bounds__(256, 4) kb_bulk_row(const EnsDesc* __restrict__ d,
+                                                    const long long* __restrict__ tile0, int n,
+                                                    long long ntiles, int parity) {
+    using T = typename Pop<S>::T;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(tile0 + mid) <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const EnsDesc& D = d[lo];
+        const Grid g = D.g;
+        const Coef c = D.c;
+        const int r = (int)(t - D.tile0);   // row z * ny + y
+        const int y = r % g.ny, z = r / g.ny;
+        const T* fin = (const T*)D.f[parity];
+        T* fout = (T*)D.f[parity ^ 1];
+        ForceArgs fa{};
+        if (D.has_ibm) {
+            fa.dev = D.a.dev;
+            fa.slot = (int)(D.a.dev->cur & 1);
+            pair_body<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
+        } else {
+            pair_body<S, PULL, kForceNone>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
+        }
+    }
+}
+
+void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
+                          int n, long long ntiles, int parity, int grid, cudaStream_t st) {
+    if (storage == CLBM_STORE_F16S) {
+        if (pull) kb_bulk_row<CLBM_STORE_F16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        else kb_bulk_row<CLBM_STORE_F16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+    } else if (storage == CLBM_STORE_BF16S) {
+        if (pull) kb_bulk_row<CLBM_STORE_BF16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        else kb_bulk_row<CLBM_STORE_BF16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+    }
+}
+
 #define CLBM_ENS_STORE(storage, ...)                                                         \
     switch (storage) {                                                                       \
         case CLBM_STORE_F32: { constexpr int S_ = CLBM_STORE_F32; __VA_ARGS__; } break;     \

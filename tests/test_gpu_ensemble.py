@@ -30,7 +30,7 @@ def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, gra
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
     t = ens.tuning()
-    assert t["tile_width"] in (128, 256) and t["blocks"] > 0 and t["tiles"] > 0
+    assert t["tile_width"] in (0, 128, 256) and t["blocks"] > 0 and t["tiles"] > 0
     for cfg, member in zip(cases, ens.sims):
         alone = pkg.Simulation(cfg)
         alone.run(24, graph=graph)
