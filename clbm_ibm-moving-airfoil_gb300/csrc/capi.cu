@@ -1051,7 +1051,9 @@ int ens_tune(clbm_ensemble* e) {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         e->launches += 4 * (long long)e->groups.size();
-        if (ms < best) {
+        // CLBM_ENS_ROWS=1 / 0 forces / forbids the row mode (tests); default: the faster
+        const int force = knob("CLBM_ENS_ROWS", -1);
+        if (force == 1 || (force != 0 && ms < best)) {
             e->rows = true;
             e->bulk_ms = ms / 3.0f;
         }

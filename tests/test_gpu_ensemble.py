@@ -22,10 +22,14 @@ def _cases(pkg, storage, n=5, lattices=SMALL):
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", ["cell", "pair"])
 @pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
-def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant, lattices):
-    """The single runs use either full-grid kernel; all variants give the same bits."""
+@pytest.mark.parametrize("rows", ["1", "0"])
+def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant, lattices,
+                                            rows):
+    """The single runs use either full-grid kernel; all variants give the same bits; the
+    16-bit ensemble bulk pass with one row per block (rows = 1) or row segments."""
     pkg = built_pkg
     monkeypatch.setenv("CLBM_KERNEL", variant)
+    monkeypatch.setenv("CLBM_ENS_ROWS", rows)
     cases = _cases(pkg, storage, lattices=lattices)
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
