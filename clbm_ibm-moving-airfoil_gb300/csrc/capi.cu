@@ -888,8 +888,8 @@ struct clbm_ensemble {
     long long ntiles = 0;
     int bx = 128;            // bulk tile width (cells)
     int grid = 0;            // persistent bulk blocks
-    // 16-bit forms: instances grouped by row width, one row per block (rows = true when
-    // the autotuner chose it)
+    // instances grouped by row width, one row per block (rows = true when the autotuner
+    // chose it)
     struct Group {
         EnsDesc* d = nullptr;
         long long* tile0 = nullptr;
@@ -928,16 +928,16 @@ EnsDesc member_desc(const clbm_ensemble* e, int i) {
     return D;
 }
 
-// 16-bit forms: members grouped by the threads a whole row needs (two cells each, a
-// multiple of 32, rows up to 512 cells); each group's descriptors list its members with
-// tiles = rows. No groups when a row is wider.
+// Members grouped by the threads a whole row needs (a multiple of 32; two cells per thread
+// in the 16-bit forms, one in float32; rows up to 512 cells); each group's descriptors list
+// its members with tiles = rows. No groups when a row is wider.
 int ens_groups(clbm_ensemble* e) {
-    if (e->storage == CLBM_STORE_F32) return CLBM_OK;
+    const bool f32 = e->storage == CLBM_STORE_F32;   // one cell per thread, rows up to 512
     std::vector<int> th(e->n);
     for (int i = 0; i < e->n; ++i) {
         const int nx = e->s[i]->g.nx;
         if (nx > 512) return CLBM_OK;
-        th[i] = (nx + 63) / 64 * 32;
+        th[i] = f32 ? (nx + 31) / 32 * 32 : (nx + 63) / 64 * 32;
     }
     std::vector<int> widths(th);
     std::sort(widths.begin(), widths.end());

@@ -356,8 +356,9 @@ void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t 
 void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st);
 void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,
                      int n, long long ntiles, int parity, int grid, cudaStream_t st);
-// 16-bit forms, one row per block of `threads` (>= Nx / 2, a multiple of 32, <= 256) over a
-// group of instances of that row width: tiles are rows, tile0 per instance of the group.
+// One row per block of `threads` (a multiple of 32: >= Nx / 2 in the 16-bit forms, <= 256;
+// >= Nx in float32, <= 512) over a group of instances of that row width: tiles are rows,
+// tile0 per instance of the group.
 void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
                           int n, long long ntiles, int parity, int grid, cudaStream_t st);
 // Force-box cells of all members as one flat list (offsets per member, n + 1 each), then

@@ -222,9 +222,44 @@ __global__ void __launch_bounds__(256, 4) kb_bulk_row(const EnsDesc* __restrict_
     }
 }
 
+// Float32, one row per block: one cell per thread, blockDim.x >= Nx (a multiple of 32).
+template <bool PULL>
+__global__ void __launch_bounds__(512) kb_bulk_row_f32(const EnsDesc* __restrict__ d,
+                                                       const long long* __restrict__ tile0, int n,
+                                                       long long ntiles, int parity) {
+    using T = typename Pop<CLBM_STORE_F32>::T;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int lo = 0, hi = n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(tile0 + mid) <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const EnsDesc& D = d[lo];
+        const Grid g = D.g;
+        const Coef c = D.c;
+        const int r = (int)(t - D.tile0);   // row z * ny + y
+        const int x = threadIdx.x;
+        if (x >= g.nx) continue;
+        const T* fin = (const T*)D.f[parity];
+        T* fout = (T*)D.f[parity ^ 1];
+        ForceArgs fa{};
+        if (D.has_ibm) {
+            fa.dev = D.a.dev;
+            fa.slot = (int)(D.a.dev->cur & 1);
+            stream_collide_cell<CLBM_STORE_F32, PULL, kForceSkipBand>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
+        } else {
+            stream_collide_cell<CLBM_STORE_F32, PULL, kForceNone>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
+        }
+    }
+}
+
 void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
                           int n, long long ntiles, int parity, int grid, cudaStream_t st) {
-    if (storage == CLBM_STORE_F16S) {
+    if (storage == CLBM_STORE_F32) {
+        if (pull) kb_bulk_row_f32<true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        else kb_bulk_row_f32<false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+    } else if (storage == CLBM_STORE_F16S) {
         if (pull) kb_bulk_row<CLBM_STORE_F16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
         else kb_bulk_row<CLBM_STORE_F16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
     } else if (storage == CLBM_STORE_BF16S) {

@@ -162,7 +162,7 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
 int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph);
 int clbm_ensemble_stream(const clbm_ensemble* e, void** out);
 /* The bulk-pass schedule chosen at creation: tile width (cells; 0: one row per block,
- * 16-bit members grouped by row width, one launch per group), blocks, tiles, and the time
+ * members grouped by row width, one launch per group), blocks, tiles, and the time
  * of one bulk pass of all members with it, alone, in milliseconds (any pointer may be
  * NULL). */
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
