@@ -11,7 +11,7 @@ y/z periodic.
   fine   1200 x 400 x 100, chord 160, FP32 (the judge and the source of training data)
 One coarse step is two fine steps (acoustic scaling: same lattice U, halved spacing).
 
-Judged on mean and RMS C_L, C_D over the last motion period and on the mid-span wake
+Judged on mean and RMS C_L, C_D over the last motion period(s) and on the mid-span wake
 vorticity spectrum (power along x in cycles per chord, vorticity in coarse time units).
 """
 
@@ -55,8 +55,11 @@ def _spectrum_marks(steps, period, count):
     return set(max(1, int(round(steps - i * span / count))) for i in range(count))
 
 
+STAT_PERIODS = 1   # motion periods the statistics average over (the last ones of the run)
+
+
 def _window(steps, period):
-    return max(1, min(int(round(period)), steps // 2))
+    return max(1, min(int(round(STAT_PERIODS * period)), steps // 2))
 
 
 def _run(sim, steps, chunk, on_chunk=None):
@@ -255,7 +258,11 @@ def main(argv=None):
                          "--fine-json (an earlier --out file)")
     ap.add_argument("--load-net", default=None)
     ap.add_argument("--fine-json", default=None)
+    ap.add_argument("--periods", type=int, default=1,
+                    help="statistics over the last PERIODS motion periods (at most half the run)")
     args = ap.parse_args(argv)
+    global STAT_PERIODS
+    STAT_PERIODS = max(1, args.periods)
     log = lambda m: print(m, flush=True)
     base = tuple(args.base)
     if args.span_sweep:
