@@ -121,12 +121,13 @@ __device__ __forceinline__ long long spread_q(float f, float w) {
 template <int K>
 __device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Grid& g, int m0, int lane,
                                                    MarkerTaps (&tp)[K], bool (&has)[K]) {
-    float xk[K], yk[K], zk[K], us[K], vs[K], uxv[K][2], uyv[K][2];
+    float xk[K], yk[K], zk[K], vxk[K], vyk[K], us[K], vs[K], uxv[K][2], uyv[K][2];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         has[k] = m0 + k < a.n;
         const int m = has[k] ? m0 + k : 0;   // launched only with a.n >= 1
         xk[k] = a.X[m]; yk[k] = a.Y[m]; zk[k] = a.Z[m];
+        vxk[k] = a.VX[m]; vyk[k] = a.VY[m];   // with the positions: one round trip less
     }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -173,8 +174,8 @@ __device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Gri
     for (int k = 0; k < K; ++k) {
         if (!has[k]) continue;
         const int m = m0 + k;
-        tp[k].fx = fmaxf(-0.05f, fminf(0.05f, -(us[k] - a.VX[m])));
-        tp[k].fy = fmaxf(-0.05f, fminf(0.05f, -(vs[k] - a.VY[m])));
+        tp[k].fx = fmaxf(-0.05f, fminf(0.05f, -(us[k] - vxk[k])));
+        tp[k].fy = fmaxf(-0.05f, fminf(0.05f, -(vs[k] - vyk[k])));
         if (lane == 0) {
             a.Uk[m] = us[k];
             a.Vk[m] = vs[k];
