@@ -4,10 +4,12 @@
 // (EnsDesc) tells the batched kernels where they are. The marker, interpolation and
 // force-sum kernels index the instance with blockIdx.y (each instance uses as many x-blocks
 // as it needs, the rest leave); band-prepare and the box pass run one thread per force-box
-// cell over a flat list of all instances' boxes. The bulk stream-collide pass runs
-// persistent blocks over one flat list of tiles (runs of consecutive cells) of all
-// instances, so lattices of different sizes share the GPU without tail effects; the tile
-// width and the number of persistent blocks are picked by timing at creation.
+// cell over a flat list of all instances' boxes. The bulk stream-collide pass runs over
+// one flat list of tiles of all instances (runs of consecutive cells, or row segments for
+// the two-cell 16-bit body), or with one row per block over groups of instances of equal
+// row width, so lattices of different sizes share the GPU without tail effects; the tile
+// width, the row mode and the number of persistent blocks are picked by timing at
+// creation.
 // Every per-cell and per-marker computation is the single-lattice code (lbm_device.cuh,
 // ibm_device.cuh), so an instance gives the same bits as when it is stepped alone.
 #include <algorithm>
