@@ -447,23 +447,26 @@ template <> struct Pair<CLBM_STORE_BF16S> {
 
 // Cells (x0, x0 + 1) of row (y, z), x0 even, for a warp of consecutive pairs of one row
 // (lanes past the lattice edge take part in the shuffles and store nothing).
-template <int S, bool PULL, int FMODE>
+// IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
+template <int S, bool PULL, int FMODE, bool IDX32 = false>
 __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
                                           typename Pair<S>::T* __restrict__ fout, const Grid& g,
                                           const Coef& c, const ForceArgs& fa, int x0, int y, int z) {
     using P = Pair<S>;
+    using I = typename std::conditional<IDX32, unsigned, long long>::type;
+    const I plane = (I)g.plane;
     constexpr unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
     // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
     if (__all_sync(kFull, !act0)) return;
     const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
-    const long long row = ((long long)z * g.ny + y) * g.pitch;
+    const I row = ((I)z * (I)g.ny + (I)y) * (I)g.pitch;
     float h0[19], h1[19];
     if (!PULL) {
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            const float2 p = P::ld2(fin + q * g.plane + row + x0c);
+            const float2 p = P::ld2(fin + ((I)q * plane + row + (I)x0c));
             h0[q] = p.x;
             h1[q] = p.y;
         }
@@ -476,7 +479,7 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
         for (int q = 0; q < 19; ++q) {
             const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
             const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-            const typename P::T* rp = fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch;
+            const typename P::T* rp = fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch);
             const float2 p = P::ld2(rp + x0c);
             if (ex(q) == 0) {
                 h0[q] = p.x;
@@ -511,7 +514,7 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
             for (int q = 0; q < 19; ++q) {
                 const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
                 const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-                h0[q] = P::ld1(fin + q * g.plane + ((long long)sz * g.ny + sy) * g.pitch + (xe - ex(q)));
+                h0[q] = P::ld1(fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)(xe - ex(q))));
             }
         }
     }
@@ -553,15 +556,15 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
     collide_pair<true>(h0, h1, c, use0, use1, frc0, frc1, F0x, F0y, F0z, F1x, F1y, F1z);
     if (use0 && use1) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) P::st2(fout + q * g.plane + row + x0, h0[q], h1[q]);
+        for (int q = 0; q < 19; ++q) P::st2(fout + ((I)q * plane + row + (I)x0), h0[q], h1[q]);
     } else {
         if (use0) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0, h0[q]);
+            for (int q = 0; q < 19; ++q) P::st1(fout + ((I)q * plane + row + (I)x0), h0[q]);
         }
         if (use1) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) P::st1(fout + q * g.plane + row + x0 + 1, h1[q]);
+            for (int q = 0; q < 19; ++q) P::st1(fout + ((I)q * plane + row + (I)x0 + 1), h1[q]);
         }
     }
 }

@@ -46,12 +46,12 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
 // Two cells per thread (Pair, pair_body in lbm_device.cuh).
 // PX threads per block (2 PX cells along x): 64 or 128, whichever leaves fewer idle lanes
 // at the row ends (pair_threads).
-template <int S, bool PULL, int FMODE, int PX>
+template <int S, bool PULL, int FMODE, int PX, bool IDX32>
 __global__ void __launch_bounds__(PX, 1024 / PX) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
                                                                     typename Pair<S>::T* __restrict__ fout,
                                                                     Grid g, Coef c, ForceArgs fa) {
-    pair_body<S, PULL, FMODE>(fin, fout, g, c, fa, 2 * (blockIdx.x * PX + threadIdx.x), blockIdx.y,
-                              blockIdx.z);
+    pair_body<S, PULL, FMODE, IDX32>(fin, fout, g, c, fa, 2 * (blockIdx.x * PX + threadIdx.x), blockIdx.y,
+                                     blockIdx.z);
 }
 
 static int pair_threads(int nx) {
@@ -59,19 +59,28 @@ static int pair_threads(int nx) {
     return w64 < w128 ? 64 : 128;
 }
 
-template <int S, bool PULL, int PX>
-static void pair_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
-                        const ForceArgs& fa, cudaStream_t st) {
+template <int S, bool PULL, int PX, bool IDX32>
+static void pair_launch_i(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                          const ForceArgs& fa, cudaStream_t st) {
     using T = typename Pair<S>::T;
     const dim3 grid((g.nx + 2 * PX - 1) / (2 * PX), g.ny, g.nz);
     if (fmode == kForceNone)
-        k_stream_collide_pair<S, PULL, kForceNone, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        k_stream_collide_pair<S, PULL, kForceNone, PX, IDX32><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else if (fmode == kForceBand)
-        k_stream_collide_pair<S, PULL, kForceBand, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        k_stream_collide_pair<S, PULL, kForceBand, PX, IDX32><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else if (fmode == kForceSkipBand)
-        k_stream_collide_pair<S, PULL, kForceSkipBand, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        k_stream_collide_pair<S, PULL, kForceSkipBand, PX, IDX32><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
     else
-        k_stream_collide_pair<S, PULL, kForceDense, PX><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+        k_stream_collide_pair<S, PULL, kForceDense, PX, IDX32><<<grid, PX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+}
+
+// 32-bit element indices while every index of the 19 planes fits (one wide multiply-add
+// per address instead of 64-bit index arithmetic).
+template <int S, bool PULL, int PX>
+static void pair_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                        const ForceArgs& fa, cudaStream_t st) {
+    if (19LL * g.plane <= 0xffffffffLL) pair_launch_i<S, PULL, PX, true>(fmode, fin, fout, g, c, fa, st);
+    else pair_launch_i<S, PULL, PX, false>(fmode, fin, fout, g, c, fa, st);
 }
 
 // ------------------------------------------------------------------ TMA-staged kernel
