@@ -194,7 +194,7 @@ template <> struct Pop<CLBM_STORE_F32> {
     static __device__ __forceinline__ float ld(const T* p, int q) { (void)q; return __ldg(p); }
     static __device__ __forceinline__ void st(T* p, int q, float v) { (void)q; __stcs(p, v); }
     static __device__ __forceinline__ float ld_raw(const T* p) { return __ldg(p); }
-    static __device__ __forceinline__ void st_raw(T* p, float v) { __stcs(p, v); }
+    static __device__ __forceinline__ void st_raw(T* p, float v) { *p = v; }
 };
 template <> struct Pop<CLBM_STORE_F16S> {
     using T = __half;

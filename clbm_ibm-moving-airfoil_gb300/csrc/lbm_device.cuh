@@ -424,10 +424,10 @@ template <> struct Pair<CLBM_STORE_F16S> {
     static __device__ __forceinline__ float ld1(const T* p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ void st2(T* p, float a, float b) {
         const __half2 h = __floats2half2_rn(a, b);
-        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+        *reinterpret_cast<unsigned int*>(p) = *reinterpret_cast<const unsigned int*>(&h);
     }
     static __device__ __forceinline__ void st1(T* p, float a) {
-        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(a)));
+        *reinterpret_cast<unsigned short*>(p) = __half_as_ushort(__float2half_rn(a));
     }
 };
 template <> struct Pair<CLBM_STORE_BF16S> {
@@ -438,21 +438,21 @@ template <> struct Pair<CLBM_STORE_BF16S> {
     static __device__ __forceinline__ float ld1(const T* p) { return __bfloat162float(__ldg(p)); }
     static __device__ __forceinline__ void st2(T* p, float a, float b) {
         const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        __stcs(reinterpret_cast<unsigned int*>(p), *reinterpret_cast<const unsigned int*>(&h));
+        *reinterpret_cast<unsigned int*>(p) = *reinterpret_cast<const unsigned int*>(&h);
     }
     static __device__ __forceinline__ void st1(T* p, float a) {
-        __stcs(reinterpret_cast<unsigned short*>(p), __bfloat16_as_ushort(__float2bfloat16_rn(a)));
+        *reinterpret_cast<unsigned short*>(p) = __bfloat16_as_ushort(__float2bfloat16_rn(a));
     }
 };
 
 // Cells (x0, x0 + 1) of row (y, z), x0 even, for a warp of consecutive pairs of one row
 // (lanes past the lattice edge take part in the shuffles and store nothing).
 // IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
-template <int S, bool PULL, int FMODE, bool IDX32 = false>
+// P: the loads and stores of the storage form (Pair<S>).
+template <int S, bool PULL, int FMODE, bool IDX32 = false, class P = Pair<S>>
 __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
                                           typename Pair<S>::T* __restrict__ fout, const Grid& g,
                                           const Coef& c, const ForceArgs& fa, int x0, int y, int z) {
-    using P = Pair<S>;
     using I = typename std::conditional<IDX32, unsigned, long long>::type;
     const I plane = (I)g.plane;
     constexpr unsigned kFull = 0xffffffffu;
