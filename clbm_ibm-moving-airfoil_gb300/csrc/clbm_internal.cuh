@@ -192,7 +192,7 @@ template <> struct Pop<CLBM_STORE_F32> {
     using T = float;
     static constexpr bool kShifted = false;
     static __device__ __forceinline__ float ld(const T* p, int q) { (void)q; return __ldg(p); }
-    static __device__ __forceinline__ void st(T* p, int q, float v) { (void)q; __stcs(p, v); }
+    static __device__ __forceinline__ void st(T* p, int q, float v) { (void)q; *p = v; }
     static __device__ __forceinline__ float ld_raw(const T* p) { return __ldg(p); }
     static __device__ __forceinline__ void st_raw(T* p, float v) { *p = v; }
 };
@@ -203,12 +203,11 @@ template <> struct Pop<CLBM_STORE_F16S> {
         return __half2float(__ldg(p)) + wq(q);
     }
     static __device__ __forceinline__ void st(T* p, int q, float v) {
-        __stcs(reinterpret_cast<unsigned short*>(p),
-               __half_as_ushort(__float2half_rn(v - wq(q))));
+        *reinterpret_cast<unsigned short*>(p) = __half_as_ushort(__float2half_rn(v - wq(q)));
     }
     static __device__ __forceinline__ float ld_raw(const T* p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ void st_raw(T* p, float v) {
-        __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
+        *reinterpret_cast<unsigned short*>(p) = __half_as_ushort(__float2half_rn(v));
     }
 };
 template <> struct Pop<CLBM_STORE_BF16S> {
@@ -218,12 +217,11 @@ template <> struct Pop<CLBM_STORE_BF16S> {
         return __bfloat162float(__ldg(p)) + wq(q);
     }
     static __device__ __forceinline__ void st(T* p, int q, float v) {
-        __stcs(reinterpret_cast<unsigned short*>(p),
-               __bfloat16_as_ushort(__float2bfloat16_rn(v - wq(q))));
+        *reinterpret_cast<unsigned short*>(p) = __bfloat16_as_ushort(__float2bfloat16_rn(v - wq(q)));
     }
     static __device__ __forceinline__ float ld_raw(const T* p) { return __bfloat162float(__ldg(p)); }
     static __device__ __forceinline__ void st_raw(T* p, float v) {
-        __stcs(reinterpret_cast<unsigned short*>(p), __bfloat16_as_ushort(__float2bfloat16_rn(v)));
+        *reinterpret_cast<unsigned short*>(p) = __bfloat16_as_ushort(__float2bfloat16_rn(v));
     }
 };
 

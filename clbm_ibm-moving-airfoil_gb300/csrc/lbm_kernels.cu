@@ -13,7 +13,7 @@
 //   4. maps raw moments back to populations with the closed form of M_raw^-1 (entries
 //      0, +-1/4, +-1/2, +-1; clbm_moving.py:233-238) and adds Guo forcing
 //      (clbm_moving.py:240-249) where the force is non-zero;
-//   5. stores f_post for the next step, coalesced and with streaming stores.
+//   5. stores f_post for the next step, coalesced (plain stores: the streaming hint measured slower).
 // Algorithmic traffic: 19 loads + 19 stores per cell (152 B/cell float32, 76 B/cell for
 // the 16-bit shifted forms); the force fields add 8 B per cell inside the IBM band only.
 #include <algorithm>
@@ -100,9 +100,9 @@ template <> struct Stg<CLBM_STORE_F32> {
     static __device__ __forceinline__ float2 lds2(const T* p) { return *reinterpret_cast<const float2*>(p); }
     static __device__ __forceinline__ float lds1(const T* p) { return *p; }
     static __device__ __forceinline__ void st2(T* p, float a, float b) {
-        __stcs(reinterpret_cast<float2*>(p), make_float2(a, b));
+        *reinterpret_cast<float2*>(p) = make_float2(a, b);
     }
-    static __device__ __forceinline__ void st1(T* p, float a) { __stcs(p, a); }
+    static __device__ __forceinline__ void st1(T* p, float a) { *p = a; }
 };
 template <> struct Stg<CLBM_STORE_F16S> {
     using T = __half;
