@@ -712,6 +712,9 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
             s->g_slot = slot;
         }
         const int per = ibm ? (ibm->a.n > 0 ? kKernelsPerIbmStep : kKernelsPerIbmStep - 2) : 1;
+        // a direct step before the replay may have left its bulk pass running on the second
+        // stream; the graph's first kernels read the state that pass writes
+        if (int rc = join_bulk(s)) return rc;
         while (nsteps - done >= kGraphSteps) {
             CK(cudaGraphLaunch(s->gexec, s->st));
             done += kGraphSteps;
@@ -1172,6 +1175,7 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
             return fail(CLBM_ERR_STATE, "clbm_ensemble_run: member %d was stepped or destroyed "
                         "outside the ensemble", i);
     for (clbm_solver* s : e->s) {
+        if (int rc = join_bulk(s)) return rc;
         CK(cudaEventRecord(e->ev_sync, s->st));
         CK(cudaStreamWaitEvent(e->st, e->ev_sync, 0));
     }

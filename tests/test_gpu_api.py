@@ -217,3 +217,23 @@ def test_shifted_storage_error_against_fp64_oracle(gpkg, oracle_mod, storage, to
     assert e_u < tol and e_f < 10 * tol
     assert e_mean["cl"] < 1e-2 and e_mean["cd"] < 1e-2
     sim.close()
+
+
+def test_graph_replay_after_a_direct_step_waits_for_its_bulk_pass(gpkg):
+    """An IBM step launched directly leaves its bulk pass running on the second stream
+    (joined by the next call); a divergence check between runs makes the next run start
+    with such a step and then replay the graph already captured. The replay must wait for
+    that bulk pass: two chunks with a check between give the bits of one run (600x200x50,
+    FP16, where any overlap with the pass changes the stored values)."""
+    cfg = gpkg.full_case(storage="f16")
+    runs = []
+    for chunks in ((400,), (200, 200)):
+        sim = gpkg.Simulation(cfg)
+        for k in chunks:
+            sim.run(k, graph=True)
+            sim.solver.synchronize()
+            sim.solver.check()
+        runs.append((sim.ibm.force_history(400), sim.solver.read_populations()))
+        sim.close()
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
