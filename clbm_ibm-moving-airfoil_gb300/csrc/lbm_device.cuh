@@ -522,8 +522,13 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
     bool in0 = false, in1 = false;
     if (FMODE == kForceSkipBand || FMODE == kForceBand) {
         const Band b = load_band(fa.dev, fa.slot);
-        in0 = act0 && in_band(b, x0, y, z, g.ny, g.nz);
-        in1 = act1 && in_band(b, x0 + 1, y, z, g.ny, g.nz);
+        // the two cells share their row: the y/z part of the test once, then x per cell
+        int oy = y - b.j0; if (oy < 0) oy += g.ny;
+        int oz = z - b.k0; if (oz < 0) oz += g.nz;
+        if (oy < b.jlen && oz < b.klen) {
+            in0 = act0 && (unsigned)(x0 - b.i0) < (unsigned)b.ilen;
+            in1 = act1 && (unsigned)(x0 + 1 - b.i0) < (unsigned)b.ilen;
+        }
     }
     const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
     const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
