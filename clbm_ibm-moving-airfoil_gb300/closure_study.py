@@ -8,7 +8,7 @@ within a few thousand steps, so no fine reference run exists there), U = 0.05, k
 quarter chord at (2c, Ny/2), Peskin 4-point IBM, Zou-He inlet, zero-gradient outlet,
 y/z periodic.
   coarse  600 x 200 x 50,  chord 80,  FP16 shifted storage (plain and with the closure)
-  fine   1200 x 400 x 100, chord 160, FP32 (the judge and the source of training data)
+  fine   1200 x 400 x 100, chord 160, FP32 (the reference run and the source of training data)
 One coarse step is two fine steps (acoustic scaling: same lattice U, halved spacing).
 
 Judged on mean and RMS C_L, C_D over the last motion period(s) and on the mid-span wake

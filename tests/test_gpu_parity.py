@@ -49,7 +49,7 @@ def test_gpu_matches_reference_golden(gpkg, case):
             m = s.read_macro()
             for k in ("rho", "ux", "uy"):
                 assert rel_l2(m[k], d[f"s{step}_{k}"]) < TOL_FIELD, (step, k)
-            # uz is a small secondary component: its error is judged on the velocity scale
+            # uz is a small secondary component: its error is measured on the velocity scale
             uscale = np.max(np.abs(d[f"s{step}_ux"]))
             assert np.max(np.abs(m["uz"] - d[f"s{step}_uz"])) < TOL_FIELD * uscale
         if step in d["f_record"]:
