@@ -11,7 +11,7 @@ y/z periodic.
   fine   1200 x 400 x 100, chord 160, FP32 (the reference run and the source of training data)
 One coarse step is two fine steps (acoustic scaling: same lattice U, halved spacing).
 
-Judged on mean and RMS C_L, C_D over the last motion period(s) and on the mid-span wake
+Compared on mean and RMS C_L, C_D over the last motion period(s) and on the mid-span wake
 vorticity spectrum (power along x in cycles per chord, vorticity in coarse time units).
 """
 
