@@ -235,6 +235,50 @@ def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
     return out
 
 
+def workload_config(cfg, storage, world, closure=None):
+    """The `config` object of both arms' JSON lines (the same keys and values for the same
+    workload)."""
+    return {
+        "workload": "moving NACA0012 wing, D3Q19 CLBM + IBM, 600x200x50, chord 80, Re 200",
+        "lattice": [cfg.nx, cfg.ny, cfg.nz], "markers": cfg.n_markers,
+        "storage": storage, "parallelism": f"replicas x{world}",
+        "l2": "inputs larger than L2: 2 x %.0f MB population buffers" %
+              (cfg.cells * 19 * (4 if storage == "f32" else 2) / 1e6),
+        "step": "one time step of main_moving.py:116-122: compute_force + LBM step",
+        "closure": closure or "off",
+    }
+
+
+FP64_FIXTURE = os.path.join(ROOT, "tests", "golden", "long_f64_600x200x50_10053.npz")
+
+
+def form_errors(pkg, device, storage, closure=None):
+    """Mean and RMS C_L / C_D of the same workload over one motion period (10,053 steps,
+    graph-replayed) against the FP64-everywhere oracle run of the same case (committed
+    fixture), as relative errors; None without the fixture."""
+    import numpy as np
+    if not os.path.exists(FP64_FIXTURE):
+        return None
+    fix = np.load(FP64_FIXTURE)
+    steps = int(fix["steps"])
+    cfg = pkg.full_case(storage=storage)
+    sim = pkg.Simulation(cfg, device=device)
+    if closure is not None:
+        sim.solver.set_closure(closure)
+    sim.run(steps, graph=True)
+    hist = sim.ibm.force_history(steps)
+    sim.close()
+
+    def stats(h):
+        c = pkg.force_coefficients(h, cfg)
+        return {"cl_mean": float(np.mean(c["cl"])), "cl_rms": float(np.std(c["cl"])),
+                "cd_mean": float(np.mean(c["cd"])), "cd_rms": float(np.std(c["cd"]))}
+    got, ref = stats(hist), stats(fix["hist"])
+    out = {k: abs(got[k] - ref[k]) / abs(ref[k]) for k in got}
+    out["against"] = f"FP64 oracle, same case, {steps} steps (one motion period)"
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -243,13 +287,16 @@ def run_reference(args, rank, world):
     cfg = pkg.full_case(storage="f32")
     from oracle.oracle import Oracle, load
     threads = load().oracle_max_threads()
-    # bounded sample: the oracle needs ~0.5-2 s per full step of this case
-    k = max(1, min(args.steps, 8))
-    w = max(0, min(args.warmup, 1))
+    # every requested step is timed, unless at the measured warm-up rate the timed steps
+    # would take longer than the budget (a few minutes); then the first steps that fit
+    budget_s = 240.0
+    w = max(1, args.warmup)
     o = Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
                cfg.X0, cfg.Y0, cfg.Z0)
-    if w:
-        o.run(0, w, cfg.motion(), record=False)
+    t0 = time.perf_counter()
+    o.run(0, w, cfg.motion(), record=False)
+    per_step = (time.perf_counter() - t0) / w
+    k = max(1, min(args.steps, int(budget_s / max(per_step, 1e-9))))
     t0 = time.perf_counter()
     o.run(w, k, cfg.motion(), record=False)
     dt = time.perf_counter() - t0
@@ -260,11 +307,10 @@ def run_reference(args, rank, world):
         "warmup": w, "ms_per_step": dt / k * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": "moving NACA0012 wing, D3Q19 CLBM + IBM, 600x200x50, chord 80, Re 200",
-                   "lattice": [cfg.nx, cfg.ny, cfg.nz], "markers": cfg.n_markers,
-                   "storage": "f32"},
+        "config": workload_config(cfg, "f32", world),
         "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
-                         "sample": f"{k} of the requested {args.steps} steps after {w} warm-up; "
+                         "sample": f"{k} of the requested {args.steps} steps after {w} warm-up "
+                                   f"step(s) (timed steps capped at {budget_s:.0f} s); "
                                    "Taichi is not installed, so the reference arm is the "
                                    "C/OpenMP restatement of its unfused step"},
         "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -363,15 +409,8 @@ def run_gpu(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": args.storage, "data": "synthetic",
-            "config": {
-                "workload": "moving NACA0012 wing, D3Q19 CLBM + IBM, 600x200x50, chord 80, Re 200",
-                "lattice": [cfg.nx, cfg.ny, cfg.nz], "markers": cfg.n_markers,
-                "storage": args.storage, "parallelism": f"replicas x{world}",
-                "l2": "inputs larger than L2: 2 x %.0f MB population buffers" %
-                      (cfg.cells * 19 * (4 if args.storage == "f32" else 2) / 1e6),
-                "timed_region": "direct launches, per-step IBM + fused stream-collide",
-                "closure": args.closure or "off",
-            },
+            "config": workload_config(cfg, args.storage, world, args.closure),
+            "timed_region": "direct launches, per-step IBM + fused stream-collide",
             "graph_value": cfg.cells * args.steps * world / (graph_ms / 1e3) / 1e6,
             "gpu_launches": gpu_launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -403,6 +442,14 @@ def run_gpu(args, rank, world, local):
             forms["f16_closure"] = measure_form(pkg, torch, local, "f16", pkg.closure.ClosureNet.load(net))
         for v in forms.values():
             v["speedup_vs_f32"] = v["value"] / result["value"]
+        # the metric's "at stated C_L/C_D error": each form over one motion period against
+        # the FP64 oracle of the same case (the plain float32 path too, for reference)
+        closure_net = pkg.closure.ClosureNet.load(net) if os.path.exists(net) else None
+        for name, st, cl in (("f16", "f16", None), ("bf16", "bf16", None),
+                             ("f16_closure", "f16", closure_net)):
+            if name in forms:
+                forms[name]["cl_cd_error"] = form_errors(pkg, local, st, cl)
+        result["cl_cd_error"] = form_errors(pkg, local, "f32")
         result["forms"] = forms
     if result is not None and not args.no_ensemble:
         result["ensemble"] = {s: measure_ensemble(pkg, torch, local, s) for s in ("f32", "f16")}

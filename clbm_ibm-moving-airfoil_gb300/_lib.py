@@ -23,7 +23,7 @@ EXPORTED = (
     "clbm_read_populations", "clbm_write_populations", "clbm_check", "ibm_create",
     "ibm_destroy", "ibm_compute_force", "ibm_compute_force_motion", "ibm_read_forces",
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
-    "clbm_synchronize", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
+    "clbm_synchronize", "clbm_set_rho_floor", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
@@ -101,6 +101,7 @@ def lib():
             "ibm_step_count": [vp, ctypes.POINTER(i64)],
             "clbm_run": [vp, vp, ctypes.POINTER(Motion), i32, i32],
             "clbm_synchronize": [vp],
+            "clbm_set_rho_floor": [vp, d],
             "clbm_stream": [vp, pvp],
             "clbm_selftest_wait_timeout": [vp, i32],
             "clbm_profile_enable": [vp, i32],

@@ -5,6 +5,7 @@ the CUDA runtime into one shared library whose entry points are declared in
 ``include/clbm_gb300.h``.
 """
 
+import json
 import os
 import subprocess
 import sys
@@ -13,6 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libclbm_gb300.so")
+# record of the nvcc command lines that produced LIB (the target architecture is checked
+# from it on machines without a GPU)
+INFO = os.path.join(BUILD, "build_info.json")
 SOURCES = ["lbm_kernels.cu", "ibm_kernels.cu", "ensemble.cu", "closure.cu", "capi.cu", "closure_api.cu",
            "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -50,8 +54,9 @@ def build(force=False, verbose_ptxas=False):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), src, obj))
-    objs, errors = [], []
+    objs, errors, cmds = [], [], []
     for p, src, obj in procs:
+        cmds.append(p.args)
         out = p.communicate()[0].decode(errors="replace")
         if p.returncode != 0:
             errors.append(f"--- {src}\n{out}")
@@ -63,6 +68,9 @@ def build(force=False, verbose_ptxas=False):
     tmp = LIB + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     subprocess.run(cmd, check=True)
+    cmds.append(cmd)
+    with open(INFO, "w") as fh:
+        json.dump({"arch": ARCH, "commands": cmds}, fh, indent=1)
     os.replace(tmp, LIB)
     return LIB
 

@@ -14,12 +14,16 @@ constexpr double kWd[19] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
 constexpr int kHistCap = 1 << 16;
-// kernels one graph-captured step launches: markers, band-prepare, interp/spread, finish,
-// bulk stream-collide, box stream-collide
-constexpr int kKernelsPerIbmStep = 6;
+// kernels one graph-captured step launches: markers, band-prepare, interp/spread, bulk
+// stream-collide, box stream-collide with the force sums
+constexpr int kKernelsPerIbmStep = 5;
 // steps per captured graph (even, so buffer and box-slot parities repeat); within a graph
 // each step's marker kernel overlaps the previous step's bulk pass
 constexpr int kGraphSteps = 8;
+// density floor of the divergence monitor: main_moving.py:143 stops below rho = 0.3
+constexpr double kRhoFloor = 0.3;
+// graph replays clbm_run keeps in flight; it reads the status word of the oldest one
+constexpr int kReplaysInFlight = 4;
 
 }  // namespace
 
@@ -68,17 +72,30 @@ int join_bulk(clbm_solver* s) {
     return CLBM_OK;
 }
 
+// Box pass of an IBM step on stream st: with the force sums of the IBM call when they are
+// still pending (no separate force-sum kernel then).
+void box_pass(clbm_solver* s, const ForceArgs& fa, const clbm_ibm* ibm, long long box_cells,
+              cudaStream_t st) {
+    if (ibm && ibm->sums_pending) {
+        launch_stream_collide_box_sums(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur],
+                                       s->g, s->c, fa, ibm->a, box_cells, st);
+        ibm->sums_pending = false;
+    } else {
+        launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
+                                  s->c, fa, box_cells, st);
+    }
+}
+
 // One fused stream-collide launch on stream `st`, bracketed by timing events if profiling.
 int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bool box,
-             long long box_cells) {
+             long long box_cells, const clbm_ibm* ibm = nullptr) {
     if (s->prof) {
         if (int rc = record_event(s, st)) return rc;
         s->ev_tag.resize(s->ev_used / 2 + 1);
         s->ev_tag[s->ev_used / 2] = box ? 1 : 0;
     }
     if (box) {
-        launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
-                                  s->c, fa, box_cells, st);
+        box_pass(s, fa, ibm, box_cells, st);
     } else if (s->closure && (fmode == kForceNone || fmode == kForceSkipBand)) {
         ClosureArgs ca{};
         ca.params = s->cl_params;
@@ -94,6 +111,17 @@ int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bo
     if (s->prof)
         if (int rc = record_event(s, st)) return rc;
     s->launches += 1;
+    return CLBM_OK;
+}
+
+// Force sums of an IBM call that no step has completed yet, by the force-sum kernel (needed
+// when the history is read, or another compute_force comes, before the next step).
+int flush_sums(const clbm_ibm* ibm) {
+    if (!ibm->sums_pending) return CLBM_OK;
+    launch_ibm_finish(ibm->a, ibm->s->g, ibm->s->st);
+    CK_LAUNCH();
+    ibm->s->launches += 1;
+    ibm->sums_pending = false;
     return CLBM_OK;
 }
 
@@ -113,7 +141,7 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         if (serial) {
             if (int rc = sc_timed(s, kForceSkipBand, fa, s->st, false, 0)) return rc;
             const long long bc = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
-            if (int rc = sc_timed(s, kForceBand, fa, s->st, true, bc)) return rc;
+            if (int rc = sc_timed(s, kForceBand, fa, s->st, true, bc, ibm)) return rc;
             s->cur = 1 - s->cur;
             s->local = false;
             s->macro_full = false;
@@ -129,7 +157,7 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         if (int rc = sc_timed(s, kForceSkipBand, fa, s->st2, false, 0)) return rc;
         CK(cudaEventRecord(s->ev_bulk, s->st2));
         const long long box_cells = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
-        if (int rc = sc_timed(s, kForceBand, fa, s->st, true, box_cells)) return rc;
+        if (int rc = sc_timed(s, kForceBand, fa, s->st, true, box_cells, ibm)) return rc;
         s->bulk_pending = true;  // joined by the next call (after the next marker kernel)
     }
     s->cur = 1 - s->cur;
@@ -141,6 +169,8 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
 
 int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motion& m) {
     clbm_solver* s = ibm->s;
+    // a previous call that no step completed: its sums first (they advance the counter)
+    if (int rc = flush_sums(ibm)) return rc;
     // the marker kernel needs only the motion: it runs beside the previous step's bulk pass
     launch_ibm_markers(ibm->a, s->g, devm, mf, m, s->st);
     CK(cudaEventRecord(ibm->ev_box, s->st));
@@ -150,9 +180,10 @@ int ibm_force_impl(clbm_ibm* ibm, bool devm, const MotionF& mf, const clbm_motio
                         ibm->a.fx, ibm->a.fy, s->rho, s->ux, s->uy, s->uz, ibm->a.max_bx,
                         ibm->a.max_by, ibm->a.max_bz, !s->macro_full, s->st);
     launch_ibm_interp_spread(ibm->a, s->g, s->st);
-    launch_ibm_finish(ibm->a, s->g, s->st);
     CK_LAUNCH();
-    s->launches += (ibm->a.n > 0) ? 4 : 2;
+    s->launches += (ibm->a.n > 0) ? 3 : 1;
+    // the force sums of this call are computed by the box pass of the next step
+    ibm->sums_pending = true;
     ibm->calls += 1;
     return CLBM_OK;
 }
@@ -249,6 +280,8 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
     s->c.c23 = (float)(2.0 / 3.0);
     s->c.c16 = (float)(1.0 / 6.0);
     for (int q = 0; q < 19; ++q) s->c.wc[q] = (float)(kWd[q] * (1.0 - cfg->s_v * 0.5));
+    s->c.rho_floor = (float)kRhoFloor;
+    s->c.status = nullptr;  // monitor off while the variants are timed on zeroed buffers
     auto bail = [&](int rc) { clbm_destroy(s); return rc; };
     int prio_low = 0, prio_high = 0;
     cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
@@ -276,6 +309,13 @@ int clbm_create(const clbm_config* cfg, clbm_solver** out) {
     cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st);
     s->g.status = s->status;
     s->variant = pick_variant(s);
+    s->c.status = s->status;
+    if (cudaHostAlloc((void**)&s->h_status, sizeof(unsigned int), cudaHostAllocDefault) != cudaSuccess)
+        return bail(fail(CLBM_ERR_CUDA, "clbm_create: pinned allocation failed"));
+    *s->h_status = 0;
+    for (cudaEvent_t& e : s->ev_replay)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "clbm_create: event creation failed"));
     launch_init(cfg->storage, s->f[0], s->g, s->c, s->st);
     launch_fill_macro(s->g, s->c, s->rho, s->ux, s->uy, s->uz, s->st);
     s->launches += 2;
@@ -303,6 +343,9 @@ int clbm_destroy(clbm_solver* s) {
         if (p) cudaFree(p);
     if (s->ev_bulk) cudaEventDestroy(s->ev_bulk);
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    for (cudaEvent_t e : s->ev_replay)
+        if (e) cudaEventDestroy(e);
+    if (s->h_status) cudaFreeHost(s->h_status);
     if (s->st2) cudaStreamDestroy(s->st2);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -433,6 +476,8 @@ int clbm_write_populations(clbm_solver* s, const float* f_host) {
     CK(cudaMemcpyAsync(s->stage, f_host, n * sizeof(float), cudaMemcpyHostToDevice, s->st));
     launch_import_populations(s->cfg.storage, s->stage, s->f[s->cur], s->g, s->st);
     CK_LAUNCH();
+    // a new state: the monitor's record of the old one no longer applies
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st));
     s->launches += 1;
     s->local = true;
     s->macro_full = false;
@@ -460,7 +505,7 @@ int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_ma
     CK(cudaMemcpyAsync(h, s->stats, sizeof(h), cudaMemcpyDeviceToHost, s->st));
     CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
-    if (status)
+    if (status & kStatusWaitTimeout)
         return fail(CLBM_ERR_STATE, "clbm_check: a device wait gave up (status %u); results of "
                     "the affected steps are invalid", status);
     const bool any = h[0] != ~0ull;
@@ -474,6 +519,10 @@ int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_ma
     if (h[3] > 0 || !any || rmin < rho_floor)
         return fail(CLBM_ERR_DIVERGED, "clbm_check: diverged (rho_min=%g, nonfinite=%llu)", rmin,
                     (unsigned long long)h[3]);
+    if (status & kStatusDiverged)
+        return fail(CLBM_ERR_DIVERGED, "clbm_check: a collision met a density below %g or not "
+                    "finite since the state was last written (rho_min now %g)",
+                    (double)s->c.rho_floor, rmin);
     return CLBM_OK;
 }
 
@@ -617,6 +666,7 @@ int ibm_read_markers(const clbm_ibm* ibm, float* out) {
 int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out) {
     if (int rc = check_bound(ibm, "ibm_read_force_history")) return rc;
     if (!out || count < 0) return fail(CLBM_ERR_ARG, "ibm_read_force_history: bad argument");
+    if (int rc = flush_sums(ibm)) return rc;
     const long long avail = std::min<long long>(ibm->calls, kHistCap);
     if (count > avail)
         return fail(CLBM_ERR_ARG, "ibm_read_force_history: %d entries requested, %lld available",
@@ -674,6 +724,9 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
         ++done;
     }
     if (graph && nsteps - done >= kGraphSteps) {
+        // captured steps complete their own calls' sums; one left from before goes first
+        if (ibm)
+            if (int rc = flush_sums(ibm)) return rc;
         const int slot = ibm ? (int)(ibm->calls & 1) : 0;
         const bool same = s->gexec && s->g_ibm == ibm && s->g_cur == s->cur && s->g_slot == slot &&
                           (!ibm || std::memcmp(&s->g_m, m, sizeof(clbm_motion)) == 0);
@@ -688,6 +741,11 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
             int rc = CLBM_OK;
             for (int k = 0; k < kGraphSteps && !rc; ++k) rc = one();
             if (!rc) rc = join_bulk(s);  // all captured work rejoins the capture stream
+            // each replay ends by copying the status word to pinned host memory, where the
+            // replay loop below reads the divergence monitor without a stream sync
+            if (!rc && cudaMemcpyAsync(s->h_status, s->status, sizeof(unsigned int),
+                                       cudaMemcpyDeviceToHost, s->st) != cudaSuccess)
+                rc = fail(CLBM_ERR_CUDA, "clbm_run: status copy could not be captured");
             capturing = false;
             cudaGraph_t graph_obj = nullptr;
             cudaError_t e = cudaStreamEndCapture(s->st, &graph_obj);
@@ -715,8 +773,30 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
         // a direct step before the replay may have left its bulk pass running on the second
         // stream; the graph's first kernels read the state that pass writes
         if (int rc = join_bulk(s)) return rc;
+        // At most kReplaysInFlight replays are queued: before each launch beyond that, wait
+        // for the oldest and read the status word it copied out. A run that diverged stops
+        // within kReplaysInFlight + 1 replays of the step that diverged (main_moving.py:143-145
+        // breaks its loop on the same condition at its vis steps).
+        *s->h_status = 0;
+        long long replays = 0;
         while (nsteps - done >= kGraphSteps) {
+            if (replays >= kReplaysInFlight) {
+                CK(cudaEventSynchronize(s->ev_replay[replays % kReplaysInFlight]));
+                const unsigned int st_word = *(volatile unsigned int*)s->h_status;
+                if (st_word & (kStatusDiverged | kStatusWaitTimeout)) {
+                    s->local = false;
+                    s->macro_full = false;
+                    if (st_word & kStatusWaitTimeout)
+                        return fail(CLBM_ERR_STATE, "clbm_run: a device wait gave up (status %u)",
+                                    st_word);
+                    return fail(CLBM_ERR_DIVERGED, "clbm_run: diverged: a collision met a "
+                                "density below %g or not finite; stopped after %d of %d steps",
+                                (double)s->c.rho_floor, done, nsteps);
+                }
+            }
             CK(cudaGraphLaunch(s->gexec, s->st));
+            CK(cudaEventRecord(s->ev_replay[replays % kReplaysInFlight], s->st));
+            ++replays;
             done += kGraphSteps;
             s->version += kGraphSteps;
             s->launches += kGraphSteps * per;
@@ -739,8 +819,11 @@ int clbm_synchronize(clbm_solver* s) {
     unsigned int status = 0;
     CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
     CK(cudaStreamSynchronize(s->st));
-    if (status)
+    if (status & kStatusWaitTimeout)
         return fail(CLBM_ERR_STATE, "clbm_synchronize: a device wait gave up (status %u)", status);
+    if (status & kStatusDiverged)
+        return fail(CLBM_ERR_DIVERGED, "clbm_synchronize: diverged: a collision met a density "
+                    "below %g or not finite", (double)s->c.rho_floor);
     return CLBM_OK;
 }
 
@@ -864,6 +947,15 @@ int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_la
     return CLBM_OK;
 }
 
+int clbm_set_rho_floor(clbm_solver* s, double rho_floor) {
+    if (!s || std::isnan(rho_floor)) return fail(CLBM_ERR_ARG, "clbm_set_rho_floor: invalid argument");
+    if (int rc = join_bulk(s)) return rc;
+    CK(cudaStreamSynchronize(s->st));
+    s->c.rho_floor = rho_floor < 0.0 ? -3.0e38f : (float)rho_floor;
+    free_graph(s);  // captured launches hold the old coefficients
+    return CLBM_OK;
+}
+
 int clbm_host_alloc(int64_t bytes, void** out) {
     if (!out || bytes <= 0) return fail(CLBM_ERR_ARG, "clbm_host_alloc: invalid argument");
     CK(cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault));
@@ -899,6 +991,7 @@ struct clbm_ensemble {
         int n = 0;
         long long ntiles = 0;
         int threads = 0;
+        int rows_per_tile = 1;   // 16-bit forms: rows packed into one block
     };
     std::vector<Group> groups;
     bool rows = false;
@@ -931,36 +1024,56 @@ EnsDesc member_desc(const clbm_ensemble* e, int i) {
     return D;
 }
 
-// Members grouped by the threads a whole row needs (a multiple of 32; two cells per thread
-// in the 16-bit forms, one in float32; rows up to 512 cells); each group's descriptors list
-// its members with tiles = rows. No groups when a row is wider.
+// Row mode of the bulk pass. Float32: members grouped by the threads a whole row needs (a
+// multiple of 32, one cell per thread, rows up to 512 cells), one row per block. 16-bit
+// forms: members grouped by row width, R rows packed into a block of two cells per thread.
+// Each group's descriptors list its members with their tiles. No groups when a row is
+// wider.
 int ens_groups(clbm_ensemble* e) {
     const bool f32 = e->storage == CLBM_STORE_F32;   // one cell per thread, rows up to 512
-    std::vector<int> th(e->n);
+    // group key: float32 the block width (one row per block); 16-bit forms the row width
+    std::vector<int> key(e->n);
     for (int i = 0; i < e->n; ++i) {
         const int nx = e->s[i]->g.nx;
-        if (nx > 512) return CLBM_OK;
-        th[i] = f32 ? (nx + 31) / 32 * 32 : (nx + 63) / 64 * 32;
+        if (nx > (f32 ? 512 : 1024)) return CLBM_OK;
+        key[i] = f32 ? (nx + 31) / 32 * 32 : nx;
     }
-    std::vector<int> widths(th);
-    std::sort(widths.begin(), widths.end());
-    widths.erase(std::unique(widths.begin(), widths.end()), widths.end());
-    for (int w : widths) {
+    std::vector<int> keys(key);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    for (int k : keys) {
+        // 16-bit forms: R rows of Nx / 2 pairs per block, the R (block of at most 512
+        // threads) that leaves the fewest idle lanes, the smallest R among equals
+        int threads = k, R = 1;
+        if (!f32) {
+            const int npairs = (k + 1) / 2;
+            double best = 2.0;
+            for (int r = 1; r * npairs <= 512; ++r) {
+                const int th = (r * npairs + 31) / 32 * 32;
+                const double idle = 1.0 - (double)(r * npairs) / th;
+                if (idle < best - 1e-9) {
+                    best = idle;
+                    threads = th;
+                    R = r;
+                }
+            }
+        }
         std::vector<EnsDesc> h;
         std::vector<long long> t0;
         long long tiles = 0;
         for (int i = 0; i < e->n; ++i) {
-            if (th[i] != w) continue;
+            if (key[i] != k) continue;
             EnsDesc D = member_desc(e, i);
             D.tile0 = tiles;
             t0.push_back(tiles);
-            tiles += (long long)D.g.ny * D.g.nz;
+            tiles += ((long long)D.g.ny * D.g.nz + R - 1) / R;
             h.push_back(D);
         }
         clbm_ensemble::Group gr;
         gr.n = (int)h.size();
         gr.ntiles = tiles;
-        gr.threads = w;
+        gr.threads = threads;
+        gr.rows_per_tile = R;
         e->groups.push_back(gr);
         clbm_ensemble::Group& G = e->groups.back();
         CK(cudaMalloc(&G.d, sizeof(EnsDesc) * G.n));
@@ -974,7 +1087,7 @@ int ens_groups(clbm_ensemble* e) {
 
 void ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
     for (const auto& G : e->groups)
-        launch_ens_bulk_rows(e->storage, pull, G.threads, G.d, G.tile0, G.n, G.ntiles, e->cur,
+        launch_ens_bulk_rows(e->storage, pull, G.threads, G.rows_per_tile, G.d, G.tile0, G.n, G.ntiles, e->cur,
                              (int)std::min<long long>(G.ntiles, 1LL << 30), st);
 }
 
@@ -1174,8 +1287,11 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
         if (e->s[i]->cur != e->cur || (e->ibm[i] && e->ibm[i]->s != e->s[i]))
             return fail(CLBM_ERR_STATE, "clbm_ensemble_run: member %d was stepped or destroyed "
                         "outside the ensemble", i);
-    for (clbm_solver* s : e->s) {
+    for (int i = 0; i < e->n; ++i) {
+        clbm_solver* s = e->s[i];
         if (int rc = join_bulk(s)) return rc;
+        if (e->ibm[i])   // a member's own compute_force that no step completed
+            if (int rc = flush_sums(e->ibm[i])) return rc;
         CK(cudaEventRecord(e->ev_sync, s->st));
         CK(cudaStreamWaitEvent(e->st, e->ev_sync, 0));
     }

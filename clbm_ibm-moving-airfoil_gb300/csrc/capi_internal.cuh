@@ -65,6 +65,8 @@ struct clbm_solver {
     int variant = clbm::kVariantStaged;  // full-grid stream-collide kernel (chosen at create)
     float variant_ms[clbm::kVariants] = {};  // autotune time per launch of each variant (0: not timed)
     unsigned int* status = nullptr;
+    unsigned int* h_status = nullptr;  // pinned copy of *status, written by each graph replay
+    cudaEvent_t ev_replay[4] = {};     // ends of the last graph replays (divergence polling)
     // profiling of the fused kernel
     bool prof = false;
     std::vector<cudaEvent_t> ev;
@@ -91,5 +93,9 @@ struct clbm_ibm {
     long long calls = 0;          // host mirror of the device call counter
     cudaEvent_t ev_box = nullptr; // recorded on st after the marker kernel of compute_force
     long long box_version = -1;   // solver state version that ev_box belongs to
+    // the force sums of the last compute_force are not yet in the history: the box pass of
+    // the next step computes them (or, if another call needs them first, the force-sum
+    // kernel does)
+    mutable bool sums_pending = false;
 };
 

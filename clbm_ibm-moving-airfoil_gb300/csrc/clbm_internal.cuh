@@ -33,6 +33,12 @@ __host__ __device__ constexpr int ez(int q) {
     return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
          : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
 }
+// Index of the opposite direction -e_q.
+__host__ __device__ constexpr int opposite(int q) {
+    for (int p = 0; p < 19; ++p)
+        if (ex(p) == -ex(q) && ey(p) == -ey(q) && ez(p) == -ez(q)) return p;
+    return q;
+}
 __host__ __device__ constexpr float wq(int q) {
     return q == 0 ? 1.0f / 3.0f : (q <= 6 ? 1.0f / 18.0f : 1.0f / 36.0f);
 }
@@ -47,6 +53,8 @@ struct Grid {
 };
 
 constexpr unsigned int kStatusWaitTimeout = 1u;
+// status bit: some collision met a density below the floor or a non-finite density
+constexpr unsigned int kStatusDiverged = 2u;
 
 // Collision and boundary constants, rounded to float once on the host.
 struct Coef {
@@ -55,6 +63,10 @@ struct Coef {
     float ux_in, uy_in;
     float c23, c16;   // 2/3 and 1/6 of the Zou-He inlet
     float wc[19];     // w_q * (1 - s_v / 2), Guo forcing weight
+    // divergence monitor: a collision whose density is below rho_floor or not finite sets
+    // kStatusDiverged in *status (no monitor when status is null)
+    float rho_floor;
+    unsigned int* status;
 };
 
 // Learned sub-grid closure: a 19 -> 32 -> 32 -> 1 network (GELU, BF16 weights, FP32
@@ -107,6 +119,8 @@ struct IbmDev {
     int box[2][6];         // slot (call index & 1): imin, -imax, jmin, -jmax, kmin, -kmax
     unsigned int ticket;   // last-block detection of the force-sum kernel
     unsigned int mticket;  // last-block detection of the marker kernel
+    unsigned int bticket;  // last-block detection of the box pass with the force sums
+    long long ksum[2];     // box pass: exact integer sums of the clipped Eulerian force
     // slot: the Band of box[slot] (i0, ilen, j0, jlen, k0, klen, 0, 0), written by the last
     // block of the marker kernel once the box is complete, so the passes that test cells
     // against the box read six integers instead of converting the box in every thread
@@ -279,6 +293,12 @@ void set_last_error(const char* msg);
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
                                const Grid& g, const Coef& c, const ForceArgs& fa,
                                long long max_cells, cudaStream_t st);
+struct IbmArrays;
+// The same box pass, also computing the force sums of the call whose box it is into the
+// history ring and advancing the device call counter (ibm_box_sums_tail).
+void launch_stream_collide_box_sums(int storage, bool pull, const void* fin, void* fout,
+                                    const Grid& g, const Coef& c, const ForceArgs& fa,
+                                    const IbmArrays& a, long long max_cells, cudaStream_t st);
 // Macro (rho, u without force) of the current state for every cell of the grid; optional
 // statistics into stats[0..3] (ordered-int min rho, max rho, max |u|^2, nonfinite count).
 void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
@@ -357,8 +377,9 @@ void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const lon
 // One row per block of `threads` (a multiple of 32: >= Nx / 2 in the 16-bit forms, <= 256;
 // >= Nx in float32, <= 512) over a group of instances of that row width: tiles are rows,
 // tile0 per instance of the group.
-void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
-                          int n, long long ntiles, int parity, int grid, cudaStream_t st);
+void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile, const EnsDesc* d,
+                          const long long* tile0, int n, long long ntiles, int parity, int grid,
+                          cudaStream_t st);
 // Force-box cells of all members as one flat list (offsets per member, n + 1 each), then
 // band-prepare and box pass over it with `grid` blocks of 256 threads.
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st);

@@ -376,4 +376,64 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     }
 }
 
+// Force sums folded into the box pass (single lattice): each block of the box pass brings
+// the integer sums kx, ky of its cells' clipped Eulerian force (units of 2^-40); they are
+// added exactly into dev->ksum; the last block to finish converts them, sums the marker
+// forces in a fixed order (thread-strided, warp butterfly, warps in order), writes the
+// history entry of the call whose box this was, and advances the device call counter --
+// the work of ibm_finish_body without its own launch. The Eulerian part is the same exact
+// integer sum; the marker part is the same set of doubles added in another fixed order.
+__device__ __forceinline__ void ibm_box_sums_tail(const IbmArrays& a, long long kx, long long ky) {
+    __shared__ long long kred[32][2];
+    __shared__ double dred[32][2];
+    __shared__ bool last;
+    IbmDev* dev = a.dev;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        kx += __shfl_xor_sync(0xffffffffu, kx, o);
+        ky += __shfl_xor_sync(0xffffffffu, ky, o);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (lane == 0) { kred[warp][0] = kx; kred[warp][1] = ky; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long sx = 0, sy = 0;
+        for (int w = 0; w < nw; ++w) { sx += kred[w][0]; sy += kred[w][1]; }
+        if (sx) atomicAdd((unsigned long long*)&dev->ksum[0], (unsigned long long)sx);
+        if (sy) atomicAdd((unsigned long long*)&dev->ksum[1], (unsigned long long)sy);
+        __threadfence();
+        last = atomicAdd(&dev->bticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double mx = 0.0, my = 0.0;
+    for (int m = threadIdx.x; m < a.n; m += blockDim.x) {
+        mx += (double)a.FXk[m];
+        my += (double)a.FYk[m];
+    }
+    mx = warp_sum(mx); my = warp_sum(my);
+    if (lane == 0) { dred[warp][0] = mx; dred[warp][1] = my; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tx = 0.0, ty = 0.0;
+        for (int w = 0; w < nw; ++w) { tx += dred[w][0]; ty += dred[w][1]; }
+        const long long s = dev->step + 1;
+        const long long ex = (long long)__ldcg((const unsigned long long*)&dev->ksum[0]);
+        const long long ey = (long long)__ldcg((const unsigned long long*)&dev->ksum[1]);
+        double* h = a.hist + 4 * ((s - 1) % a.hist_cap);
+        h[0] = (double)ex * (double)kForceInvScale;
+        h[1] = (double)ey * (double)kForceInvScale;
+        h[2] = tx;
+        h[3] = ty;
+        dev->ksum[0] = 0;
+        dev->ksum[1] = 0;
+        dev->bticket = 0u;
+        // the previous call's box was consumed by this call's band-prepare
+        for (int e = 0; e < 6; ++e) dev->box[(s + 1) & 1][e] = kBoxEmpty;
+        __threadfence();
+        dev->step = s;
+    }
+}
+
 }  // namespace clbm

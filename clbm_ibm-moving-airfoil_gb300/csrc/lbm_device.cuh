@@ -9,19 +9,32 @@
 namespace clbm {
 
 // 3D Zou-He velocity inlet on the post-stream populations of an x = 0 cell,
-// clbm_moving.py:266-294 (same operation order).
+// clbm_moving.py:266-294, in the same operation order with every operation explicitly
+// rounded (no contraction), so the inlet column repeats the reference's float32 values.
 __device__ __forceinline__ void zou_he(float (&v)[19], const Coef& c) {
     const float ux_in = c.ux_in, uy_in = c.uy_in;
-    float S_known = v[0] + v[3] + v[4] + v[5] + v[6] + v[15] + v[16] + v[17] + v[18];
-    float S_out = v[2] + v[8] + v[10] + v[12] + v[14];
-    float rho_in = (S_known + 2.0f * S_out) / (1.0f - ux_in);
-    float diff_y = v[3] - v[4];
-    float diff_z = v[5] - v[6];
-    v[1] = v[2] + c.c23 * rho_in * ux_in;
-    v[7] = v[10] + c.c16 * rho_in * ux_in + 0.5f * rho_in * uy_in - 0.5f * diff_y;
-    v[9] = v[8] + c.c16 * rho_in * ux_in - 0.5f * rho_in * uy_in + 0.5f * diff_y;
-    v[11] = v[14] + c.c16 * rho_in * ux_in - 0.5f * diff_z;
-    v[13] = v[12] + c.c16 * rho_in * ux_in + 0.5f * diff_z;
+    float S_known = v[0];
+    S_known = __fadd_rn(S_known, v[3]);
+    S_known = __fadd_rn(S_known, v[4]);
+    S_known = __fadd_rn(S_known, v[5]);
+    S_known = __fadd_rn(S_known, v[6]);
+    S_known = __fadd_rn(S_known, v[15]);
+    S_known = __fadd_rn(S_known, v[16]);
+    S_known = __fadd_rn(S_known, v[17]);
+    S_known = __fadd_rn(S_known, v[18]);
+    float S_out = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v[2], v[8]), v[10]), v[12]), v[14]);
+    const float rho_in = __fdiv_rn(__fadd_rn(S_known, __fmul_rn(2.0f, S_out)), __fsub_rn(1.0f, ux_in));
+    const float diff_y = __fsub_rn(v[3], v[4]);
+    const float diff_z = __fsub_rn(v[5], v[6]);
+    const float a23 = __fmul_rn(__fmul_rn(c.c23, rho_in), ux_in);
+    const float a16 = __fmul_rn(__fmul_rn(c.c16, rho_in), ux_in);
+    const float hy = __fmul_rn(__fmul_rn(0.5f, rho_in), uy_in);
+    const float dy = __fmul_rn(0.5f, diff_y), dz = __fmul_rn(0.5f, diff_z);
+    v[1] = __fadd_rn(v[2], a23);
+    v[7] = __fsub_rn(__fadd_rn(__fadd_rn(v[10], a16), hy), dy);
+    v[9] = __fadd_rn(__fsub_rn(__fadd_rn(v[8], a16), hy), dy);
+    v[11] = __fsub_rn(__fadd_rn(v[14], a16), dz);
+    v[13] = __fadd_rn(__fadd_rn(v[12], a16), dz);
 }
 
 // Gather the post-stream, post-boundary populations S(x, y, z) of the stored state.
@@ -140,6 +153,21 @@ __device__ __forceinline__ V1 operator*(V1 a, V1 b) { return {__fmul_rn(a.x, b.x
 __device__ __forceinline__ V1 vfma(V1 a, V1 b, V1 c) { return {__fmaf_rn(a.x, b.x, c.x)}; }
 __device__ __forceinline__ V1 vsplat(float a, V1) { return {a}; }
 __device__ __forceinline__ V1 vrcp(V1 a) { return {__frcp_rn(a.x)}; }
+__device__ __forceinline__ V1 vdiv(V1 a, V1 b) { return {__fdiv_rn(a.x, b.x)}; }
+// x / 3 and x / 9, correctly rounded, without a division instruction sequence: the
+// quotient RN(x * RN(1/d)) corrected once by its exact remainder (Markstein's iteration
+// for division by a constant, P. Markstein, "IA-64 and Elementary Functions", 2000). For
+// d = 3 and d = 9 it returns RN(x / d) for every float x with a normal or zero
+// numerator (checked exhaustively against IEEE division over all positive normal x; the
+// method is odd in x). It does not hold for every divisor, so it is used for these two.
+template <int D>
+__device__ __forceinline__ V1 vdiv_int(V1 x) {
+    static_assert(D == 3 || D == 9, "exactness checked for 3 and 9 only");
+    constexpr float d = (float)D, rd = 1.0f / (float)D;
+    const float q0 = __fmul_rn(x.x, rd);
+    const float rem = __fmaf_rn(-q0, d, x.x);
+    return {__fmaf_rn(rem, rd, q0)};
+}
 
 __device__ __forceinline__ V2 operator+(V2 a, V2 b) {
     V2 d;
@@ -175,6 +203,22 @@ __device__ __forceinline__ V2 vsplat(float a, V2) { return vpack(a, a); }
 __device__ __forceinline__ V2 vrcp(V2 a) {
     const float2 t = vunpack(a);
     return vpack(__frcp_rn(t.x), __frcp_rn(t.y));
+}
+
+// Divergence monitor, the device form of main_moving.py:143-145 (which stops the run when
+// rho_min < 0.3 or a field is not finite on its vis steps): every collision compares its
+// cell's density with the floor; a density below it or not finite (NaN fails both tests)
+// sets a sticky status bit that the host reads between steps or graph replays. Two
+// comparisons per cell on a value the collision computes anyway; no extra memory traffic.
+__device__ __forceinline__ void monitor_rho(const Coef& c, float r) {
+    if (c.status && !(r >= c.rho_floor && r <= 3.0e38f)) atomicOr(c.status, kStatusDiverged);
+}
+__device__ __forceinline__ void monitor_rho(const Coef& c, F1 r) { monitor_rho(c, r.x); }
+__device__ __forceinline__ void monitor_rho(const Coef& c, V1 r) { monitor_rho(c, r.x); }
+__device__ __forceinline__ void monitor_rho(const Coef& c, V2 r) {
+    const float2 t = vunpack(r);
+    monitor_rho(c, t.x);
+    monitor_rho(c, t.y);
 }
 
 // Cascaded collision in central-moment space followed by the raw-moment back transform,
@@ -218,6 +262,7 @@ __device__ __forceinline__ void collide_v(V (&f)[19], const Coef& c, V Fx, V Fy,
         pyy = pyy + third;
         pzz = pzz + third;
     }
+    monitor_rho(c, r);
     const V inv = vrcp(r);
     V u = mx * inv, v = my * inv, w = mz * inv;
     if (FORCE) {
@@ -328,16 +373,213 @@ __device__ __forceinline__ void collide_v(V (&f)[19], const Coef& c, V Fx, V Fy,
     }
 }
 
-// Scalar entry point: one cell held as float[19] (F1 for float32 storage, V1 for the
-// shifted 16-bit forms).
+// Float32 storage: the collision in the reference's own operation order wherever that
+// order is cheap to keep, every operation explicitly rounded (V1, no contraction):
+//  * rho and the momentum as sums over q in q order, u = m / rho + (F / 2) / rho
+//    (_macro_with_force, clbm_moving.py:105-115);
+//  * the relaxation with its divisions by 3 and 9 (clbm_moving.py:170-196);
+//  * the raw post-collision moments T term by term, left to right (clbm_moving.py:198-231;
+//    the third-order central moments are zero there, and adding a zero is exact);
+//  * the back transform f*_q = sum_j M_raw^-1[q][j] T_j summed over j in order
+//    (clbm_moving.py:233-238). The entries of M_raw^-1 (config_moving.py:62-73) are 0,
+//    +-1/4, +-1/2 and +-1: every product is exact and the zero terms add nothing, so the
+//    91 non-zero terms summed in j order round exactly as the reference's dense 19 x 19 loop
+//    does for the same T (a common factor 1/2 or 1/4 is applied after the sum, which scales
+//    every rounding by that power of two).
+// Keeping the back transform's summation order matters for mass: in a nearly uniform flow
+// every cell rounds the same values the same way, so a summation order whose roundings do
+// not cancel over the 19 populations shifts the total mass by the same amount in every cell
+// and step.
+// Unforced cells (nearly all of them) take the second-order central moments from the raw
+// moments (pair sums, shifted by the velocity) instead of the reference's 19-term sums of
+// f (e - u)^p, which would cost about 500 more operations per cell. Forced cells -- the
+// IBM force box, a few per cent of the lattice, run by their own pass -- take the
+// reference's sums and its Guo term too, so where the body acts the step repeats the
+// reference's arithmetic operation for operation.
+struct RefMacro {
+    V1 r, mx, my, mz, u, v, w;
+};
+
+template <bool FORCE>
+__device__ __forceinline__ RefMacro ref_macro(const V1 (&f)[19], const Coef& c, V1 Fx, V1 Fy,
+                                              V1 Fz) {
+    using V = V1;
+    RefMacro m;
+    // _macro_with_force: r += f_q, m += e_q f_q in q order (e_q f_q is +-f_q or an exact 0)
+    V r = f[0];
+#pragma unroll
+    for (int q = 1; q < 19; ++q) r = r + f[q];
+    monitor_rho(c, r);
+    m.r = r;
+    m.mx = ((((((((f[1] - f[2]) + f[7]) - f[8]) + f[9]) - f[10]) + f[11]) - f[12]) + f[13]) - f[14];
+    m.my = ((((((((f[3] - f[4]) + f[7]) + f[8]) - f[9]) - f[10]) + f[15]) - f[16]) + f[17]) - f[18];
+    m.mz = ((((((((f[5] - f[6]) + f[11]) + f[12]) - f[13]) - f[14]) + f[15]) + f[16]) - f[17]) - f[18];
+    m.u = vdiv(m.mx, r);
+    m.v = vdiv(m.my, r);
+    m.w = vdiv(m.mz, r);
+    if (FORCE) {
+        const V half = vsplat(0.5f, r);
+        m.u = m.u + vdiv(half * Fx, r);
+        m.v = m.v + vdiv(half * Fy, r);
+        m.w = m.w + vdiv(half * Fz, r);
+    }
+    return m;
+}
+
+// Relaxation, raw post-collision moments and back transform from the second-order
+// central moments (clbm_moving.py:170-238); writes f.
+__device__ __forceinline__ void ref_relax_back(V1 (&f)[19], const Coef& c, const RefMacro& m,
+                                               V1 k200, V1 k020, V1 k002, V1 k110, V1 k101,
+                                               V1 k011, V1 osv) {
+    using V = V1;
+    const V r = m.r, u = m.u, v = m.v, w = m.w;
+    const V half = vsplat(0.5f, r), quarter = vsplat(0.25f, r), two = vsplat(2.0f, r);
+    const V four = vsplat(4.0f, r);
+    // cascade relaxation, clbm_moving.py:170-196
+    const V k110s = k110 * osv, k101s = k101 * osv, k011s = k011 * osv;
+    const V kA = (k200 + k020) + k002;
+    const V kAs = kA - vsplat(c.s_e, r) * (kA - r);
+    const V kDs = (k200 - k020) * osv, kEs = (k200 - k002) * osv;
+    const V k200s = vdiv_int<3>((kAs + kDs) + kEs);
+    const V k020s = vdiv_int<3>((kAs - two * kDs) + kEs);
+    const V k002s = vdiv_int<3>((kAs + kDs) - two * kEs);
+    const V r9 = vdiv_int<9>(r);
+    // raw post-collision moments, clbm_moving.py:198-231
+    const V ur = u * r, vr = v * r, wr = w * r;
+    const V uu = u * u, vv = v * v, ww = w * w, uv = u * v, uw = u * w, vw = v * w;
+    const V T110 = k110s + uv * r, T101 = k101s + uw * r, T011 = k011s + vw * r;
+    const V T200 = k200s + uu * r, T020 = k020s + vv * r, T002 = k002s + ww * r;
+    const V T210 = ((two * u) * k110s + v * k200s) + (uu * v) * r;
+    const V T120 = ((two * v) * k110s + u * k020s) + (uv * v) * r;
+    const V T201 = ((two * u) * k101s + w * k200s) + (uu * w) * r;
+    const V T021 = ((two * v) * k011s + w * k020s) + (vv * w) * r;
+    const V T102 = ((two * w) * k101s + u * k002s) + (uw * w) * r;
+    const V T012 = ((two * w) * k011s + v * k002s) + (vw * w) * r;
+    const V T220 = (((r9 + ((four * u) * v) * k110s) + vv * k200s) + uu * k020s) + ((uu * v) * v) * r;
+    const V T202 = (((r9 + ((four * u) * w) * k101s) + ww * k200s) + uu * k002s) + ((uu * w) * w) * r;
+    const V T022 = (((r9 + ((four * v) * w) * k011s) + ww * k020s) + vv * k002s) + ((vv * w) * w) * r;
+    // back transform: non-zero terms of each row of M_raw^-1 in column order
+    f[0] = (((((r - T200) - T020) - T002) + T220) + T202) + T022;
+    f[1] = half * ((((((ur + T200) - T120) - T102) - T220) - T202));
+    f[2] = half * ((((((T200 - ur) + T120) + T102) - T220) - T202));
+    f[3] = half * ((((((vr + T020) - T210) - T012) - T220) - T022));
+    f[4] = half * ((((((T020 - vr) + T210) + T012) - T220) - T022));
+    f[5] = half * ((((((wr + T002) - T201) - T021) - T202) - T022));
+    f[6] = half * ((((((T002 - wr) + T201) + T021) - T202) - T022));
+    f[7] = quarter * (((T110 + T210) + T120) + T220);
+    f[8] = quarter * (((T210 - T110) - T120) + T220);
+    f[9] = quarter * ((T120 - (T110 + T210)) + T220);
+    f[10] = quarter * (((T110 - T210) - T120) + T220);
+    f[11] = quarter * (((T101 + T201) + T102) + T202);
+    f[12] = quarter * (((T201 - T101) - T102) + T202);
+    f[13] = quarter * ((T102 - (T101 + T201)) + T202);
+    f[14] = quarter * (((T101 - T201) - T102) + T202);
+    f[15] = quarter * (((T011 + T021) + T012) + T022);
+    f[16] = quarter * (((T021 - T011) - T012) + T022);
+    f[17] = quarter * ((T012 - (T011 + T021)) + T022);
+    f[18] = quarter * (((T011 - T021) - T012) + T022);
+}
+
+// Unforced float32 collision (the bulk of the lattice).
+template <bool SVC = false>
+__device__ __forceinline__ void collide_ref(V1 (&f)[19], const Coef& c, V1 osv_cell = V1{}) {
+    using V = V1;
+    const V zero = vsplat(0.0f, f[0]), m_two = vsplat(-2.0f, f[0]);
+    const RefMacro m = ref_macro<false>(f, c, zero, zero, zero);
+    const V r = m.r, u = m.u, v = m.v, w = m.w;
+    // second-order raw moments from pair sums, central moments about u
+    const V sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+    const V a = f[7] + f[8], b = f[9] + f[10], cc = f[11] + f[12], d = f[13] + f[14];
+    const V e = f[15] + f[16], h = f[17] + f[18];
+    const V ab = a + b, cd = cc + d, eh = e + h;
+    const V pxx = (sx + ab) + cd, pyy = (sy + ab) + eh, pzz = (sz + cd) + eh;
+    const V pxy = (f[7] + f[10]) - (f[8] + f[9]);
+    const V pxz = (f[11] + f[14]) - (f[12] + f[13]);
+    const V pyz = (f[15] + f[18]) - (f[16] + f[17]);
+    const V ur = u * r, vr = v * r, wr = w * r;
+    const V k200 = vfma(u, vfma(m_two, m.mx, ur), pxx);
+    const V k020 = vfma(v, vfma(m_two, m.my, vr), pyy);
+    const V k002 = vfma(w, vfma(m_two, m.mz, wr), pzz);
+    const V k110 = pxy - vfma(u, m.my - vr, v * m.mx);
+    const V k101 = pxz - vfma(u, m.mz - wr, w * m.mx);
+    const V k011 = pyz - vfma(v, m.mz - wr, w * m.my);
+    const V osv = SVC ? osv_cell : vsplat(c.one_m_sv, r);
+    ref_relax_back(f, c, m, k200, k020, k002, k110, k101, k011, osv);
+}
+
+// Forced float32 collision: _macro_with_force, the central moments as the reference's sums
+// over q of f_q (e_q - u)^p (clbm_moving.py:139-168), relaxation and back transform as
+// above, and the Guo term as the reference writes it (clbm_moving.py:240-249):
+// f*_q += (w_q (1 - s_v / 2)) [((e - u) / cs2 + (e.u) e / cs2^2) . F], with the float32
+// constants cs2 = 1/3 and cs2^2. (e_a - u_a) / cs2 takes three values per axis and
+// (e.u) e_a / cs2^2 is +-(e.u) / cs2^2 or an exact zero, with (e.u) of opposite directions
+// exact negatives, so 18 divisions give every quotient the reference forms.
+__device__ __forceinline__ void collide_ref_forced(V1 (&f)[19], const Coef& c, V1 Fx, V1 Fy,
+                                                   V1 Fz) {
+    using V = V1;
+    const V zero = vsplat(0.0f, f[0]);
+    const RefMacro m = ref_macro<true>(f, c, Fx, Fy, Fz);
+    const V u = m.u, v = m.v, w = m.w;
+    V k110 = zero, k101 = zero, k011 = zero, k200 = zero, k020 = zero, k002 = zero;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const V xix = vsplat((float)ex(q), zero) - u;
+        const V xiy = vsplat((float)ey(q), zero) - v;
+        const V xiz = vsplat((float)ez(q), zero) - w;
+        const V fx_ = f[q] * xix, fy_ = f[q] * xiy;
+        k110 = k110 + fx_ * xiy;
+        k101 = k101 + fx_ * xiz;
+        k011 = k011 + fy_ * xiz;
+        k200 = k200 + f[q] * (xix * xix);
+        k020 = k020 + f[q] * (xiy * xiy);
+        k002 = k002 + f[q] * (xiz * xiz);
+    }
+    ref_relax_back(f, c, m, k200, k020, k002, k110, k101, k011, vsplat(c.one_m_sv, zero));
+    const V cs2 = vsplat(1.0f / 3.0f, zero);
+    const V cs4 = vsplat((float)((1.0 / 3.0) * (1.0 / 3.0)), zero);
+    const V one = vsplat(1.0f, zero);
+    // (e_a - u_a) / cs2 for e_a = -1, 0, +1
+    const V Ax[3] = {vdiv(zero - one - u, cs2), vdiv(zero - u, cs2), vdiv(one - u, cs2)};
+    const V Ay[3] = {vdiv(zero - one - v, cs2), vdiv(zero - v, cs2), vdiv(one - v, cs2)};
+    const V Az[3] = {vdiv(zero - one - w, cs2), vdiv(zero - w, cs2), vdiv(one - w, cs2)};
+    // (e.u) / cs2^2 of the first direction of each opposite pair (clbm_moving.py order
+    // x, y, z within e.u); the opposite direction takes its negative
+    V D[19];
+    D[0] = zero;
+#pragma unroll
+    for (int q = 1; q < 19; ++q) {
+        if (opposite(q) < q) {
+            D[q] = zero - D[opposite(q)];
+            continue;
+        }
+        V eu = zero;
+        bool first = true;
+        if (ex(q) != 0) { eu = ex(q) > 0 ? u : zero - u; first = false; }
+        if (ey(q) != 0) { const V t = ey(q) > 0 ? v : zero - v; eu = first ? t : eu + t; first = false; }
+        if (ez(q) != 0) { const V t = ez(q) > 0 ? w : zero - w; eu = first ? t : eu + t; first = false; }
+        D[q] = vdiv(eu, cs4);
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const V cx = ex(q) == 0 ? Ax[1] : (ex(q) > 0 ? Ax[2] + D[q] : Ax[0] - D[q]);
+        const V cy = ey(q) == 0 ? Ay[1] : (ey(q) > 0 ? Ay[2] + D[q] : Ay[0] - D[q]);
+        const V cz = ez(q) == 0 ? Az[1] : (ez(q) > 0 ? Az[2] + D[q] : Az[0] - D[q]);
+        f[q] = f[q] + vsplat(c.wc[q], zero) * ((cx * Fx + cy * Fy) + cz * Fz);
+    }
+}
+
+// Scalar entry point: one cell held as float[19]; float32 storage collides in the
+// reference's order (collide_ref), the shifted 16-bit forms on the deviations (V1, the
+// same rounded operations as the packed two-cell form).
 template <bool FORCE, bool DEV = false>
 __device__ __forceinline__ void collide(float (&f)[19], const Coef& c, float Fx, float Fy,
                                         float Fz) {
-    using V = typename std::conditional<DEV, V1, F1>::type;
-    V t[19];
+    V1 t[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) t[q].x = f[q];
-    collide_v<V, FORCE, DEV>(t, c, V{Fx}, V{Fy}, V{Fz});
+    if (DEV) collide_v<V1, FORCE, true>(t, c, V1{Fx}, V1{Fy}, V1{Fz});
+    else if (FORCE) collide_ref_forced(t, c, V1{Fx}, V1{Fy}, V1{Fz});
+    else collide_ref(t, c);
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = t[q].x;
 }
@@ -359,11 +601,11 @@ __device__ __forceinline__ void collide_ho(float (&f)[19], const Coef& c, const 
 // One cell whose deviatoric second-order moments relax with 1 - osv (closure).
 template <bool DEV>
 __device__ __forceinline__ void collide_sv(float (&f)[19], const Coef& c, float osv) {
-    using V = typename std::conditional<DEV, V1, F1>::type;
-    V t[19];
+    V1 t[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) t[q].x = f[q];
-    collide_v<V, false, DEV, false, true>(t, c, V{0.f}, V{0.f}, V{0.f}, nullptr, V{osv});
+    if (DEV) collide_v<V1, false, true, false, true>(t, c, V1{0.f}, V1{0.f}, V1{0.f}, nullptr, V1{osv});
+    else collide_ref<true>(t, c, V1{osv});
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = t[q].x;
 }
@@ -612,12 +854,16 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
     store_raw<S>(fout, g, cell, f);
 }
 
-// Forced stream-collide of box cell t of band b (the box pass, one cell).
-template <int S, bool PULL>
+// Forced stream-collide of box cell t of band b (the box pass, one cell). SUMS: also add
+// the cell's clipped force, in units of 2^-40, to kx, ky (the Eulerian part of the
+// lift/drag sums; every clipped value is an integer multiple of 2^-40, so the integer sums
+// are exact in any order).
+template <int S, bool PULL, bool SUMS = false>
 __device__ __forceinline__ void box_pass_cell(const typename Pop<S>::T* __restrict__ fin,
                                               typename Pop<S>::T* __restrict__ fout,
                                               const Grid& g, const Coef& c, const ForceArgs& fa,
-                                              const Band& b, int t) {
+                                              const Band& b, int t, long long* kx = nullptr,
+                                              long long* ky = nullptr) {
     int x, y, z;
     box_cell(b, g.ny, g.nz, t, x, y, z);
     float f[19];
@@ -625,6 +871,10 @@ __device__ __forceinline__ void box_pass_cell(const typename Pop<S>::T* __restri
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
     const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
     const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+    if (SUMS) {
+        *kx += (long long)(Fx * kForceScale);
+        *ky += (long long)(Fy * kForceScale);
+    }
     collide<true, Pop<S>::kShifted>(f, c, Fx, Fy, 0.0f);
     store_raw<S>(fout, g, cell, f);
 }

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdlib>
 
+#include "ibm_device.cuh"
 #include "lbm_device.cuh"
 
 namespace clbm {
@@ -40,6 +41,20 @@ __global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S
                                                             typename Pop<S>::T* __restrict__ fout,
                                                             Grid g, Coef c, ForceArgs fa) {
     box_pass_body<S, PULL>(fin, fout, g, c, fa, blockIdx.x, gridDim.x);
+}
+
+// The box pass of a step that also completes its IBM call: force sums into the history
+// ring (ibm_box_sums_tail) instead of a separate force-sum kernel.
+template <int S, bool PULL>
+__global__ void __launch_bounds__(256) k_stream_collide_box_sums(const typename Pop<S>::T* __restrict__ fin,
+                                                                 typename Pop<S>::T* __restrict__ fout,
+                                                                 Grid g, Coef c, ForceArgs fa, IbmArrays a) {
+    const Band b = load_band(fa.dev, fa.slot);
+    const int cells = b.ilen * b.jlen * b.klen;
+    long long kx = 0, ky = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells; t += gridDim.x * blockDim.x)
+        box_pass_cell<S, PULL, true>(fin, fout, g, c, fa, b, t, &kx, &ky);
+    ibm_box_sums_tail(a, kx, ky);
 }
 
 // ------------------------------------------------------------------ 16-bit pair kernel
@@ -312,15 +327,25 @@ __device__ __forceinline__ unsigned int ordered(float v) {
 }
 
 // _macro_post (clbm_moving.py:305-321) over the whole grid, plus divergence statistics.
+// Grid-stride over row segments of kBX cells: a block of kBX threads takes segments
+// blockIdx.x, blockIdx.x + gridDim.x, ... (segment t: x block t % nxb, row t / nxb), keeps
+// its statistics in registers, and reduces them once at the end (warp shuffles, then shared
+// memory), so the four global atomics on the same words are made once per block instead of
+// once per warp of the lattice.
 template <int S, bool PULL>
-__global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
-                             float* rho, float* ux, float* uy, float* uz,
-                             unsigned long long* stats) {
-    const int x = blockIdx.x * kBX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
+__global__ void __launch_bounds__(kBX) k_macro_full(const typename Pop<S>::T* __restrict__ fin,
+                                                    Grid g, Coef c, float* rho, float* ux,
+                                                    float* uy, float* uz,
+                                                    unsigned long long* stats) {
+    const int nxb = (g.nx + kBX - 1) / kBX;
+    const long long segs = (long long)nxb * g.ny * g.nz;
     unsigned int rmin = 0xffffffffu, rmax = 0u, u2max = 0u;
     unsigned int bad = 0;
-    if (x < g.nx) {
+    for (long long t = blockIdx.x; t < segs; t += gridDim.x) {
+        const int x = (int)(t % nxb) * kBX + threadIdx.x;
+        const long long row = t / nxb;
+        const int y = (int)(row % g.ny), z = (int)(row / g.ny);
+        if (x >= g.nx) continue;
         float f[19];
         gather<S, PULL>(fin, g, c, x, y, z, f);
         float r = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
@@ -332,7 +357,7 @@ __global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g,
             mz += (float)ez(q) * f[q];
         }
         const float u = mx / r, v = my / r, w = mz / r;
-        const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+        const long long cell = (row * g.pitch) + x;
         rho[cell] = r;
         ux[cell] = u;
         uy[cell] = v;
@@ -340,10 +365,11 @@ __global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g,
         if (stats) {
             const float u2 = u * u + v * v + w * w;
             if (!isfinite(r) || !isfinite(u2)) {
-                bad = 1;
+                bad += 1;
             } else {
-                rmin = rmax = ordered(r);
-                u2max = ordered(u2);
+                rmin = min(rmin, ordered(r));
+                rmax = max(rmax, ordered(r));
+                u2max = max(u2max, ordered(u2));
             }
         }
     }
@@ -354,7 +380,19 @@ __global__ void k_macro_full(const typename Pop<S>::T* __restrict__ fin, Grid g,
         u2max = max(u2max, __shfl_xor_sync(0xffffffffu, u2max, o));
         bad += __shfl_xor_sync(0xffffffffu, bad, o);
     }
+    __shared__ unsigned int red[kBX / 32][4];
+    const int warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
+        red[warp][0] = rmin; red[warp][1] = rmax; red[warp][2] = u2max; red[warp][3] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kBX / 32; ++k) {
+            rmin = min(rmin, red[k][0]);
+            rmax = max(rmax, red[k][1]);
+            u2max = max(u2max, red[k][2]);
+            bad += red[k][3];
+        }
         if (rmin != 0xffffffffu) {
             atomicMin(stats + 0, (unsigned long long)rmin);
             atomicMax(stats + 1, (unsigned long long)rmax);
@@ -471,6 +509,19 @@ __global__ void k_fill_macro(Grid g, Coef c, float* rho, float* ux, float* uy, f
 // ---------------------------------------------------------------- launchers
 static dim3 cell_grid(const Grid& g) { return dim3((g.nx + kBX - 1) / kBX, g.ny, g.nz); }
 
+// Blocks of the grid-stride macro pass: 16 resident blocks of kBX threads per SM.
+static int macro_full_blocks() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            sms = 148;
+        n = sms * 16;
+    }
+    return n;
+}
+
 #define CLBM_DISPATCH_STORE(storage, ...)                                                  \
     switch (storage) {                                                                     \
         case CLBM_STORE_F32: { constexpr int S_ = CLBM_STORE_F32; __VA_ARGS__; } break;   \
@@ -548,13 +599,26 @@ void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fo
     });
 }
 
+void launch_stream_collide_box_sums(int storage, bool pull, const void* fin, void* fout,
+                                    const Grid& g, const Coef& c, const ForceArgs& fa,
+                                    const IbmArrays& a, long long max_cells, cudaStream_t st) {
+    const int blocks = box_blocks(max_cells, 256);
+    CLBM_DISPATCH_STORE(storage, {
+        using T = typename Pop<S_>::T;
+        if (pull) k_stream_collide_box_sums<S_, true><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);
+        else k_stream_collide_box_sums<S_, false><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);
+    });
+}
+
 void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
                        float* rho, float* ux, float* uy, float* uz,
                        unsigned long long* stats, cudaStream_t st) {
     CLBM_DISPATCH_STORE(storage, {
         using T = typename Pop<S_>::T;
-        if (pull) k_macro_full<S_, true><<<cell_grid(g), kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
-        else k_macro_full<S_, false><<<cell_grid(g), kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
+        const long long segs = (long long)((g.nx + kBX - 1) / kBX) * g.ny * g.nz;
+        const int blocks = (int)std::min<long long>(segs, macro_full_blocks());
+        if (pull) k_macro_full<S_, true><<<blocks, kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
+        else k_macro_full<S_, false><<<blocks, kBX, 0, st>>>((const T*)f, g, c, rho, ux, uy, uz, stats);
     });
 }
 

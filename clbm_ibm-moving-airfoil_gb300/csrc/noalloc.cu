@@ -4,12 +4,18 @@
 // kernel of an IBM step (sum of the clipped Eulerian force over all cells and sum of the
 // marker forces), but over force fields and marker forces that the caller already holds in
 // device memory, for example fields produced by another solver component or exported into
-// a framework tensor. Some callers cannot call cudaMalloc at this point: code that runs
-// while another library captures a CUDA graph (allocation is not capturable), code inside
-// a real-time loop whose memory budget is fixed up front, or hosts whose device memory is
-// owned by a pool allocator they cannot reach. For them this entry point allocates
-// nothing: its per-block partial sums live in a file-scope __device__ array of fixed size,
-// which every GPU that loads this library holds until the process exits.
+// a framework tensor. Some callers cannot call cudaMalloc at this point: a real-time loop
+// whose memory budget is fixed up front, or a host whose device memory is owned by a pool
+// allocator it cannot reach (an allocation outside that pool would fail or fragment it).
+// For them this entry point allocates nothing: its per-block partial sums live in a
+// file-scope __device__ array of fixed size, which every GPU that loads this library holds
+// until the process exits.
+//
+// The call is synchronous: it ends by copying the sums to host memory and waiting for
+// `stream`. A stream that is being captured into a CUDA graph cannot do either, so a call
+// on a capturing stream (or on the legacy default stream while another stream captures in
+// global mode) is refused with CLBM_ERR_STATE before any work is issued, and the caller's
+// capture stays valid.
 #include <cstdio>
 #include <mutex>
 
@@ -123,9 +129,27 @@ extern "C" int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return nfail(CLBM_ERR_CUDA, "ibm_force_sums_noalloc: no usable current CUDA device");
+    cudaStream_t st = (cudaStream_t)stream;
+    // Refuse a stream under capture before issuing anything: the call ends with a copy to
+    // host memory and a stream synchronisation, which a capture does not allow. On the
+    // legacy default stream the query itself fails while another stream captures in global
+    // mode (cudaErrorStreamCaptureImplicit, which leaves that capture valid).
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        const cudaError_t qe = cudaStreamIsCapturing(st, &cs);
+        if (qe != cudaSuccess) (void)cudaGetLastError();  // the query's own error, not the caller's
+        if (qe == cudaErrorStreamCaptureImplicit || (qe == cudaSuccess && cs != cudaStreamCaptureStatusNone))
+            return nfail(CLBM_ERR_STATE,
+                         "ibm_force_sums_noalloc: the stream is being captured into a CUDA graph; "
+                         "the call copies to host memory and waits for the stream, so it must "
+                         "run outside capture");
+        if (qe != cudaSuccess)
+            return nfail(CLBM_ERR_CUDA, "ibm_force_sums_noalloc: cudaStreamIsCapturing failed");
+    }
     // One-time set-up per device, with that device current: device addresses of the
-    // file-scope scratch. The first call on a device therefore makes runtime calls that are
-    // not allowed during stream capture; make it before any capture begins.
+    // file-scope scratch, looked up once and kept for the life of the process (so
+    // cudaDeviceReset while this library is in use is not supported: the kept addresses
+    // would belong to the destroyed context).
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
         if (!g_ready[dev]) {
@@ -139,7 +163,16 @@ extern "C" int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t 
         }
     }
     const Scratch& sc = g_scratch[dev];
-    cudaStream_t st = (cudaStream_t)stream;
+    // An error left pending by the caller's own earlier work is reported as such and left
+    // for the caller to read (cudaPeekAtLastError does not clear it).
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        char buf[256];
+        snprintf(buf, sizeof(buf),
+                 "ibm_force_sums_noalloc: a CUDA error from earlier work is pending (%s); "
+                 "nothing was launched", cudaGetErrorName(pending));
+        return nfail(CLBM_ERR_CUDA, buf);
+    }
     // The array keeps the last call's contents: clear the ticket that must start at zero.
     if (cudaMemsetAsync(sc.ticket, 0, sizeof(unsigned int), st) != cudaSuccess)
         return nfail(CLBM_ERR_CUDA, "ibm_force_sums_noalloc: cudaMemsetAsync failed");

@@ -108,7 +108,14 @@ class Solver:
                              int(nsteps), 1 if graph else 0))
 
     def synchronize(self):
+        """Wait for the solver's work; raises DivergedError when the device divergence
+        monitor fired (a collision met a density below the floor or not finite)."""
         check(lib().clbm_synchronize(self._h))
+
+    def set_rho_floor(self, rho_floor):
+        """Density floor of the device divergence monitor (default 0.3, the threshold of
+        main_moving.py:143); a negative floor keeps only the non-finite test."""
+        check(lib().clbm_set_rho_floor(self._h, float(rho_floor)))
 
     def selftest_wait_timeout(self, spin_limit=4096):
         """Make one staged launch's bounded wait run out on purpose; returns the error the

@@ -22,7 +22,7 @@ extern "C" {
 #define CLBM_OK 0
 #define CLBM_ERR_CUDA 1     /* a CUDA runtime call failed */
 #define CLBM_ERR_ARG 2      /* invalid argument or configuration */
-#define CLBM_ERR_DIVERGED 3 /* non-finite or rho < threshold found by clbm_check */
+#define CLBM_ERR_DIVERGED 3 /* non-finite or rho < threshold (clbm_check, device monitor) */
 #define CLBM_ERR_STATE 4    /* call not valid in the current state */
 
 /* Population storage forms. F32 stores f_q; the shifted forms store f_q - w_q. */
@@ -81,12 +81,14 @@ int clbm_read_vorticity_slice(clbm_solver* s, int32_t z, float* out);
 
 /* lbm.f.to_numpy(): post-stream, post-boundary populations (Nx, Ny, Nz, 19) float32. */
 int clbm_read_populations(clbm_solver* s, float* f_host);
-/* lbm.f.from_numpy(): replace the state by host populations (Nx, Ny, Nz, 19). */
+/* lbm.f.from_numpy(): replace the state by host populations (Nx, Ny, Nz, 19). Clears the
+ * device status word (a new state starts with a clean divergence record). */
 int clbm_write_populations(clbm_solver* s, const float* f_host);
 
 /* Divergence statistics of the current state (main_moving.py:130-145): rho min/max,
  * max |u| and the count of non-finite rho/u values. Returns CLBM_ERR_DIVERGED when
- * nonfinite > 0 or rho_min < rho_floor. */
+ * nonfinite > 0 or rho_min < rho_floor, or when the device divergence monitor (see
+ * clbm_set_rho_floor) recorded a bad density since the state was last written. */
 int clbm_check(clbm_solver* s, double rho_floor, double* rho_min, double* rho_max,
                double* u_max, int64_t* nonfinite);
 
@@ -123,17 +125,22 @@ int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out);
 int ibm_step_count(const clbm_ibm* ibm, int64_t* out);
 
 /* No counterpart in the reference. Allocation-free force sums for callers that cannot call
- * cudaMalloc (code running while another library captures a CUDA graph, real-time loops
- * with a fixed memory budget, hosts whose device memory belongs to a pool they cannot
- * reach): the same sums as one entry of ibm_read_force_history -- sum of fx, fy clipped to
- * +-0.05 over all cells, and sum of FX_k, FY_k -- over caller-owned device arrays fx, fy in
- * the reference layout (Nx, Ny, Nz) and FXk, FYk (n markers; may be NULL when n == 0),
+ * cudaMalloc when they need lift/drag: real-time loops whose device memory budget is fixed
+ * up front, and hosts whose device memory belongs to a pool allocator they cannot reach.
+ * Computes the same sums as one entry of ibm_read_force_history -- sum of fx, fy clipped
+ * to +-0.05 over all cells, and sum of FX_k, FY_k -- over caller-owned device arrays fx, fy
+ * in the reference layout (Nx, Ny, Nz) and FXk, FYk (n markers; may be NULL when n == 0),
  * written to host out[4]. Runs on `stream` (a cudaStream_t; NULL for the default stream)
- * and waits for it. Its scratch is a fixed file-scope device array that every GPU loading
- * this library holds until exit; lattices above 67,108,864 cells are rejected with
- * CLBM_ERR_ARG. The first call on a device looks up that array's device address, a
- * runtime call that must not happen during stream capture, so make the first call before
- * capturing. All calls on a device share the array: calls that overlap on the GPU race. */
+ * and is synchronous: it copies the sums to host memory and waits for `stream` before it
+ * returns. It must therefore run outside stream capture: a call on a stream that is being
+ * captured is refused with CLBM_ERR_STATE before any work is issued (the capture stays
+ * valid). Its scratch is a fixed file-scope device array that every GPU loading this
+ * library holds until exit; lattices above 67,108,864 cells are rejected with
+ * CLBM_ERR_ARG. All calls on a device share the array: calls that overlap on the GPU (on
+ * different streams or host threads) race and must not be made. A CUDA error already
+ * pending from the caller's own work is reported (CLBM_ERR_CUDA) and left pending. The
+ * array's device address is looked up on the first call on each device and kept, so
+ * cudaDeviceReset is not supported while this library is in use. */
 int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t nx, int32_t ny, int32_t nz,
                            const float* FXk, const float* FYk, int32_t n, void* stream,
                            double* out);
@@ -141,7 +148,11 @@ int ibm_force_sums_noalloc(const float* fx, const float* fy, int32_t nx, int32_t
 /* The driver loop of main_moving.py:116-122 for nsteps steps: per step
  * ibm_compute_force_motion then clbm_step. use_graph != 0: eight steps are captured once
  * into a CUDA graph (motion law on the device) and replayed; a remainder below eight runs as
- * direct launches (motion law on the host). ibm may be NULL (zero force). */
+ * direct launches (motion law on the host). ibm may be NULL (zero force). Graph replays
+ * stop themselves on divergence (main_moving.py:143-145): each replay copies the device
+ * status word to pinned host memory, at most four replays are in flight, and when the
+ * divergence monitor has fired the call returns CLBM_ERR_DIVERGED within five replays (40
+ * steps) of the step that diverged. */
 int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps,
              int32_t use_graph);
 
@@ -169,8 +180,18 @@ int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* b
                          int64_t* tiles, float* bulk_ms);
 int clbm_ensemble_destroy(clbm_ensemble* e);
 
-/* Wait for all queued work of the solver. */
+/* Wait for all queued work of the solver. Returns CLBM_ERR_STATE when a bounded device
+ * wait gave up, CLBM_ERR_DIVERGED when the divergence monitor fired. */
 int clbm_synchronize(clbm_solver* s);
+
+/* Divergence monitor (the device form of main_moving.py:143-145, which stops a run when
+ * rho_min < 0.3 or a field is not finite): every collision of every step compares its
+ * cell's density with this floor, and a density below it or not finite sets a sticky
+ * bit of the device status word, reported by clbm_synchronize, clbm_check and clbm_run.
+ * Default 0.3; a negative floor keeps only the non-finite test. Set it before creating an
+ * ensemble that holds this solver (the ensemble copies the coefficients). No reference
+ * counterpart beyond the host check it replaces. */
+int clbm_set_rho_floor(clbm_solver* s, double rho_floor);
 
 /* Failure-detection self test (no counterpart in the reference, which has no device
  * waits): runs one launch of the shared-memory-staged stream-collide kernel whose block

@@ -30,9 +30,19 @@ def test_library_exports_every_declared_symbol(built_pkg):
 
 
 def test_library_is_built_for_sm103a(built_pkg):
-    path = built_pkg.lib_path()
-    data = open(path, "rb").read()
-    assert b"sm_103a" in data or b"sm_103" in data
+    """Every nvcc command that produced the library (recorded by the build) targets
+    sm_103a and nothing else."""
+    import json
+    from importlib import import_module
+    b = import_module(built_pkg.__name__ + ".build")
+    assert b.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    info = json.load(open(b.INFO))
+    assert info["arch"] == b.ARCH
+    assert len(info["commands"]) == len(b.SOURCES) + 1
+    for cmd in info["commands"]:
+        gencodes = [cmd[i + 1] for i, a in enumerate(cmd) if a == "-gencode"]
+        assert gencodes == ["arch=compute_103a,code=sm_103a"], cmd
+        assert not any(a.startswith(("-arch", "--gpu-architecture", "-code")) for a in cmd), cmd
 
 
 @pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU error path")

@@ -57,6 +57,34 @@ def test_host_forces_match_oracle(gpkg, oracle_mod):
     assert rel_l2(m["ux"], ux) < 1e-5 and rel_l2(m["uy"], uy) < 1e-4 and rel_l2(m["uz"], uz) < 1e-4
 
 
+@pytest.mark.parametrize("variant", ["cell", "staged"])
+def test_forced_float32_steps_repeat_reference_arithmetic(gpkg, oracle_mod, monkeypatch, variant):
+    """Forced float32 cells (the IBM force box; here every cell, through caller-supplied
+    forces) collide with the reference's own arithmetic operation for operation --
+    _macro_with_force, central moments as 19-term sums, relaxation, raw moments, the back
+    transform in M_raw^-1 column order and the Guo term (clbm_moving.py:96-249) -- and the
+    streaming, Zou-He inlet and outlet copy are exact or in the reference's order: steps
+    from the same state give the oracle's populations and macroscopic fields bit for bit."""
+    monkeypatch.setenv("CLBM_KERNEL", variant)
+    shape = (37, 12, 5)
+    f = _random_state(shape, seed=11)
+    rng = np.random.default_rng(12)
+    F = [(2e-3 * rng.standard_normal(shape)).astype(np.float32) for _ in range(3)]
+    s = gpkg.Solver(*shape, 1.42, 1.0, 0.048, -0.007)
+    o = oracle_mod.Oracle(*shape, 1.42, 1.0, 0.048, -0.007, [], [], [])
+    s.write_populations(f)
+    o.set_f(f)
+    o.set_forces(*F)
+    for _ in range(6):
+        s.step_host_force(*F)
+        o.lbm_step()
+    np.testing.assert_array_equal(s.read_populations(), o.f())
+    m = s.read_macro()
+    for k, v in zip(("rho", "ux", "uy", "uz"), o.macro()):
+        np.testing.assert_array_equal(m[k], v, err_msg=k)
+    s.close()
+
+
 def test_divergence_is_reported(gpkg):
     s = gpkg.Solver(20, 8, 4, 1.5)
     st = s.check()
@@ -72,6 +100,51 @@ def test_divergence_is_reported(gpkg):
     s.write_populations(f)
     with pytest.raises(gpkg.DivergedError):
         s.check(rho_floor=0.3)
+    s.close()
+
+
+def test_graph_replayed_run_stops_itself_on_divergence(gpkg):
+    """The device divergence monitor (every collision tests its density) inside the captured
+    time loop: a NaN injected host-side makes a graph-replayed run stop on its own within
+    five replays, instead of running its 400 steps, and clbm_synchronize keeps reporting it
+    until a new state is written (main_moving.py:143-145)."""
+    cfg = gpkg.wing_case(64, 32, 6, 10.0, re=30.0)
+    sim = gpkg.Simulation(cfg)
+    sim.run(24, graph=True)
+    sim.solver.synchronize()                       # healthy so far: no report
+    f = sim.solver.read_populations()
+    good = f.copy()
+    f[40, 20, 3, 7] = np.nan
+    sim.solver.write_populations(f)
+    before = sim.ibm.step_count()
+    with pytest.raises(gpkg.DivergedError) as ei:
+        sim.run(400, graph=True)
+    assert "stopped after" in str(ei.value)
+    ran = sim.ibm.step_count() - before
+    assert 8 <= ran <= 1 + 6 * 8, ran
+    with pytest.raises(gpkg.DivergedError):
+        sim.solver.synchronize()
+    sim.solver.write_populations(good)             # a new state clears the record
+    sim.run(16, graph=True)
+    sim.solver.synchronize()
+    sim.close()
+
+
+def test_density_floor_of_the_monitor(gpkg):
+    """A density of 0.2 at one cell is caught by the default floor (0.3, as
+    main_moving.py:143) in direct steps too; with a negative floor only non-finite values
+    are."""
+    s = gpkg.Solver(20, 8, 4, 1.5)
+    f = s.read_populations()
+    f[5, 3, 2, :] *= 0.2
+    s.write_populations(f)
+    s.step()
+    with pytest.raises(gpkg.DivergedError):
+        s.synchronize()
+    s.set_rho_floor(-1.0)
+    s.write_populations(f)
+    s.step()
+    s.synchronize()
     s.close()
 
 

@@ -1,0 +1,133 @@
+"""The drop-in modules on the GPU, driven by the reference's own drivers, and the
+reference's configuration variants stepped on the GPU.
+
+tests/test_dropin.py runs main_moving.py and main_highRe.py unmodified through the drop-in
+modules (``compat/``) on the CPU and pins the calls they make (the committed trace in
+tests/golden/dropin_<driver>.npz): per step ``ibm.compute_force(lbm.ux, lbm.uy, xc, yc,
+theta, vx, vy, omega)`` with the arguments of ``_motion_state(step)``, then
+``lbm.step(fx, fy, fz)``, and on every vis step ``lbm.rho/ux/uy/uz.to_numpy()``
+(main_moving.py:116-128). Here the same calls go through the same drop-in modules backed by
+the CUDA library, and the fields they return are compared with the frames the reference's
+own solver wrote (the fixture's frames). The driver's ``ti.init`` (main_moving.py:28-37)
+goes through the drop-in ``taichi``: the GPU arch initialises, the CPU fallback raises.
+"""
+
+import importlib
+import os
+import sys
+import types
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+COMPAT = os.path.join(ROOT, "clbm_ibm-moving-airfoil_gb300", "compat")
+FIELDS = ("rho", "ux", "uy", "uz")
+
+
+@pytest.fixture()
+def dropin_env():
+    saved = dict(sys.modules)
+    path = list(sys.path)
+    for name in ("taichi", "clbm_moving", "airfoil_moving", "config_moving", "config_highRe",
+                 "_clbm_gb300_pkg"):
+        sys.modules.pop(name, None)
+    sys.path.insert(0, COMPAT)
+    yield
+    for name in list(sys.modules):
+        if name not in saved:
+            del sys.modules[name]
+    sys.modules.update(saved)
+    sys.path[:] = path
+
+
+def _config_module(fix, name):
+    m = types.ModuleType(name)
+    for key in fix.files:
+        if key.startswith("cfg_"):
+            v = fix[key]
+            setattr(m, key[4:], v.item() if v.ndim == 0 else v)
+    return m
+
+
+@pytest.mark.parametrize("driver", ["main_moving", "main_highRe"])
+def test_reference_driver_calls_through_dropin_modules(built_pkg, dropin_env, driver):
+    fix = np.load(os.path.join(GOLDEN, f"dropin_{driver}.npz"))
+    cfg = _config_module(fix, "config_moving")
+    if driver == "main_highRe":
+        sys.modules["config_highRe"] = cfg      # main_highRe.py:26-27
+    sys.modules["config_moving"] = cfg
+    ti = importlib.import_module("taichi")
+    assert ti.__file__.startswith(COMPAT)
+    ti.init(arch=ti.gpu, default_fp=ti.f32, default_ip=ti.i32, fast_math=True)
+    with pytest.raises(RuntimeError):
+        ti.init(arch=ti.cpu, default_fp=ti.f32, default_ip=ti.i32, cpu_max_num_threads=8)
+    clbm_moving = importlib.import_module("clbm_moving")
+    airfoil_moving = importlib.import_module("airfoil_moving")
+    assert clbm_moving.__file__.startswith(COMPAT) and airfoil_moving.__file__.startswith(COMPAT)
+
+    lbm = clbm_moving.CLBMSolver()
+    ibm = airfoil_moving.DroneMovingIBM()
+    frames, cur = [], {}
+    fx = fy = fz = None
+    for kind, args, field in zip(fix["trace_kind"], fix["trace_args"], fix["trace_field"]):
+        if kind == 0:
+            fx, fy, fz = ibm.compute_force(lbm.ux, lbm.uy, *[float(a) for a in args])
+        elif kind == 1:
+            lbm.step(fx, fy, fz)
+        else:
+            name = FIELDS[int(field)]
+            a = getattr(lbm, name).to_numpy()
+            assert a.shape == (int(cfg.Nx), int(cfg.Ny), int(cfg.Nz)) and a.dtype == np.float32
+            cur[name] = a
+            if len(cur) == 4:
+                frames.append(cur)
+                cur = {}
+    assert len(frames) == int(fix["n_frames"])
+    for k, fr in enumerate(frames, start=1):
+        want = {n: fix[f"frame{k}_{n}"] for n in FIELDS}
+        e_rho = rel_l2(fr["rho"], want["rho"])
+        e_u = rel_l2(np.stack([fr["ux"], fr["uy"], fr["uz"]]),
+                     np.stack([want["ux"], want["uy"], want["uz"]]))
+        assert e_rho < 1e-5 and e_u < 1e-5, (driver, k, e_rho, e_u)
+        assert rel_l2(fr["ux"], want["ux"]) < 1e-5 and rel_l2(fr["uy"], want["uy"]) < 1e-5
+    # the lift/drag support of the drop-in IBM reads the last step's force sums
+    Fx, Fy = ibm.body_force()
+    assert np.isfinite(Fx) and np.isfinite(Fy) and (Fx != 0.0 or Fy != 0.0)
+    lbm._solver.close()
+
+
+def _variant_against_oracle(pkg, oracle_mod, cfg, steps):
+    sim = pkg.Simulation(cfg)
+    ref = oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                            cfg.X0, cfg.Y0, cfg.Z0)
+    for step in range(1, steps + 1):
+        sim.step_host_motion(step)
+        ref.compute_force(*cfg.motion_state(step))
+        ref.lbm_step()
+    got = sim.solver.read_macro()
+    mk = sim.ibm.read_markers()
+    sim.close()
+    rho, ux, uy, uz = ref.macro()
+    want_mk = ref.markers()
+    ref.close()
+    e = {"rho": rel_l2(got["rho"], rho), "ux": rel_l2(got["ux"], ux), "uy": rel_l2(got["uy"], uy),
+         "FXk": rel_l2(mk["FXk"], want_mk["FXk"]), "FYk": rel_l2(mk["FYk"], want_mk["FYk"])}
+    print(cfg.name, {k: f"{v:.2e}" for k, v in e.items()})
+    assert e["rho"] < 1e-5 and e["ux"] < 1e-5 and e["uy"] < 1e-5
+    assert e["FXk"] < 1e-4 and e["FYk"] < 1e-4
+
+
+def test_fish_variant_against_oracle(built_pkg, oracle_mod):
+    """The swimmer of fish/config_fish.py (800x250x25, 4:1 ellipse, Re 300, k = 0.8)
+    stepped on the GPU through the same API, against the oracle."""
+    _variant_against_oracle(built_pkg, oracle_mod, built_pkg.fish_case(), 20)
+
+
+def test_highre_airplane_variant_against_oracle(built_pkg, oracle_mod):
+    """The high-Re airplane of config_highRe.py (800x260x220, chord 120, Re 1000, 8 degree
+    inflow, the reference's own marker set) stepped on the GPU, against the oracle."""
+    _variant_against_oracle(built_pkg, oracle_mod, built_pkg.highre_airplane_case(), 3)

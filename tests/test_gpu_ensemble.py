@@ -80,3 +80,48 @@ def test_ensemble_tiled_spreading_is_bit_identical(built_pkg, monkeypatch):
     for a, b in zip(out["direct"], out["tiled"]):
         np.testing.assert_array_equal(a[0], b[0])
         np.testing.assert_array_equal(a[1], b[1])
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_ensemble_at_its_real_sizes(built_pkg, oracle_mod, storage):
+    """The batched ensemble as the bench runs it: 64 members drawn with seeds 0..63 from the
+    lattices 150x60x12, 200x80x16 and 300x100x24 (chord Nx / 6.25, Re, heave, pitch, phase
+    and k drawn per seed), with the schedule the autotuner picks for them, 50 steps. The
+    first member of each lattice and the last member give the bits of the same case stepped
+    alone; in float32 one member (300x100x24) matches the oracle within the plain-path
+    bounds."""
+    pkg = built_pkg
+    cases = [pkg.config.ensemble_case(seed, storage=storage) for seed in range(64)]
+    steps = 50
+    ens = pkg.Ensemble(cases)
+    ens.run(steps)
+    ens.synchronize()
+    t = ens.tuning()
+    assert t["blocks"] > 0 and t["tiles"] > 0 and t["bulk_us"] > 0
+    firsts = {}
+    for i, c in enumerate(cases):
+        firsts.setdefault((c.nx, c.ny, c.nz), i)
+    assert len(firsts) == 3
+    picked = sorted(set(firsts.values()) | {63})
+    for i in picked:
+        member, cfg = ens.sims[i], cases[i]
+        alone = pkg.Simulation(cfg)
+        alone.run(steps)
+        np.testing.assert_array_equal(member.solver.read_populations(),
+                                      alone.solver.read_populations(), err_msg=f"member {i}")
+        np.testing.assert_allclose(member.ibm.force_history(steps), alone.ibm.force_history(steps),
+                                   rtol=1e-12, atol=1e-14)
+        alone.close()
+    if storage == "f32":
+        i = firsts[(300, 100, 24)]
+        cfg = cases[i]
+        ref = oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                                cfg.X0, cfg.Y0, cfg.Z0)
+        ref_hist = ref.run(0, steps, cfg.motion())
+        rho, ux, uy, uz = ref.macro()
+        ref.close()
+        got = ens.sims[i].solver.read_macro()
+        assert rel_l2(got["rho"], rho) <= 1e-5
+        assert rel_l2(np.stack([got["ux"], got["uy"], got["uz"]]), np.stack([ux, uy, uz])) <= 1e-5
+        assert rel_l2(ens.sims[i].ibm.force_history(steps), ref_hist) <= 1e-4
+    ens.close()

@@ -177,7 +177,10 @@ def test_body_across_periodic_y_seam(gpkg, oracle_mod, monkeypatch, variant):
     """The wing placed at y0 = 2, so its lower surface lies below y = 0 and its stencils
     and force box wrap across the periodic y boundary (the band's y range starts at
     Ny - 3 and continues at 0): 80 steps against the oracle, with the bulk kernel variants
-    that skip the box cells."""
+    that skip the box cells. rho and u (the velocity field) within 1e-5 of the float32
+    oracle; per component, against the FP64 oracle, within twice the float32 oracle's own
+    error (uy, the small cross-flow component, differs between the two float32
+    computations by about 1e-5 relative L2, the float32 oracle alone from FP64 by 8.9e-6)."""
     monkeypatch.setenv("CLBM_KERNEL", variant)
     from dataclasses import replace
     cfg = replace(gpkg.small_case(), y0=2.0)
@@ -188,8 +191,18 @@ def test_body_across_periodic_y_seam(gpkg, oracle_mod, monkeypatch, variant):
     ref_hist = ref.run(0, nsteps, cfg.motion())
     got = sim.solver.read_macro()
     want = dict(zip(("rho", "ux", "uy", "uz"), ref.macro()))
-    for k in ("rho", "ux", "uy"):
-        assert rel_l2(got[k], want[k]) < TOL_FIELD, k
+    ref64 = oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                              cfg.X0, cfg.Y0, cfg.Z0, real="f64")
+    ref64.run(0, nsteps, cfg.motion(), record=False)
+    exact = dict(zip(("rho", "ux", "uy", "uz"), ref64.macro()))
+    ref64.close()
+    assert rel_l2(got["rho"], want["rho"]) < TOL_FIELD
+    u = lambda d: np.stack([d["ux"], d["uy"], d["uz"]])  # noqa: E731
+    assert rel_l2(u(got), u(want)) < TOL_FIELD
+    for k in ("ux", "uy"):
+        e_gpu, e_ref = rel_l2(got[k], exact[k]), rel_l2(want[k], exact[k])
+        print(f"{variant} {k}: GPU float32 vs FP64 {e_gpu:.2e}, oracle float32 vs FP64 {e_ref:.2e}")
+        assert e_gpu <= 2.0 * e_ref, k
     assert rel_l2(sim.ibm.force_history(nsteps), ref_hist) < TOL_FORCE
     mk = sim.ibm.read_markers()
     assert mk["Y"].min() < 0.0  # stencils below y = 0 wrap to the top rows
