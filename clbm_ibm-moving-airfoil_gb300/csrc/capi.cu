@@ -991,7 +991,6 @@ struct clbm_ensemble {
         int n = 0;
         long long ntiles = 0;
         int threads = 0;
-        int rows_per_tile = 1;   // 16-bit forms: rows packed into one block
     };
     std::vector<Group> groups;
     bool rows = false;
@@ -1024,56 +1023,36 @@ EnsDesc member_desc(const clbm_ensemble* e, int i) {
     return D;
 }
 
-// Row mode of the bulk pass. Float32: members grouped by the threads a whole row needs (a
-// multiple of 32, one cell per thread, rows up to 512 cells), one row per block. 16-bit
-// forms: members grouped by row width, R rows packed into a block of two cells per thread.
-// Each group's descriptors list its members with their tiles. No groups when a row is
-// wider.
+// Members grouped by the threads a whole row needs (a multiple of 32; two cells per thread
+// in the 16-bit forms, one in float32; rows up to 512 cells); each group's descriptors list
+// its members with tiles = rows. No groups when a row is wider.
 int ens_groups(clbm_ensemble* e) {
     const bool f32 = e->storage == CLBM_STORE_F32;   // one cell per thread, rows up to 512
-    // group key: float32 the block width (one row per block); 16-bit forms the row width
-    std::vector<int> key(e->n);
+    std::vector<int> th(e->n);
     for (int i = 0; i < e->n; ++i) {
         const int nx = e->s[i]->g.nx;
-        if (nx > (f32 ? 512 : 1024)) return CLBM_OK;
-        key[i] = f32 ? (nx + 31) / 32 * 32 : nx;
+        if (nx > 512) return CLBM_OK;
+        th[i] = f32 ? (nx + 31) / 32 * 32 : (nx + 63) / 64 * 32;
     }
-    std::vector<int> keys(key);
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-    for (int k : keys) {
-        // 16-bit forms: R rows of Nx / 2 pairs per block, the R (block of at most 512
-        // threads) that leaves the fewest idle lanes, the smallest R among equals
-        int threads = k, R = 1;
-        if (!f32) {
-            const int npairs = (k + 1) / 2;
-            double best = 2.0;
-            for (int r = 1; r * npairs <= 512; ++r) {
-                const int th = (r * npairs + 31) / 32 * 32;
-                const double idle = 1.0 - (double)(r * npairs) / th;
-                if (idle < best - 1e-9) {
-                    best = idle;
-                    threads = th;
-                    R = r;
-                }
-            }
-        }
+    std::vector<int> widths(th);
+    std::sort(widths.begin(), widths.end());
+    widths.erase(std::unique(widths.begin(), widths.end()), widths.end());
+    for (int w : widths) {
         std::vector<EnsDesc> h;
         std::vector<long long> t0;
         long long tiles = 0;
         for (int i = 0; i < e->n; ++i) {
-            if (key[i] != k) continue;
+            if (th[i] != w) continue;
             EnsDesc D = member_desc(e, i);
             D.tile0 = tiles;
             t0.push_back(tiles);
-            tiles += ((long long)D.g.ny * D.g.nz + R - 1) / R;
+            tiles += (long long)D.g.ny * D.g.nz;
             h.push_back(D);
         }
         clbm_ensemble::Group gr;
         gr.n = (int)h.size();
         gr.ntiles = tiles;
-        gr.threads = threads;
-        gr.rows_per_tile = R;
+        gr.threads = w;
         e->groups.push_back(gr);
         clbm_ensemble::Group& G = e->groups.back();
         CK(cudaMalloc(&G.d, sizeof(EnsDesc) * G.n));
@@ -1087,7 +1066,7 @@ int ens_groups(clbm_ensemble* e) {
 
 void ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
     for (const auto& G : e->groups)
-        launch_ens_bulk_rows(e->storage, pull, G.threads, G.rows_per_tile, G.d, G.tile0, G.n, G.ntiles, e->cur,
+        launch_ens_bulk_rows(e->storage, pull, G.threads, G.d, G.tile0, G.n, G.ntiles, e->cur,
                              (int)std::min<long long>(G.ntiles, 1LL << 30), st);
 }
 

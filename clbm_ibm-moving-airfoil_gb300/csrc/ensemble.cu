@@ -189,20 +189,15 @@ kb_bulk(const EnsDesc* __restrict__ d, const long long* __restrict__ tile0, int 
     }
 }
 
-// 16-bit forms, whole rows per block: tile t of a group covers rows
-// (t - tile0[i]) * R ... + R - 1 of instance i (y fastest), packed back to back over the
-// block's threads with two cells per thread: thread p takes pair p % (Nx / 2) of the tile's
-// row p / (Nx / 2). Instances are grouped by row width, one launch per group, and R is
-// chosen per width so that few lanes idle (a 150-cell row alone fills 75 of 96 lanes; two
-// rows fill 150 of 160). Lanes of one warp may hold different rows: pair_body's x shifts
-// take a neighbour lane's element, and where that lane holds another row (at the first pair
-// of a row, or the last) the value is one the boundary conditions replace (the inlet
-// unknowns rebuilt by Zou-He, the outlet column copied from Nx - 2), so the packing gives
-// the same bits as one row per block.
+// 16-bit forms, one row per block: tile t of a group is row (t - tile0[i]) of instance i
+// (y fastest), the block's warps cover the row with two cells per thread (blockDim.x >=
+// Nx / 2, the smallest multiple of 32). Instances are grouped by that width, one launch per
+// group, so a 150-, 200- or 300-cell row costs 3, 4 or 5 warps and the row (y, z) stays
+// uniform across the block.
 template <int S, bool PULL>
-__global__ void __launch_bounds__(512, 2) kb_bulk_row(const EnsDesc* __restrict__ d,
+__global__ void __launch_bounds__(256, 4) kb_bulk_row(const EnsDesc* __restrict__ d,
                                                     const long long* __restrict__ tile0, int n,
-                                                    long long ntiles, int parity, int rows_per_tile) {
+                                                    long long ntiles, int parity) {
     using T = typename Pop<S>::T;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int lo = 0, hi = n - 1;
@@ -214,13 +209,7 @@ __global__ void __launch_bounds__(512, 2) kb_bulk_row(const EnsDesc* __restrict_
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
         const Coef c = D.c;
-        const int rows = g.ny * g.nz;
-        const int npairs = (g.nx + 1) >> 1;
-        const int rl = (int)threadIdx.x / npairs;
-        const int r_raw = (int)(t - D.tile0) * rows_per_tile + rl;  // row z * ny + y
-        const bool live = rl < rows_per_tile && r_raw < rows;
-        const int r = live ? r_raw : rows - 1;            // idle lanes address a valid row
-        const int x0 = live ? 2 * ((int)threadIdx.x - rl * npairs) : g.pitch;
+        const int r = (int)(t - D.tile0);   // row z * ny + y
         const int y = r % g.ny, z = r / g.ny;
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
@@ -228,9 +217,9 @@ __global__ void __launch_bounds__(512, 2) kb_bulk_row(const EnsDesc* __restrict_
         if (D.has_ibm) {
             fa.dev = D.a.dev;
             fa.slot = (int)(D.a.dev->cur & 1);
-            pair_body<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, x0, y, z);
+            pair_body<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
         } else {
-            pair_body<S, PULL, kForceNone>(fin, fout, g, c, fa, x0, y, z);
+            pair_body<S, PULL, kForceNone>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
         }
     }
 }
@@ -267,19 +256,17 @@ __global__ void __launch_bounds__(512) kb_bulk_row_f32(const EnsDesc* __restrict
     }
 }
 
-void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile, const EnsDesc* d,
-                          const long long* tile0, int n, long long ntiles, int parity, int grid,
-                          cudaStream_t st) {
-    const int R = rows_per_tile;
+void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
+                          int n, long long ntiles, int parity, int grid, cudaStream_t st) {
     if (storage == CLBM_STORE_F32) {
         if (pull) kb_bulk_row_f32<true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
         else kb_bulk_row_f32<false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
     } else if (storage == CLBM_STORE_F16S) {
-        if (pull) kb_bulk_row<CLBM_STORE_F16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
-        else kb_bulk_row<CLBM_STORE_F16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
+        if (pull) kb_bulk_row<CLBM_STORE_F16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        else kb_bulk_row<CLBM_STORE_F16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
     } else if (storage == CLBM_STORE_BF16S) {
-        if (pull) kb_bulk_row<CLBM_STORE_BF16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
-        else kb_bulk_row<CLBM_STORE_BF16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
+        if (pull) kb_bulk_row<CLBM_STORE_BF16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        else kb_bulk_row<CLBM_STORE_BF16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
     }
 }
 
