@@ -74,28 +74,27 @@ int join_bulk(clbm_solver* s) {
 
 // Box pass of an IBM step on stream st: with the force sums of the IBM call when they are
 // still pending (no separate force-sum kernel then).
-void box_pass(clbm_solver* s, const ForceArgs& fa, const clbm_ibm* ibm, long long box_cells,
-              cudaStream_t st) {
-    if (ibm && ibm->sums_pending) {
+void box_pass(clbm_solver* s, const ForceArgs& fa, const clbm_ibm* ibm, cudaStream_t st) {
+    if (ibm->sums_pending) {
         launch_stream_collide_box_sums(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur],
-                                       s->g, s->c, fa, ibm->a, box_cells, st);
+                                       s->g, s->c, fa, ibm->a, st);
         ibm->sums_pending = false;
     } else {
         launch_stream_collide_box(s->cfg.storage, !s->local, s->f[s->cur], s->f[1 - s->cur], s->g,
-                                  s->c, fa, box_cells, st);
+                                  s->c, fa, ibm->a.max_bx, ibm->a.max_by, ibm->a.max_bz, st);
     }
 }
 
 // One fused stream-collide launch on stream `st`, bracketed by timing events if profiling.
 int sc_timed(clbm_solver* s, int fmode, const ForceArgs& fa, cudaStream_t st, bool box,
-             long long box_cells, const clbm_ibm* ibm = nullptr) {
+             const clbm_ibm* ibm = nullptr) {
     if (s->prof) {
         if (int rc = record_event(s, st)) return rc;
         s->ev_tag.resize(s->ev_used / 2 + 1);
         s->ev_tag[s->ev_used / 2] = box ? 1 : 0;
     }
     if (box) {
-        box_pass(s, fa, ibm, box_cells, st);
+        box_pass(s, fa, ibm, st);
     } else if (s->closure && (fmode == kForceNone || fmode == kForceSkipBand)) {
         ClosureArgs ca{};
         ca.params = s->cl_params;
@@ -128,7 +127,7 @@ int flush_sums(const clbm_ibm* ibm) {
 int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ibm) {
     if (int rc = join_bulk(s)) return rc;
     if (fmode != kForceBand) {
-        if (int rc = sc_timed(s, fmode, fa, s->st, false, 0)) return rc;
+        if (int rc = sc_timed(s, fmode, fa, s->st, false)) return rc;
     } else {
         // IBM step in two passes. The bulk pass (cells outside the force box) needs only the
         // box, so it forks off after the marker kernel of the last compute_force and runs on
@@ -139,9 +138,8 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
         // other (the bulk pass then runs alone: its isolated time for measurements)
         static const int serial = knob("CLBM_SERIAL", 0);
         if (serial) {
-            if (int rc = sc_timed(s, kForceSkipBand, fa, s->st, false, 0)) return rc;
-            const long long bc = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
-            if (int rc = sc_timed(s, kForceBand, fa, s->st, true, bc, ibm)) return rc;
+            if (int rc = sc_timed(s, kForceSkipBand, fa, s->st, false)) return rc;
+            if (int rc = sc_timed(s, kForceBand, fa, s->st, true, ibm)) return rc;
             s->cur = 1 - s->cur;
             s->local = false;
             s->macro_full = false;
@@ -154,10 +152,9 @@ int step_impl(clbm_solver* s, int fmode, const ForceArgs& fa, const clbm_ibm* ib
             CK(cudaEventRecord(s->ev_fork, s->st));
             CK(cudaStreamWaitEvent(s->st2, s->ev_fork, 0));
         }
-        if (int rc = sc_timed(s, kForceSkipBand, fa, s->st2, false, 0)) return rc;
+        if (int rc = sc_timed(s, kForceSkipBand, fa, s->st2, false)) return rc;
         CK(cudaEventRecord(s->ev_bulk, s->st2));
-        const long long box_cells = (long long)ibm->a.max_bx * ibm->a.max_by * ibm->a.max_bz;
-        if (int rc = sc_timed(s, kForceBand, fa, s->st, true, box_cells, ibm)) return rc;
+        if (int rc = sc_timed(s, kForceBand, fa, s->st, true, ibm)) return rc;
         s->bulk_pending = true;  // joined by the next call (after the next marker kernel)
     }
     s->cur = 1 - s->cur;
@@ -1227,9 +1224,10 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         e->m.push_back(motions[i]);
         clbm_ibm* b = e->ibm.back();
         if (b) {
-            e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + 255) / 256);
+            e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + kMarkerBlock - 1) / kMarkerBlock);
             const long long warps = ((long long)b->a.n + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp;
-            e->max_spread_blocks = std::max(e->max_spread_blocks, (int)((warps * 32 + 255) / 256));
+            e->max_spread_blocks = std::max(e->max_spread_blocks,
+                                            (int)((warps * 32 + kSpreadBlock - 1) / kSpreadBlock));
         }
     }
     {

@@ -245,7 +245,8 @@ inline size_t store_bytes(int storage) { return storage == CLBM_STORE_F32 ? 4 : 
 // Force source of the fused step.
 // kForceSkipBand: bulk pass of an IBM step that leaves the cells of the force box to
 // launch_stream_collide_box, so the bulk can run while the IBM kernels compute the forces.
-enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2, kForceSkipBand = 3 };
+// kForceOnlyBand: the complement, the box pass: only the cells of the force box, forced.
+enum ForceMode { kForceNone = 0, kForceBand = 1, kForceDense = 2, kForceSkipBand = 3, kForceOnlyBand = 4 };
 
 // IBM force fields are accumulated in 64-bit fixed point with kForceScale units per unit
 // force: integer atomics are associative, so spreading is deterministic, and a float32
@@ -288,17 +289,17 @@ void launch_vorticity_slice(const float* ux, const float* uy, const Grid& g, int
 
 // Record the message clbm_last_error() returns on this thread.
 void set_last_error(const char* msg);
-// Forced stream-collide of the cells of the current IBM force box; max_cells bounds the
-// box size (grid sizing only).
+// Forced stream-collide of the cells of the current IBM force box, by rows of the box;
+// max_bx, max_by, max_bz bound the box size (grid sizing only).
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
-                               const Grid& g, const Coef& c, const ForceArgs& fa,
-                               long long max_cells, cudaStream_t st);
+                               const Grid& g, const Coef& c, const ForceArgs& fa, int max_bx,
+                               int max_by, int max_bz, cudaStream_t st);
 struct IbmArrays;
 // The same box pass, also computing the force sums of the call whose box it is into the
 // history ring and advancing the device call counter (ibm_box_sums_tail).
 void launch_stream_collide_box_sums(int storage, bool pull, const void* fin, void* fout,
                                     const Grid& g, const Coef& c, const ForceArgs& fa,
-                                    const IbmArrays& a, long long max_cells, cudaStream_t st);
+                                    const IbmArrays& a, cudaStream_t st);
 // Macro (rho, u without force) of the current state for every cell of the grid; optional
 // statistics into stats[0..3] (ordered-int min rho, max rho, max |u|^2, nonfinite count).
 void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
@@ -328,7 +329,8 @@ struct IbmArrays {
     float *ux, *uy;       // padded full grid (macro of the solver)
     IbmDev* dev;
     double* hist;
-    double* part;         // per-block partial sums of the force-sum kernel [kFinishBlocks][4]
+    double* part;         // per-block partials: force-sum kernel [kFinishBlocks][4]; box pass
+                          // marker sums [kFinishBlocks][2]
     int hist_cap;
     int max_bx, max_by, max_bz;   // upper bound of the band box dimensions
 };
@@ -342,6 +344,18 @@ void launch_ibm_markers(const IbmArrays& a, const Grid& g, bool device_motion,
 // Zero the previous call's force band and compute the macro fields on this call's band.
 constexpr int kFinishBlocks = 64;    // force-sum blocks: few, so they leave the SMs to the bulk pass
 constexpr int kSpreadMarkersPerWarp = 2;   // markers interpolated and spread by one warp
+// The IBM kernels run beside the bulk stream-collide pass, on a stream of higher priority.
+// The block scheduler starts a waiting block only on an SM where it fits, and an SM full of
+// bulk blocks frees room one bulk block at a time (64 threads x 64 registers in the 16-bit
+// forms, 128 x 48 in float32): a larger block waits while the smaller low-priority blocks
+// keep taking the freed room, in practice until the bulk grid runs out. The marker,
+// band-prepare, spreading and box-pass kernels therefore use blocks of 64 threads (the
+// 16-bit box pass with at most 64 registers).
+constexpr int kMarkerBlock = 64;
+constexpr int kBoxBlock = 64;      // band-prepare and box pass of the single lattice
+constexpr int kSpreadBlock = 64;
+constexpr int kTiledBlock = 256;   // shared-memory tiled spreading: 8 warps per tile
+constexpr int kFinishBlock = 256;
 void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
                          IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread(const EnsDesc* 
     ibm_interp_spread_body<kSpreadMarkersPerWarp>(D.a, D.g, m0, threadIdx.x & 31);
 }
 
-__global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread_tiled(const EnsDesc* __restrict__ d) {
+__global__ void __launch_bounds__(kTiledBlock) kb_interp_spread_tiled(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
     if (!D.has_ibm || (int)blockIdx.x * kTileMarkers >= D.a.n) return;  // whole block
     ibm_interp_spread_tiled_body(D.a, D.g, blockIdx.x);
@@ -285,9 +285,10 @@ void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     if (blocks < 1) return;
     if (spread_tiled()) {
-        // a block of the direct form covers 8 * kSpreadMarkersPerWarp markers; a tiled block 32
-        kb_interp_spread_tiled<<<dim3((blocks * 8 * kSpreadMarkersPerWarp + kTileMarkers - 1) / kTileMarkers, n),
-                                 kSpreadBlock, 0, st>>>(d);
+        // a block of the direct form covers (kSpreadBlock / 32) * kSpreadMarkersPerWarp
+        // markers; a tiled block kTileMarkers
+        const int per = (kSpreadBlock / 32) * kSpreadMarkersPerWarp;
+        kb_interp_spread_tiled<<<dim3((blocks * per + kTileMarkers - 1) / kTileMarkers, n), kTiledBlock, 0, st>>>(d);
         return;
     }
     kb_interp_spread<<<dim3(blocks, n), kSpreadBlock, 0, st>>>(d);

@@ -8,9 +8,6 @@
 
 namespace clbm {
 
-constexpr int kMarkerBlock = 256;
-constexpr int kSpreadBlock = 256;
-constexpr int kFinishBlock = 256;
 
 // Marker kinematics (airfoil_moving.py:100-127) of markers [bx * 256, bx * 256 + 256) and
 // the box that bounds their 4x4x4 Peskin stencils (block min, one atomicMin per entry).
@@ -216,7 +213,7 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
 // y or z) spreads with direct global atomics.
 constexpr int kTileMarkers = 32;
 constexpr int kTileCells = 2048;   // two int64 per cell: 32 KB of shared memory
-constexpr int kTileMarkersPerWarp = kTileMarkers / (kSpreadBlock / 32);
+constexpr int kTileMarkersPerWarp = kTileMarkers / (kTiledBlock / 32);
 
 __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a, const Grid& g, int chunk) {
     __shared__ long long tfx[kTileCells], tfy[kTileCells];
@@ -264,7 +261,7 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
         return;
     }
     const int vol = li * lj * lk;
-    for (int t = threadIdx.x; t < vol; t += kSpreadBlock) {
+    for (int t = threadIdx.x; t < vol; t += kTiledBlock) {
         tfx[t] = 0;
         tfy[t] = 0;
     }
@@ -282,7 +279,7 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
         }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < vol; t += kSpreadBlock) {
+    for (int t = threadIdx.x; t < vol; t += kTiledBlock) {
         const long long vx = tfx[t], vy = tfy[t];
         if (vx == 0 && vy == 0) continue;
         const int x = i0 + t % li;
@@ -378,25 +375,49 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
 
 // Force sums folded into the box pass (single lattice): each block of the box pass brings
 // the integer sums kx, ky of its cells' clipped Eulerian force (units of 2^-40); they are
-// added exactly into dev->ksum; the last block to finish converts them, sums the marker
-// forces in a fixed order (thread-strided, warp butterfly, warps in order), writes the
-// history entry of the call whose box this was, and advances the device call counter --
-// the work of ibm_finish_body without its own launch. The Eulerian part is the same exact
-// integer sum; the marker part is the same set of doubles added in another fixed order.
+// added exactly into dev->ksum. The marker forces are summed in double by the first
+// P = min(blocks, kFinishBlocks) blocks, block b over its own contiguous share of the
+// markers (thread-strided, warp butterfly, warps in order), into a.part; the last block to
+// finish adds the P partials in block order, converts the integer sums, writes the history
+// entry of the call whose box this was and advances the device call counter -- the work of
+// ibm_finish_body without its own launch. The Eulerian part is the same exact integer sum;
+// the marker part is the same set of doubles added in another fixed order. (One block
+// summing all markers would wait on one load round trip per marker and thread: 197 of them
+// at 12,600 markers and 64 threads.)
 __device__ __forceinline__ void ibm_box_sums_tail(const IbmArrays& a, long long kx, long long ky) {
     __shared__ long long kred[32][2];
     __shared__ double dred[32][2];
     __shared__ bool last;
     IbmDev* dev = a.dev;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int P = min((int)gridDim.x, kFinishBlocks);
+    if ((int)blockIdx.x < P) {
+        const int chunk = (a.n + P - 1) / P;
+        const int m0 = (int)blockIdx.x * chunk, m1 = min(a.n, m0 + chunk);
+        double mx = 0.0, my = 0.0;
+#pragma unroll 4
+        for (int m = m0 + (int)threadIdx.x; m < m1; m += blockDim.x) {
+            mx += (double)a.FXk[m];
+            my += (double)a.FYk[m];
+        }
+        mx = warp_sum(mx);
+        my = warp_sum(my);
+        if (lane == 0) { dred[warp][0] = mx; dred[warp][1] = my; }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         kx += __shfl_xor_sync(0xffffffffu, kx, o);
         ky += __shfl_xor_sync(0xffffffffu, ky, o);
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     if (lane == 0) { kred[warp][0] = kx; kred[warp][1] = ky; }
     __syncthreads();
     if (threadIdx.x == 0) {
+        if ((int)blockIdx.x < P) {
+            double tx = 0.0, ty = 0.0;
+            for (int w = 0; w < nw; ++w) { tx += dred[w][0]; ty += dred[w][1]; }
+            a.part[2 * blockIdx.x] = tx;
+            a.part[2 * blockIdx.x + 1] = ty;
+        }
         long long sx = 0, sy = 0;
         for (int w = 0; w < nw; ++w) { sx += kred[w][0]; sy += kred[w][1]; }
         if (sx) atomicAdd((unsigned long long*)&dev->ksum[0], (unsigned long long)sx);
@@ -408,11 +429,13 @@ __device__ __forceinline__ void ibm_box_sums_tail(const IbmArrays& a, long long 
     if (!last) return;
     __threadfence();
     double mx = 0.0, my = 0.0;
-    for (int m = threadIdx.x; m < a.n; m += blockDim.x) {
-        mx += (double)a.FXk[m];
-        my += (double)a.FYk[m];
+    for (int b = threadIdx.x; b < P; b += blockDim.x) {
+        mx += __ldcg(a.part + 2 * b);
+        my += __ldcg(a.part + 2 * b + 1);
     }
-    mx = warp_sum(mx); my = warp_sum(my);
+    mx = warp_sum(mx);
+    my = warp_sum(my);
+    __syncthreads();   // dred is reused
     if (lane == 0) { dred[warp][0] = mx; dred[warp][1] = my; }
     __syncthreads();
     if (threadIdx.x == 0) {

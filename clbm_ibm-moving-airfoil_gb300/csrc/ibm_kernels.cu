@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread(IbmArrays a,
     ibm_interp_spread_body<kSpreadMarkersPerWarp>(a, g, m0, threadIdx.x & 31);
 }
 
-__global__ void __launch_bounds__(kSpreadBlock) k_ibm_interp_spread_tiled(IbmArrays a, Grid g) {
+__global__ void __launch_bounds__(kTiledBlock) k_ibm_interp_spread_tiled(IbmArrays a, Grid g) {
     ibm_interp_spread_tiled_body(a, g, blockIdx.x);
 }
 
@@ -64,7 +64,7 @@ bool spread_tiled() {
 void launch_ibm_interp_spread(const IbmArrays& a, const Grid& g, cudaStream_t st) {
     if (spread_tiled()) {
         const int blocks = (a.n + kTileMarkers - 1) / kTileMarkers;
-        if (blocks > 0) k_ibm_interp_spread_tiled<<<blocks, kSpreadBlock, 0, st>>>(a, g);
+        if (blocks > 0) k_ibm_interp_spread_tiled<<<blocks, kTiledBlock, 0, st>>>(a, g);
         return;
     }
     const long long threads = (long long)(a.n + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp * 32;

@@ -691,10 +691,13 @@ template <> struct Pair<CLBM_STORE_BF16S> {
 // (lanes past the lattice edge take part in the shuffles and store nothing).
 // IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
 // P: the loads and stores of the storage form (Pair<S>).
+// kForceOnlyBand (box pass): only the cells inside the force box are collided and stored;
+// with ks, their clipped forces in units of 2^-40 are added to ks[0], ks[1] (exact).
 template <int S, bool PULL, int FMODE, bool IDX32 = false, class P = Pair<S>>
 __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
                                           typename Pair<S>::T* __restrict__ fout, const Grid& g,
-                                          const Coef& c, const ForceArgs& fa, int x0, int y, int z) {
+                                          const Coef& c, const ForceArgs& fa, int x0, int y, int z,
+                                          long long* ks = nullptr) {
     using I = typename std::conditional<IDX32, unsigned, long long>::type;
     const I plane = (I)g.plane;
     constexpr unsigned kFull = 0xffffffffu;
@@ -762,7 +765,7 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
     }
     // cells of the IBM force box: tested after the loads, so the box read does not delay them
     bool in0 = false, in1 = false;
-    if (FMODE == kForceSkipBand || FMODE == kForceBand) {
+    if (FMODE == kForceSkipBand || FMODE == kForceBand || FMODE == kForceOnlyBand) {
         const Band b = load_band(fa.dev, fa.slot);
         // the two cells share their row: the y/z part of the test once, then x per cell
         int oy = y - b.j0; if (oy < 0) oy += g.ny;
@@ -772,13 +775,13 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
             in1 = act1 && (unsigned)(x0 + 1 - b.i0) < (unsigned)b.ilen;
         }
     }
-    const bool use0 = act0 && !(FMODE == kForceSkipBand && in0);
-    const bool use1 = act1 && !(FMODE == kForceSkipBand && in1);
+    const bool use0 = act0 && (FMODE == kForceOnlyBand ? in0 : !(FMODE == kForceSkipBand && in0));
+    const bool use1 = act1 && (FMODE == kForceOnlyBand ? in1 : !(FMODE == kForceSkipBand && in1));
     if (!use0 && !use1) return;
     // body force per cell
     float F0x = 0.f, F0y = 0.f, F0z = 0.f, F1x = 0.f, F1y = 0.f, F1z = 0.f;
     bool frc0 = false, frc1 = false;
-    if (FMODE == kForceBand) {
+    if (FMODE == kForceBand || FMODE == kForceOnlyBand) {
         frc0 = in0;
         frc1 = in1;
         if (in0) {
@@ -788,6 +791,10 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
         if (in1) {
             F1x = fminf(fmaxf(qforce(fa.qx[row + x0 + 1]), -0.05f), 0.05f);
             F1y = fminf(fmaxf(qforce(fa.qy[row + x0 + 1]), -0.05f), 0.05f);
+        }
+        if (FMODE == kForceOnlyBand && ks) {
+            ks[0] += (long long)(F0x * kForceScale) + (long long)(F1x * kForceScale);
+            ks[1] += (long long)(F0y * kForceScale) + (long long)(F1y * kForceScale);
         }
     } else if (FMODE == kForceDense) {
         frc0 = act0;
@@ -818,11 +825,14 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
 
 
 // One cell of the full-grid pass: gather, force (per FMODE), collide, store.
+// kForceOnlyBand (box pass): only a cell inside the force box is collided and stored; with
+// ks, its clipped force in units of 2^-40 is added to ks[0], ks[1] (exact).
 template <int S, bool PULL, int FMODE>
 __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __restrict__ fin,
                                                     typename Pop<S>::T* __restrict__ fout,
                                                     const Grid& g, const Coef& c,
-                                                    const ForceArgs& fa, int x, int y, int z) {
+                                                    const ForceArgs& fa, int x, int y, int z,
+                                                    long long* ks = nullptr) {
     // shifted storage: the collision works on the deviations (no per-population shift)
     constexpr bool DEV = Pop<S>::kShifted;
     float f[19];
@@ -846,8 +856,13 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
             // fz is always zero there.
             const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
             const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+            if (FMODE == kForceOnlyBand && ks) {
+                ks[0] += (long long)(Fx * kForceScale);
+                ks[1] += (long long)(Fy * kForceScale);
+            }
             collide<true, DEV>(f, c, Fx, Fy, 0.0f);
         } else {
+            if (FMODE == kForceOnlyBand) return;
             collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
         }
     }
@@ -879,8 +894,8 @@ __device__ __forceinline__ void box_pass_cell(const typename Pop<S>::T* __restri
     store_raw<S>(fout, g, cell, f);
 }
 
-// Forced stream-collide of the cells of the IBM force box; block bx of nbx (256 threads)
-// takes cells bx * 256 + threadIdx.x, stepping by nbx * 256.
+// Forced stream-collide of the cells of the IBM force box; block bx of nbx (blockDim.x threads)
+// takes cells bx * blockDim.x + threadIdx.x, stepping by nbx * blockDim.x.
 template <int S, bool PULL>
 __device__ __forceinline__ void box_pass_body(const typename Pop<S>::T* __restrict__ fin,
                                               typename Pop<S>::T* __restrict__ fout,

@@ -35,26 +35,51 @@ __global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T
     stream_collide_cell<S, PULL, FMODE>(fin, fout, g, c, fa, x, blockIdx.y, blockIdx.z);
 }
 
-// Forced pass over the cells of the IBM force box (the complement of the bulk pass).
-template <int S, bool PULL>
-__global__ void __launch_bounds__(256) k_stream_collide_box(const typename Pop<S>::T* __restrict__ fin,
-                                                            typename Pop<S>::T* __restrict__ fout,
-                                                            Grid g, Coef c, ForceArgs fa) {
-    box_pass_body<S, PULL>(fin, fout, g, c, fa, blockIdx.x, gridDim.x);
-}
-
-// The box pass of a step that also completes its IBM call: force sums into the history
-// ring (ibm_box_sums_tail) instead of a separate force-sum kernel.
-template <int S, bool PULL>
-__global__ void __launch_bounds__(256) k_stream_collide_box_sums(const typename Pop<S>::T* __restrict__ fin,
-                                                                 typename Pop<S>::T* __restrict__ fout,
+// Forced pass over the cells of the IBM force box (the complement of the bulk pass), by
+// rows of the box. Work item w is x segment w % nseg of row w / nseg of the box's (y, z)
+// rows, nseg from the box's x extent; the blocks step through the items (grid-stride,
+// grid sized by the host from the box bound), so no block is launched for rows the box
+// does not have. Along a row the cells are consecutive, so the pass uses the bulk pass's
+// coalesced bodies: two cells per thread from x = i0 rounded down to even in the 16-bit
+// forms (pair_body), one cell per thread from i0 in float32 (stream_collide_cell); cells
+// outside the box are left to the bulk pass. SUMS: the block's integer force sums go to
+// ibm_box_sums_tail (force sums of the call whose box this is, history ring, call
+// counter).
+template <int S, bool PULL, bool SUMS, bool IDX32>
+__global__ void __launch_bounds__(kBoxBlock, 16) k_box_rows_pair(const typename Pair<S>::T* __restrict__ fin,
+                                                                 typename Pair<S>::T* __restrict__ fout,
                                                                  Grid g, Coef c, ForceArgs fa, IbmArrays a) {
     const Band b = load_band(fa.dev, fa.slot);
-    const int cells = b.ilen * b.jlen * b.klen;
-    long long kx = 0, ky = 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells; t += gridDim.x * blockDim.x)
-        box_pass_cell<S, PULL, true>(fin, fout, g, c, fa, b, t, &kx, &ky);
-    ibm_box_sums_tail(a, kx, ky);
+    const int xa = b.i0 & ~1;
+    const int nseg = (b.i0 + b.ilen - xa + 2 * kBoxBlock - 1) / (2 * kBoxBlock);
+    const int items = nseg * b.jlen * b.klen;
+    long long ks[2] = {0, 0};
+    for (int w = blockIdx.x; w < items; w += gridDim.x) {   // block-uniform
+        const int seg = w % nseg, r = w / nseg;
+        const int y = pmod(b.j0 + r % b.jlen, g.ny), z = pmod(b.k0 + r / b.jlen, g.nz);
+        pair_body<S, PULL, kForceOnlyBand, IDX32>(fin, fout, g, c, fa,
+                                                  xa + seg * 2 * kBoxBlock + 2 * (int)threadIdx.x, y, z,
+                                                  SUMS ? ks : nullptr);
+    }
+    if (SUMS) ibm_box_sums_tail(a, ks[0], ks[1]);
+}
+
+template <int S, bool PULL, bool SUMS>
+__global__ void __launch_bounds__(kBoxBlock, 8) k_box_rows_cell(const typename Pop<S>::T* __restrict__ fin,
+                                                                typename Pop<S>::T* __restrict__ fout,
+                                                                Grid g, Coef c, ForceArgs fa, IbmArrays a) {
+    const Band b = load_band(fa.dev, fa.slot);
+    const int nseg = (b.ilen + kBoxBlock - 1) / kBoxBlock;
+    const int items = nseg * b.jlen * b.klen;
+    long long ks[2] = {0, 0};
+    for (int w = blockIdx.x; w < items; w += gridDim.x) {
+        const int seg = w % nseg, r = w / nseg;
+        const int x = b.i0 + seg * kBoxBlock + (int)threadIdx.x;
+        const int y = pmod(b.j0 + r % b.jlen, g.ny), z = pmod(b.k0 + r / b.jlen, g.nz);
+        if (x < b.i0 + b.ilen)
+            stream_collide_cell<S, PULL, kForceOnlyBand>(fin, fout, g, c, fa, x, y, z, SUMS ? ks : nullptr);
+    }
+    if (SUMS) ibm_box_sums_tail(a, ks[0], ks[1]);
 }
 
 // ------------------------------------------------------------------ 16-bit pair kernel
@@ -583,31 +608,54 @@ int knob(const char* name, int def) {
     return e ? std::atoi(e) : def;
 }
 
-static int box_blocks(long long max_cells, int block) {
-    const long long b = (max_cells + block - 1) / block;
-    return (int)std::max<long long>(1, std::min<long long>(b, 4 * 152));
+// Launch of the box pass by rows for a box of at most max_bx x max_by x max_bz cells: one
+// block per work item of the largest box, at most 4 blocks per SM (then grid-stride).
+template <bool SUMS>
+static void box_rows_launch(int storage, bool pull, const void* fin, void* fout, const Grid& g,
+                            const Coef& c, const ForceArgs& fa, const IbmArrays& a, int max_bx,
+                            int max_by, int max_bz, cudaStream_t st) {
+    const long long rows = (long long)std::max(max_by, 1) * std::max(max_bz, 1);
+    const bool f32 = storage == CLBM_STORE_F32;
+    // float32 one cell per thread; the 16-bit pairs start at i0 rounded down to even
+    const long long nseg = f32 ? (max_bx + kBoxBlock - 1) / kBoxBlock
+                               : (max_bx + 1 + 2 * kBoxBlock - 1) / (2 * kBoxBlock);
+    const int blocks = (int)std::max<long long>(1, std::min<long long>(std::max<long long>(nseg, 1) * rows, 4 * 152));
+    if (f32) {
+        if (pull) k_box_rows_cell<CLBM_STORE_F32, true, SUMS><<<blocks, kBoxBlock, 0, st>>>((const float*)fin, (float*)fout, g, c, fa, a);
+        else k_box_rows_cell<CLBM_STORE_F32, false, SUMS><<<blocks, kBoxBlock, 0, st>>>((const float*)fin, (float*)fout, g, c, fa, a);
+        return;
+    }
+    const bool i32 = 19LL * g.plane <= 0xffffffffLL;
+#define CLBM_BOX_ROWS(S_)                                                                                  \
+    {                                                                                                      \
+        using T = typename Pair<S_>::T;                                                                    \
+        if (pull && i32) k_box_rows_pair<S_, true, SUMS, true><<<blocks, kBoxBlock, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);   \
+        else if (pull) k_box_rows_pair<S_, true, SUMS, false><<<blocks, kBoxBlock, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);  \
+        else if (i32) k_box_rows_pair<S_, false, SUMS, true><<<blocks, kBoxBlock, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);  \
+        else k_box_rows_pair<S_, false, SUMS, false><<<blocks, kBoxBlock, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);          \
+    }
+    if (storage == CLBM_STORE_F16S) CLBM_BOX_ROWS(CLBM_STORE_F16S)
+    else CLBM_BOX_ROWS(CLBM_STORE_BF16S)
+#undef CLBM_BOX_ROWS
 }
 
 void launch_stream_collide_box(int storage, bool pull, const void* fin, void* fout,
-                               const Grid& g, const Coef& c, const ForceArgs& fa,
-                               long long max_cells, cudaStream_t st) {
-    const int blocks = box_blocks(max_cells, 256);
-    CLBM_DISPATCH_STORE(storage, {
-        using T = typename Pop<S_>::T;
-        if (pull) k_stream_collide_box<S_, true><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-        else k_stream_collide_box<S_, false><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-    });
+                               const Grid& g, const Coef& c, const ForceArgs& fa, int max_bx,
+                               int max_by, int max_bz, cudaStream_t st) {
+    box_rows_launch<false>(storage, pull, fin, fout, g, c, fa, IbmArrays{}, max_bx, max_by, max_bz, st);
 }
 
 void launch_stream_collide_box_sums(int storage, bool pull, const void* fin, void* fout,
                                     const Grid& g, const Coef& c, const ForceArgs& fa,
-                                    const IbmArrays& a, long long max_cells, cudaStream_t st) {
-    const int blocks = box_blocks(max_cells, 256);
-    CLBM_DISPATCH_STORE(storage, {
-        using T = typename Pop<S_>::T;
-        if (pull) k_stream_collide_box_sums<S_, true><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);
-        else k_stream_collide_box_sums<S_, false><<<blocks, 256, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, a);
-    });
+                                    const IbmArrays& a, cudaStream_t st) {
+    box_rows_launch<true>(storage, pull, fin, fout, g, c, fa, a, a.max_bx, a.max_by, a.max_bz, st);
+}
+
+// Blocks of kBoxBlock threads for a box of at most max_cells cells: one cell per thread,
+// at most 16 blocks per SM (then grid-stride).
+static int box_blocks(long long max_cells) {
+    const long long b = (max_cells + kBoxBlock - 1) / kBoxBlock;
+    return (int)std::max<long long>(1, std::min<long long>(b, 16 * 152));
 }
 
 void launch_macro_full(int storage, bool pull, const void* f, const Grid& g, const Coef& c,
@@ -663,7 +711,7 @@ void launch_import_populations(int storage, const float* in, void* f, const Grid
 
 // Band-prepare needs the same gather; the IBM translation unit calls this launcher.
 template <int S, bool PULL>
-__global__ void k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
+__global__ void __launch_bounds__(kBoxBlock) k_band_prepare(const typename Pop<S>::T* __restrict__ fin, Grid g, Coef c,
                                IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux,
                                float* uy, float* uz, bool compute_macro) {
     band_prepare_body<S, PULL>(fin, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro, blockIdx.x,
@@ -674,11 +722,11 @@ void launch_band_prepare(int storage, bool pull, const void* f, const Grid& g, c
                          IbmDev* dev, long long* fx, long long* fy, float* rho, float* ux, float* uy,
                          float* uz, int max_bx, int max_by, int max_bz, bool compute_macro,
                          cudaStream_t st) {
-    const int blocks = box_blocks((long long)max_bx * max_by * max_bz, 256);
+    const int blocks = box_blocks((long long)max_bx * max_by * max_bz);
     CLBM_DISPATCH_STORE(storage, {
         using T = typename Pop<S_>::T;
-        if (pull) k_band_prepare<S_, true><<<blocks, 256, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
-        else k_band_prepare<S_, false><<<blocks, 256, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+        if (pull) k_band_prepare<S_, true><<<blocks, kBoxBlock, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
+        else k_band_prepare<S_, false><<<blocks, kBoxBlock, 0, st>>>((const T*)f, g, c, dev, fx, fy, rho, ux, uy, uz, compute_macro);
     });
 }
 
