@@ -687,82 +687,54 @@ template <> struct Pair<CLBM_STORE_BF16S> {
     }
 };
 
-// Cells (x0, x0 + 1) of row (y, z), x0 even, for a warp of consecutive pairs of one row
-// (lanes past the lattice edge take part in the shuffles and store nothing).
-// IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
-// P: the loads and stores of the storage form (Pair<S>).
-// kForceOnlyBand (box pass): only the cells inside the force box are collided and stored;
-// with ks, their clipped forces in units of 2^-40 are added to ks[0], ks[1] (exact).
-template <int S, bool PULL, int FMODE, bool IDX32 = false, class P = Pair<S>>
-__device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
-                                          typename Pair<S>::T* __restrict__ fout, const Grid& g,
-                                          const Coef& c, const ForceArgs& fa, int x0, int y, int z,
-                                          long long* ks = nullptr) {
+// Boundary columns of a pulled cell pair (x0, x0 + 1) of row (y, z), x0 even: the Zou-He
+// inlet at x0 = 0 on f = h + w (clbm_moving.py:266-294) and the outlet column Nx-1, a copy
+// of column Nx-2 (clbm_moving.py:296-300). For odd Nx the outlet is the first cell of the
+// last pair and its populations are pulled again like column Nx-2's.
+template <int S, bool IDX32, class P = Pair<S>>
+__device__ __forceinline__ void pair_boundaries(const typename Pair<S>::T* __restrict__ fin,
+                                                const Grid& g, const Coef& c, int x0, int y, int z,
+                                                float (&h0)[19], float (&h1)[19]) {
     using I = typename std::conditional<IDX32, unsigned, long long>::type;
-    const I plane = (I)g.plane;
-    constexpr unsigned kFull = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
-    // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
-    if (__all_sync(kFull, !act0)) return;
-    const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
-    const I row = ((I)z * (I)g.ny + (I)y) * (I)g.pitch;
-    float h0[19], h1[19];
-    if (!PULL) {
+    if (x0 == 0) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) {
-            const float2 p = P::ld2(fin + ((I)q * plane + row + (I)x0c));
-            h0[q] = p.x;
-            h1[q] = p.y;
-        }
-    } else {
+        for (int q = 0; q < 19; ++q) h0[q] += wq(q);
+        zou_he(h0, c);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) h0[q] -= wq(q);
+    }
+    if (x0 + 1 == g.nx - 1) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) h1[q] = h0[q];
+    } else if (x0 == g.nx - 1) {
         const int ym = (y == 0) ? g.ny - 1 : y - 1;
         const int yp = (y == g.ny - 1) ? 0 : y + 1;
         const int zm = (z == 0) ? g.nz - 1 : z - 1;
         const int zp = (z == g.nz - 1) ? 0 : z + 1;
+        const int xe = g.nx - 2;
+        const I plane = (I)g.plane;
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
             const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
             const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-            const typename P::T* rp = fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch);
-            const float2 p = P::ld2(rp + x0c);
-            if (ex(q) == 0) {
-                h0[q] = p.x;
-                h1[q] = p.y;
-            } else if (ex(q) == 1) {  // pull from x - 1
-                float up = __shfl_up_sync(kFull, p.y, 1);
-                if (lane == 0) up = (x0 >= 1 && x0 - 1 < g.nx) ? P::ld1(rp + (x0 - 1)) : 0.0f;
-                h0[q] = up;   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
-                h1[q] = p.x;
-            } else {                  // pull from x + 1
-                float dn = __shfl_down_sync(kFull, p.x, 1);
-                if (lane == 31) dn = (x0 + 2 < g.nx) ? P::ld1(rp + (x0 + 2)) : 0.0f;
-                h0[q] = p.y;
-                h1[q] = dn;
-            }
-        }
-        if (x0 == 0) {
-#pragma unroll
-            for (int q = 0; q < 19; ++q) h0[q] += wq(q);
-            zou_he(h0, c);
-#pragma unroll
-            for (int q = 0; q < 19; ++q) h0[q] -= wq(q);
-        }
-        if (x0 + 1 == g.nx - 1) {
-            // outlet column Nx-1 is a copy of column Nx-2 = x0 (clbm_moving.py:296-300)
-#pragma unroll
-            for (int q = 0; q < 19; ++q) h1[q] = h0[q];
-        } else if (x0 == g.nx - 1) {
-            // odd Nx: the outlet is the first cell of the last pair; pull like column Nx-2
-            const int xe = g.nx - 2;
-#pragma unroll
-            for (int q = 0; q < 19; ++q) {
-                const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
-                const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-                h0[q] = P::ld1(fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)(xe - ex(q))));
-            }
+            h0[q] = P::ld1(fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)(xe - ex(q))));
         }
     }
+}
+
+// Everything of a cell pair after its post-stream populations (h0, h1) are gathered: the
+// force-box test, the body force per FMODE, the collision and the stores. act0 / act1: the
+// cell lies inside the lattice. kForceOnlyBand (box pass): only the cells inside the force
+// box are collided and stored; with ks, their clipped forces in units of 2^-40 are added to
+// ks[0], ks[1] (exact).
+template <int S, int FMODE, bool IDX32, class P = Pair<S>>
+__device__ __forceinline__ void pair_finish(typename Pair<S>::T* __restrict__ fout, const Grid& g,
+                                            const Coef& c, const ForceArgs& fa, int x0, int y, int z,
+                                            bool act0, bool act1, float (&h0)[19], float (&h1)[19],
+                                            long long* ks) {
+    using I = typename std::conditional<IDX32, unsigned, long long>::type;
+    const I plane = (I)g.plane;
+    const I row = ((I)z * (I)g.ny + (I)y) * (I)g.pitch;
     // cells of the IBM force box: tested after the loads, so the box read does not delay them
     bool in0 = false, in1 = false;
     if (FMODE == kForceSkipBand || FMODE == kForceBand || FMODE == kForceOnlyBand) {
@@ -821,6 +793,64 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
             for (int q = 0; q < 19; ++q) P::st1(fout + ((I)q * plane + row + (I)x0 + 1), h1[q]);
         }
     }
+}
+
+// Cells (x0, x0 + 1) of row (y, z), x0 even, for a warp of consecutive pairs of one row
+// (lanes past the lattice edge take part in the shuffles and store nothing).
+// IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
+// P: the loads and stores of the storage form (Pair<S>).
+// ks: force sums of the box pass (pair_finish).
+template <int S, bool PULL, int FMODE, bool IDX32 = false, class P = Pair<S>>
+__device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict__ fin,
+                                          typename Pair<S>::T* __restrict__ fout, const Grid& g,
+                                          const Coef& c, const ForceArgs& fa, int x0, int y, int z,
+                                          long long* ks = nullptr) {
+    using I = typename std::conditional<IDX32, unsigned, long long>::type;
+    const I plane = (I)g.plane;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool act0 = x0 < g.nx, act1 = x0 + 1 < g.nx;
+    // warp-uniform exit: every lane of a warp that stays takes part in the shuffles
+    if (__all_sync(kFull, !act0)) return;
+    const int x0c = min(x0, g.pitch - 2);  // in-row address for lanes past the lattice edge
+    const I row = ((I)z * (I)g.ny + (I)y) * (I)g.pitch;
+    float h0[19], h1[19];
+    if (!PULL) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const float2 p = P::ld2(fin + ((I)q * plane + row + (I)x0c));
+            h0[q] = p.x;
+            h1[q] = p.y;
+        }
+    } else {
+        const int ym = (y == 0) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1) ? 0 : y + 1;
+        const int zm = (z == 0) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1) ? 0 : z + 1;
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
+            const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
+            const typename P::T* rp = fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch);
+            const float2 p = P::ld2(rp + x0c);
+            if (ex(q) == 0) {
+                h0[q] = p.x;
+                h1[q] = p.y;
+            } else if (ex(q) == 1) {  // pull from x - 1
+                float up = __shfl_up_sync(kFull, p.y, 1);
+                if (lane == 0) up = (x0 >= 1 && x0 - 1 < g.nx) ? P::ld1(rp + (x0 - 1)) : 0.0f;
+                h0[q] = up;   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
+                h1[q] = p.x;
+            } else {                  // pull from x + 1
+                float dn = __shfl_down_sync(kFull, p.x, 1);
+                if (lane == 31) dn = (x0 + 2 < g.nx) ? P::ld1(rp + (x0 + 2)) : 0.0f;
+                h0[q] = p.y;
+                h1[q] = dn;
+            }
+        }
+        pair_boundaries<S, IDX32, P>(fin, g, c, x0, y, z, h0, h1);
+    }
+    pair_finish<S, FMODE, IDX32, P>(fout, g, c, fa, x0, y, z, act0, act1, h0, h1, ks);
 }
 
 
