@@ -117,7 +117,8 @@ def lib():
             "clbm_ensemble_run": [vp, i32, i32],
             "clbm_ensemble_stream": [vp, pvp],
             "clbm_ensemble_tuning": [vp, ctypes.POINTER(i32), ctypes.POINTER(i32),
-                                     ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_float)],
+                                     ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(i32)],
             "clbm_ensemble_destroy": [vp],
             "clbm_closure_layout": [P],
             "clbm_closure_set": [vp, P],

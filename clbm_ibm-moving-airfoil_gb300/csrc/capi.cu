@@ -980,17 +980,19 @@ struct clbm_ensemble {
     long long ntiles = 0;
     int bx = 128;            // bulk tile width (cells)
     int grid = 0;            // persistent bulk blocks
-    // instances grouped by row width, one row per block (rows = true when the autotuner
-    // chose it)
+    // instances grouped by row width, whole rows per block (rows = true when the autotuner
+    // chose it), rows_per_tile rows per tile
     struct Group {
         EnsDesc* d = nullptr;
         long long* tile0 = nullptr;
         int n = 0;
         long long ntiles = 0;
         int threads = 0;
+        bool idx32 = true;   // 19 * plane of every member below 2^32
     };
     std::vector<Group> groups;
     bool rows = false;
+    int rows_per_tile = 1;
     float bulk_ms = 0.f;     // time of one bulk pass of the chosen schedule at creation
     int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
@@ -1020,10 +1022,20 @@ EnsDesc member_desc(const clbm_ensemble* e, int i) {
     return D;
 }
 
+void ens_free_groups(clbm_ensemble* e) {
+    for (auto& G : e->groups) {
+        if (G.d) cudaFree(G.d);
+        if (G.tile0) cudaFree(G.tile0);
+    }
+    e->groups.clear();
+}
+
 // Members grouped by the threads a whole row needs (a multiple of 32; two cells per thread
 // in the 16-bit forms, one in float32; rows up to 512 cells); each group's descriptors list
-// its members with tiles = rows. No groups when a row is wider.
-int ens_groups(clbm_ensemble* e) {
+// its members with tiles of R rows. No groups when a row is wider.
+int ens_groups(clbm_ensemble* e, int R) {
+    ens_free_groups(e);
+    e->rows_per_tile = R;
     const bool f32 = e->storage == CLBM_STORE_F32;   // one cell per thread, rows up to 512
     std::vector<int> th(e->n);
     for (int i = 0; i < e->n; ++i) {
@@ -1038,18 +1050,21 @@ int ens_groups(clbm_ensemble* e) {
         std::vector<EnsDesc> h;
         std::vector<long long> t0;
         long long tiles = 0;
+        bool idx32 = true;
         for (int i = 0; i < e->n; ++i) {
             if (th[i] != w) continue;
             EnsDesc D = member_desc(e, i);
             D.tile0 = tiles;
             t0.push_back(tiles);
-            tiles += (long long)D.g.ny * D.g.nz;
+            tiles += ((long long)D.g.ny * D.g.nz + R - 1) / R;
+            idx32 = idx32 && 19LL * D.g.plane <= 0xffffffffLL;
             h.push_back(D);
         }
         clbm_ensemble::Group gr;
         gr.n = (int)h.size();
         gr.ntiles = tiles;
         gr.threads = w;
+        gr.idx32 = idx32;
         e->groups.push_back(gr);
         clbm_ensemble::Group& G = e->groups.back();
         CK(cudaMalloc(&G.d, sizeof(EnsDesc) * G.n));
@@ -1063,7 +1078,7 @@ int ens_groups(clbm_ensemble* e) {
 
 void ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
     for (const auto& G : e->groups)
-        launch_ens_bulk_rows(e->storage, pull, G.threads, G.d, G.tile0, G.n, G.ntiles, e->cur,
+        launch_ens_bulk_rows(e->storage, pull, G.threads, e->rows_per_tile, G.idx32, G.d, G.tile0, G.n, G.ntiles, e->cur,
                              (int)std::min<long long>(G.ntiles, 1LL << 30), st);
 }
 
@@ -1132,8 +1147,17 @@ int ens_tune(clbm_ensemble* e) {
     e->grid = best_grid;
     e->bulk_ms = best / 3.0f;
     e->rows = false;
-    if (int rc = ens_groups(e)) return rc;
-    if (!e->groups.empty()) {   // one row per block, instances grouped by row width
+    // whole rows per block, instances grouped by row width, R rows per tile (the instance
+    // lookup is paid once per tile); CLBM_ENS_ROWS=1 / 0 forces / forbids the row mode
+    // (tests), CLBM_ENS_ROWS_R fixes R; default: the fastest
+    const int force = knob("CLBM_ENS_ROWS", -1);
+    const int fixed_r = knob("CLBM_ENS_ROWS_R", 0);
+    float best_rows = 1e30f;
+    int best_r = 1;
+    const std::vector<int> cand_r = fixed_r > 0 ? std::vector<int>{fixed_r} : std::vector<int>{1, 2, 4, 8};
+    for (int R : cand_r) {
+        if (int rc = ens_groups(e, R)) return rc;
+        if (e->groups.empty()) break;
         ens_bulk_rows(e, true, e->st);
         CK(cudaEventRecord(e0, e->st));
         for (int k = 0; k < 3; ++k) ens_bulk_rows(e, true, e->st);
@@ -1143,12 +1167,15 @@ int ens_tune(clbm_ensemble* e) {
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         e->launches += 4 * (long long)e->groups.size();
-        // CLBM_ENS_ROWS=1 / 0 forces / forbids the row mode (tests); default: the faster
-        const int force = knob("CLBM_ENS_ROWS", -1);
-        if (force == 1 || (force != 0 && ms < best)) {
-            e->rows = true;
-            e->bulk_ms = ms / 3.0f;
+        if (ms < best_rows) {
+            best_rows = ms;
+            best_r = R;
         }
+    }
+    if (!e->groups.empty() && (force == 1 || (force != 0 && best_rows < best))) {
+        if (int rc = ens_groups(e, best_r)) return rc;
+        e->rows = true;
+        e->bulk_ms = best_rows / 3.0f;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1334,8 +1361,9 @@ int clbm_ensemble_stream(const clbm_ensemble* e, void** out) {
 }
 
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
-                         int64_t* tiles, float* bulk_ms) {
+                         int64_t* tiles, float* bulk_ms, int32_t* rows_per_block) {
     if (!e) return fail(CLBM_ERR_ARG, "clbm_ensemble_tuning: null ensemble");
+    if (rows_per_block) *rows_per_block = e->rows ? e->rows_per_tile : 0;
     long long rows = 0;
     for (const auto& G : e->groups) rows += G.ntiles;
     if (tile_width) *tile_width = e->rows ? 0 : e->bx;
@@ -1351,10 +1379,7 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     if (e->st2) cudaStreamSynchronize(e->st2);
     ens_free_graph(e);
     if (e->d_desc) cudaFree(e->d_desc);
-    for (auto& G : e->groups) {
-        if (G.d) cudaFree(G.d);
-        if (G.tile0) cudaFree(G.tile0);
-    }
+    ens_free_groups(e);
     if (e->d_tile0) cudaFree(e->d_tile0);
     if (e->d_off) cudaFree(e->d_off);
     cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};

@@ -388,11 +388,13 @@ void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t 
 void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st);
 void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const long long* tile0,
                      int n, long long ntiles, int parity, int grid, cudaStream_t st);
-// One row per block of `threads` (a multiple of 32: >= Nx / 2 in the 16-bit forms, <= 256;
-// >= Nx in float32, <= 512) over a group of instances of that row width: tiles are rows,
-// tile0 per instance of the group.
-void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
-                          int n, long long ntiles, int parity, int grid, cudaStream_t st);
+// Whole rows per block of `threads` (a multiple of 32: >= Nx / 2 in the 16-bit forms,
+// <= 256; >= Nx in float32, <= 512) over a group of instances of that row width: a tile is
+// rows_per_tile consecutive rows of one instance, tile0 per instance of the group. idx32:
+// every instance of the group has 19 * plane < 2^32 (32-bit element indices).
+void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile, bool idx32,
+                          const EnsDesc* d, const long long* tile0, int n, long long ntiles,
+                          int parity, int grid, cudaStream_t st);
 // Force-box cells of all members as one flat list (offsets per member, n + 1 each), then
 // band-prepare and box pass over it with `grid` blocks of 256 threads.
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st);

@@ -189,15 +189,17 @@ kb_bulk(const EnsDesc* __restrict__ d, const long long* __restrict__ tile0, int 
     }
 }
 
-// 16-bit forms, one row per block: tile t of a group is row (t - tile0[i]) of instance i
-// (y fastest), the block's warps cover the row with two cells per thread (blockDim.x >=
-// Nx / 2, the smallest multiple of 32). Instances are grouped by that width, one launch per
-// group, so a 150-, 200- or 300-cell row costs 3, 4 or 5 warps and the row (y, z) stays
-// uniform across the block.
-template <int S, bool PULL>
+// 16-bit forms, whole rows per block: tile t of a group is rows R (t - tile0[i]) ...
+// R (t - tile0[i]) + R - 1 of instance i (row index z * ny + y, y fastest), computed one
+// after the other; the block's warps cover a row with two cells per thread (blockDim.x >=
+// Nx / 2, the smallest multiple of 32). Instances are grouped by that width, one launch
+// per group, so a 150-, 200- or 300-cell row costs 3, 4 or 5 warps and the row (y, z)
+// stays uniform across the block. The instance lookup and its descriptor reads (dependent
+// loads) are paid once per R rows.
+template <int S, bool PULL, bool IDX32>
 __global__ void __launch_bounds__(256, 4) kb_bulk_row(const EnsDesc* __restrict__ d,
                                                     const long long* __restrict__ tile0, int n,
-                                                    long long ntiles, int parity) {
+                                                    long long ntiles, int parity, int R) {
     using T = typename Pop<S>::T;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int lo = 0, hi = n - 1;
@@ -209,26 +211,30 @@ __global__ void __launch_bounds__(256, 4) kb_bulk_row(const EnsDesc* __restrict_
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
         const Coef c = D.c;
-        const int r = (int)(t - D.tile0);   // row z * ny + y
-        const int y = r % g.ny, z = r / g.ny;
+        const int rows = g.ny * g.nz;
+        const int r0 = (int)(t - D.tile0) * R;
+        const int r1 = min(r0 + R, rows);
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
         ForceArgs fa{};
         if (D.has_ibm) {
             fa.dev = D.a.dev;
             fa.slot = (int)(D.a.dev->cur & 1);
-            pair_body<S, PULL, kForceSkipBand>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
+            for (int r = r0; r < r1; ++r)
+                pair_body<S, PULL, kForceSkipBand, IDX32>(fin, fout, g, c, fa, 2 * threadIdx.x, r % g.ny, r / g.ny);
         } else {
-            pair_body<S, PULL, kForceNone>(fin, fout, g, c, fa, 2 * threadIdx.x, y, z);
+            for (int r = r0; r < r1; ++r)
+                pair_body<S, PULL, kForceNone, IDX32>(fin, fout, g, c, fa, 2 * threadIdx.x, r % g.ny, r / g.ny);
         }
     }
 }
 
-// Float32, one row per block: one cell per thread, blockDim.x >= Nx (a multiple of 32).
+// Float32, whole rows per block (R per tile, as above): one cell per thread, blockDim.x >=
+// Nx (a multiple of 32).
 template <bool PULL>
 __global__ void __launch_bounds__(512) kb_bulk_row_f32(const EnsDesc* __restrict__ d,
                                                        const long long* __restrict__ tile0, int n,
-                                                       long long ntiles, int parity) {
+                                                       long long ntiles, int parity, int R) {
     using T = typename Pop<CLBM_STORE_F32>::T;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         int lo = 0, hi = n - 1;
@@ -240,34 +246,45 @@ __global__ void __launch_bounds__(512) kb_bulk_row_f32(const EnsDesc* __restrict
         const EnsDesc& D = d[lo];
         const Grid g = D.g;
         const Coef c = D.c;
-        const int r = (int)(t - D.tile0);   // row z * ny + y
         const int x = threadIdx.x;
         if (x >= g.nx) continue;
+        const int rows = g.ny * g.nz;
+        const int r0 = (int)(t - D.tile0) * R;
+        const int r1 = min(r0 + R, rows);
         const T* fin = (const T*)D.f[parity];
         T* fout = (T*)D.f[parity ^ 1];
         ForceArgs fa{};
         if (D.has_ibm) {
             fa.dev = D.a.dev;
             fa.slot = (int)(D.a.dev->cur & 1);
-            stream_collide_cell<CLBM_STORE_F32, PULL, kForceSkipBand>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
+            for (int r = r0; r < r1; ++r)
+                stream_collide_cell<CLBM_STORE_F32, PULL, kForceSkipBand>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
         } else {
-            stream_collide_cell<CLBM_STORE_F32, PULL, kForceNone>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
+            for (int r = r0; r < r1; ++r)
+                stream_collide_cell<CLBM_STORE_F32, PULL, kForceNone>(fin, fout, g, c, fa, x, r % g.ny, r / g.ny);
         }
     }
 }
 
-void launch_ens_bulk_rows(int storage, bool pull, int threads, const EnsDesc* d, const long long* tile0,
-                          int n, long long ntiles, int parity, int grid, cudaStream_t st) {
+void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile, bool idx32,
+                          const EnsDesc* d, const long long* tile0, int n, long long ntiles,
+                          int parity, int grid, cudaStream_t st) {
+    const int R = rows_per_tile;
     if (storage == CLBM_STORE_F32) {
-        if (pull) kb_bulk_row_f32<true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
-        else kb_bulk_row_f32<false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
-    } else if (storage == CLBM_STORE_F16S) {
-        if (pull) kb_bulk_row<CLBM_STORE_F16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
-        else kb_bulk_row<CLBM_STORE_F16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
-    } else if (storage == CLBM_STORE_BF16S) {
-        if (pull) kb_bulk_row<CLBM_STORE_BF16S, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
-        else kb_bulk_row<CLBM_STORE_BF16S, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity);
+        if (pull) kb_bulk_row_f32<true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
+        else kb_bulk_row_f32<false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);
+        return;
     }
+#define CLBM_ENS_ROW(S_)                                                                                  \
+    {                                                                                                     \
+        if (pull && idx32) kb_bulk_row<S_, true, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);  \
+        else if (pull) kb_bulk_row<S_, true, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);     \
+        else if (idx32) kb_bulk_row<S_, false, true><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);    \
+        else kb_bulk_row<S_, false, false><<<grid, threads, 0, st>>>(d, tile0, n, ntiles, parity, R);             \
+    }
+    if (storage == CLBM_STORE_F16S) CLBM_ENS_ROW(CLBM_STORE_F16S)
+    else if (storage == CLBM_STORE_BF16S) CLBM_ENS_ROW(CLBM_STORE_BF16S)
+#undef CLBM_ENS_ROW
 }
 
 #define CLBM_ENS_STORE(storage, ...)                                                         \

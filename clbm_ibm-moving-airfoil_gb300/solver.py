@@ -348,9 +348,11 @@ class Ensemble:
         """Bulk-pass schedule chosen at creation and the time of one bulk pass of all
         members with it, alone (bulk_us)."""
         w, b, t, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_float()
+        r = ctypes.c_int32()
         check(lib().clbm_ensemble_tuning(self._h, ctypes.byref(w), ctypes.byref(b), ctypes.byref(t),
-                                         ctypes.byref(ms)))
-        return dict(tile_width=w.value, blocks=b.value, tiles=t.value, bulk_us=round(ms.value * 1e3, 2))
+                                         ctypes.byref(ms), ctypes.byref(r)))
+        return dict(tile_width=w.value, blocks=b.value, tiles=t.value, bulk_us=round(ms.value * 1e3, 2),
+                    rows_per_block=r.value)
 
     def synchronize(self):
         for s in self.sims:

@@ -172,12 +172,12 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
  * device), as a two-step CUDA graph replay when use_graph != 0. */
 int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph);
 int clbm_ensemble_stream(const clbm_ensemble* e, void** out);
-/* The bulk-pass schedule chosen at creation: tile width (cells; 0: one row per block,
- * members grouped by row width, one launch per group), blocks, tiles, and the time
- * of one bulk pass of all members with it, alone, in milliseconds (any pointer may be
- * NULL). */
+/* The bulk-pass schedule chosen at creation: tile width (cells; 0: whole rows per block,
+ * members grouped by row width, one launch per group), blocks, tiles, the time of one
+ * bulk pass of all members with it, alone, in milliseconds, and in the row mode the rows
+ * one block computes per tile (0 otherwise). Any pointer may be NULL. */
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
-                         int64_t* tiles, float* bulk_ms);
+                         int64_t* tiles, float* bulk_ms, int32_t* rows_per_block);
 int clbm_ensemble_destroy(clbm_ensemble* e);
 
 /* Wait for all queued work of the solver. Returns CLBM_ERR_STATE when a bounded device

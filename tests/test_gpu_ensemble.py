@@ -22,19 +22,25 @@ def _cases(pkg, storage, n=5, lattices=SMALL):
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", ["cell", "pair"])
 @pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
-@pytest.mark.parametrize("rows", ["1", "0"])
+@pytest.mark.parametrize("rows", ["1", "1:3", "0"])
 def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant, lattices,
                                             rows):
     """The single runs use either full-grid kernel; all variants give the same bits; the
-    16-bit ensemble bulk pass with one row per block (rows = 1) or row segments."""
+    ensemble bulk pass with whole rows per block (rows = 1: the autotuner's rows per tile;
+    1:3: three rows per tile, which does not divide the members' row counts) or with row
+    segments / runs (0)."""
     pkg = built_pkg
     monkeypatch.setenv("CLBM_KERNEL", variant)
-    monkeypatch.setenv("CLBM_ENS_ROWS", rows)
+    mode, _, per_tile = rows.partition(":")
+    monkeypatch.setenv("CLBM_ENS_ROWS", mode)
+    monkeypatch.setenv("CLBM_ENS_ROWS_R", per_tile or "0")
     cases = _cases(pkg, storage, lattices=lattices)
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
     t = ens.tuning()
     assert t["tile_width"] in (0, 128, 256) and t["blocks"] > 0 and t["tiles"] > 0
+    if mode == "1":
+        assert t["tile_width"] == 0 and t["rows_per_block"] == int(per_tile or t["rows_per_block"]) > 0
     for cfg, member in zip(cases, ens.sims):
         alone = pkg.Simulation(cfg)
         alone.run(24, graph=graph)
