@@ -993,6 +993,10 @@ struct clbm_ensemble {
     std::vector<Group> groups;
     bool rows = false;
     int rows_per_tile = 1;
+    // streams of the groups after the first (the groups' bulk launches run concurrently, so
+    // the short launches of the small groups fill each other's ramp-up and tail)
+    std::vector<cudaStream_t> gst;
+    std::vector<cudaEvent_t> gev;   // [0]: fork; [1 + k]: end of group k + 1
     float bulk_ms = 0.f;     // time of one bulk pass of the chosen schedule at creation
     int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
@@ -1072,14 +1076,40 @@ int ens_groups(clbm_ensemble* e, int R) {
         CK(cudaMemcpyAsync(G.d, h.data(), sizeof(EnsDesc) * G.n, cudaMemcpyHostToDevice, e->st));
         CK(cudaMemcpyAsync(G.tile0, t0.data(), sizeof(long long) * G.n, cudaMemcpyHostToDevice, e->st));
     }
+    // the group with the most tiles first
+    std::stable_sort(e->groups.begin(), e->groups.end(),
+                     [](const clbm_ensemble::Group& a, const clbm_ensemble::Group& b) { return a.ntiles > b.ntiles; });
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    while (e->gst.size() + 1 < e->groups.size()) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lo));
+        e->gst.push_back(st);
+    }
+    while (e->gev.size() < e->groups.size()) {
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        e->gev.push_back(ev);
+    }
     CK(cudaStreamSynchronize(e->st));
     return CLBM_OK;
 }
 
-void ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
-    for (const auto& G : e->groups)
-        launch_ens_bulk_rows(e->storage, pull, G.threads, e->rows_per_tile, G.idx32, G.d, G.tile0, G.n, G.ntiles, e->cur,
-                             (int)std::min<long long>(G.ntiles, 1LL << 30), st);
+// Bulk pass in the row mode: one launch per group, the first on `st`, the others on their
+// own streams forked from and joined back to `st`.
+int ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
+    const size_t ng = e->groups.size();
+    if (ng > 1) CK(cudaEventRecord(e->gev[0], st));
+    for (size_t k = 0; k < ng; ++k) {
+        const auto& G = e->groups[k];
+        cudaStream_t sk = k == 0 ? st : e->gst[k - 1];
+        if (k > 0) CK(cudaStreamWaitEvent(sk, e->gev[0], 0));
+        launch_ens_bulk_rows(e->storage, pull, G.threads, e->rows_per_tile, G.idx32, G.d, G.tile0, G.n,
+                             G.ntiles, e->cur, (int)std::min<long long>(G.ntiles, 1LL << 30), sk);
+        if (k > 0) CK(cudaEventRecord(e->gev[k], sk));
+    }
+    for (size_t k = 1; k < ng; ++k) CK(cudaStreamWaitEvent(st, e->gev[k], 0));
+    return CLBM_OK;
 }
 
 // Device descriptors for tile width bx; returns the number of bulk tiles.
@@ -1158,9 +1188,10 @@ int ens_tune(clbm_ensemble* e) {
     for (int R : cand_r) {
         if (int rc = ens_groups(e, R)) return rc;
         if (e->groups.empty()) break;
-        ens_bulk_rows(e, true, e->st);
+        if (int rc = ens_bulk_rows(e, true, e->st)) return rc;
         CK(cudaEventRecord(e0, e->st));
-        for (int k = 0; k < 3; ++k) ens_bulk_rows(e, true, e->st);
+        for (int k = 0; k < 3; ++k)
+            if (int rc = ens_bulk_rows(e, true, e->st)) return rc;
         CK(cudaEventRecord(e1, e->st));
         CK(cudaEventSynchronize(e1));
         CK_LAUNCH();
@@ -1194,8 +1225,9 @@ int ens_step(clbm_ensemble* e) {
     launch_ens_interp_spread(e->d_desc, e->n, e->max_spread_blocks, e->st);
     launch_ens_finish(e->d_desc, e->n, e->st);
     CK(cudaStreamWaitEvent(e->st2, e->ev_box, 0));
-    if (e->rows) ens_bulk_rows(e, pull, e->st2);
-    else launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
+    if (e->rows) {
+        if (int rc = ens_bulk_rows(e, pull, e->st2)) return rc;
+    } else launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
                          e->grid, e->st2);
     CK(cudaEventRecord(e->ev_bulk, e->st2));
     launch_ens_box_flat(e->storage, pull, e->d_desc, e->n, off_new, e->cur, e->flat_grid, e->st);
@@ -1380,6 +1412,8 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     ens_free_graph(e);
     if (e->d_desc) cudaFree(e->d_desc);
     ens_free_groups(e);
+    for (cudaStream_t st : e->gst) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : e->gev) cudaEventDestroy(ev);
     if (e->d_tile0) cudaFree(e->d_tile0);
     if (e->d_off) cudaFree(e->d_off);
     cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};
