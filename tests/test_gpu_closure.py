@@ -47,7 +47,10 @@ def test_loss_and_gradient_match_oracle(built_pkg, oracle_mod, mode):
     net = built_pkg.closure.ClosureNet(p)
     loss = tr.loss(net, 0, len(sm), wscale)
     ref_loss = oracle_mod.closure_loss_grad(p, back.astype(np.float64), wscale, grad=False) / len(sm)
-    assert loss == pytest.approx(ref_loss, rel=2e-3)
+    # the oracle rounds the tensor-core operands to bf16 as the kernels do; what remains is
+    # the hardware tanh approximation and the order of the float32 sums (measured: loss
+    # within 1e-6, gradient blocks within 7.1e-4)
+    assert loss == pytest.approx(ref_loss, rel=2e-5)
     g, loss_g = tr.grad(net, 0, len(sm), wscale)
     assert loss_g == pytest.approx(loss, rel=1e-6)
     _, ref_g = oracle_mod.closure_loss_grad(p, back.astype(np.float64), wscale)
@@ -61,7 +64,7 @@ def test_loss_and_gradient_match_oracle(built_pkg, oracle_mod, mode):
     print(f"mode {mode}: loss rel {abs(loss - ref_loss) / abs(ref_loss):.2e}, gradient rel L2 "
           + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
     for k, v in errs.items():
-        assert v < 3e-2, (k, v)
+        assert v < 3e-3, (k, v)
     np.testing.assert_array_equal(g[:1024].reshape(32, 32)[:, 19:], 0.0)
     tr.close()
 
