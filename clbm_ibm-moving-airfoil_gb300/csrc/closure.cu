@@ -15,6 +15,8 @@
 // tensor memory, M = 128 rows = one cell or sample per thread of a 128-thread block).
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
 
 #include "closure_device.cuh"
 
@@ -39,13 +41,42 @@ void launch_closure_images(const float* params, uint16_t* img, cudaStream_t st) 
 namespace {
 
 constexpr uint32_t kIdescFwd = tc::idesc_bf16(128, 32);
+constexpr uint32_t kIdescF16 = tc::idesc_f16(128, 32);
 
 // Issue D = A (128 x 32, K-major) * B^T (32 x 32) as two K = 16 MMAs; commit to `bar`
 // (the completion of every MMA this thread issued so far) unless it is null.
-__device__ __forceinline__ void mma_k32(uint32_t tmem, uint32_t a, uint32_t b, uint64_t* bar) {
-    tc::mma(tmem, tc::smem_desc(a, 128, 512), tc::smem_desc(b, 128, 512), kIdescFwd, false);
-    tc::mma(tmem, tc::smem_desc(a + 256, 128, 512), tc::smem_desc(b + 256, 128, 512), kIdescFwd, true);
+__device__ __forceinline__ void mma_k32(uint32_t tmem, uint32_t a, uint32_t b, uint64_t* bar,
+                                        uint32_t idesc = kIdescFwd) {
+    tc::mma(tmem, tc::smem_desc(a, 128, 512), tc::smem_desc(b, 128, 512), idesc, false);
+    tc::mma(tmem, tc::smem_desc(a + 256, 128, 512), tc::smem_desc(b + 256, 128, 512), idesc, true);
     if (bar) tc::commit(bar);
+}
+
+// 16-bit bits of x in the storage form's own type (FP16 or BF16); exact for the stored
+// deviations, which already are values of that type.
+template <int S>
+__device__ __forceinline__ uint16_t store_bits(float x) {
+    if constexpr (S == CLBM_STORE_F16S) return __half_as_ushort(__float2half_rn(x));
+    else return __bfloat16_as_ushort(__float2bfloat16_rn(x));
+}
+
+// Row `row` of a K-major tile with 32 columns: the 19 values in the storage form's type,
+// zeros after them.
+template <int S>
+__device__ __forceinline__ void put_row19_store(unsigned char* tile, int row, const float (&v)[19]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t wv[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int k = 8 * j + 2 * t;
+            const uint32_t lo = k < 19 ? store_bits<S>(v[k < 19 ? k : 0]) : 0u;
+            const uint32_t hi = k + 1 < 19 ? store_bits<S>(v[k + 1 < 19 ? k + 1 : 0]) : 0u;
+            wv[t] = lo | (hi << 16);
+        }
+        *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(row, 8 * j, 32)) =
+            make_uint4(wv[0], wv[1], wv[2], wv[3]);
+    }
 }
 
 // Block-wide barrier that also orders tensor-core work around it.
@@ -65,26 +96,40 @@ __device__ __forceinline__ void tc_sync() {
 // layer on the CUDA cores, collision with s_h, store. Cells of the IBM force box (SkipBand)
 // are left to the box pass, which uses the plain collision with forcing; the inlet and
 // outlet columns (x = 0, nx - 1) keep the plain rates.
-template <int S, bool PULL, int FMODE, bool IDX32>
+// FMMA (16-bit forms): the raw moments of the features come from one more MMA per tile,
+// D = H M_raw^T with H the 128 cells' 19 stored deviations (exact in the storage type, FP16
+// or BF16) and M_raw's entries 0, +-1 (exact), FP32 accumulation; the binomial shift to
+// central moments (per-cell velocity) stays on the CUDA cores.
+template <int S, bool PULL, int FMODE, bool IDX32, bool FMMA>
 __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typename Pop<S>::T* __restrict__ fin,
                                                                 typename Pop<S>::T* __restrict__ fout,
                                                                 Grid g, Coef c, ForceArgs fa,
                                                                 ClosureArgs ca) {
     constexpr bool DEV = Pop<S>::kShifted;
+    static_assert(!FMMA || DEV, "the feature MMA takes the 16-bit stored deviations");
     __shared__ __align__(1024) unsigned char sA[128 * 32 * 2];
-    __shared__ __align__(1024) unsigned char sW[2 * 32 * 32 * 2];
+    __shared__ __align__(1024) unsigned char sW[(FMMA ? 3 : 2) * 32 * 32 * 2];
     __shared__ NetSmem net;
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int i = tid; i < (2 * 32 * 32 * 2) / 16; i += 128)
         reinterpret_cast<uint4*>(sW)[i] = reinterpret_cast<const uint4*>(ca.img)[i];
+    if (FMMA) {
+        // B of the feature MMA: M_raw as [moment][population], 32 x 32, K-major
+        for (int e = tid; e < 32 * 32; e += 128) {
+            const int n = e >> 5, k = e & 31;
+            const int v = (n < kIn && k < 19) ? mraw_entry(n, k) : 0;
+            *reinterpret_cast<uint16_t*>(sW + 4096 + tc::kmajor_offset(n, k, 32)) =
+                v == 0 ? (uint16_t)0 : store_bits<S>((float)v);
+        }
+    }
     load_net(ca.params, net, tid, 128);
     if (warp == 0) tc::alloc(&tbase, 32);
     if (tid == 0) tc::bar_init(&bar, 1);
     tc_sync();
     const uint32_t tm = tbase;
-    const uint32_t aA = tc::smem_addr(sA), aW1 = tc::smem_addr(sW), aW2 = aW1 + 2048;
+    const uint32_t aA = tc::smem_addr(sA), aW1 = tc::smem_addr(sW), aW2 = aW1 + 2048, aM = aW1 + 4096;
     const float nu = (1.0f / (1.0f - c.one_m_sv) - 0.5f) * (1.0f / 3.0f);  // solver viscosity
     uint32_t phase = 0;
     bool ok = true;
@@ -110,7 +155,39 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
         }
         float f[19];
         float v[32];
-        if (use) {
+        bool w = true;
+        if (FMMA) {
+            if (use) {
+                gather<S, PULL, true, IDX32>(fin, g, c, x, y, z, f);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 19; ++q) f[q] = 0.0f;
+            }
+            put_row19_store<S>(sA, tid, f);
+            tc_sync();
+            if (tid == 0) {
+                mma_k32(tm, aA, aM, &bar, S == CLBM_STORE_F16S ? kIdescF16 : kIdescFwd);
+                w = tc::bar_wait(&bar, phase, g.spin_limit);
+            }
+            ok = !__syncthreads_or(!w);
+            phase ^= 1;
+            if (!ok) break;
+            tc::fence_after();
+            tc::ld32(tc::lane_addr(tm, warp, 0), v);
+            if (use) {
+                CMom m;
+                moments_from_mraw(v, m);
+                standardise(m, net, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = 0.0f;
+            }
+            // every thread has read its row of the feature result before the A tile and
+            // the accumulator are reused
+            tc::fence_before();
+            __syncthreads();
+            tc::fence_after();
+        } else if (use) {
             gather<S, PULL, true, IDX32>(fin, g, c, x, y, z, f);
             CMom m;
             moments_full<DEV>(f, m);
@@ -122,7 +199,6 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
         put_row32(sA, tid, v);
         tc_sync();
         // one thread issues the MMAs and waits for them; the barrier releases the block
-        bool w = true;
         if (tid == 0) {
             mma_k32(tm, aA, aW1, &bar);
             w = tc::bar_wait(&bar, phase, g.spin_limit);
@@ -194,21 +270,41 @@ __global__ void __launch_bounds__(128, 8) k_closure_stream_collide(const typenam
         default: { constexpr int S_ = CLBM_STORE_BF16S; __VA_ARGS__; } break;               \
     }
 
-template <int S, bool PULL>
-static void closure_sc(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
-                       const ForceArgs& fa, const ClosureArgs& ca, int grid, cudaStream_t st) {
+// Feature path of the fused closure pass (16-bit forms): CLBM_CLOSURE_FEATURES=mma takes
+// the raw moments from the tensor cores, =cores (default) from the CUDA cores.
+static bool closure_features_mma(int storage) {
+    if (storage == CLBM_STORE_F32) return false;
+    const char* e = std::getenv("CLBM_CLOSURE_FEATURES");   // read at every launch
+    return e && !std::strcmp(e, "mma");
+}
+
+template <int S, bool PULL, bool FMMA>
+static void closure_sc_f(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                         const ForceArgs& fa, const ClosureArgs& ca, int grid, cudaStream_t st) {
     using T = typename Pop<S>::T;
     if (19LL * g.plane <= 0xffffffffLL) {   // every element index fits 32 bits
         if (fmode == kForceSkipBand)
-            k_closure_stream_collide<S, PULL, kForceSkipBand, true><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+            k_closure_stream_collide<S, PULL, kForceSkipBand, true, FMMA><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
         else
-            k_closure_stream_collide<S, PULL, kForceNone, true><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+            k_closure_stream_collide<S, PULL, kForceNone, true, FMMA><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
         return;
     }
     if (fmode == kForceSkipBand)
-        k_closure_stream_collide<S, PULL, kForceSkipBand, false><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        k_closure_stream_collide<S, PULL, kForceSkipBand, false, FMMA><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
     else
-        k_closure_stream_collide<S, PULL, kForceNone, false><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+        k_closure_stream_collide<S, PULL, kForceNone, false, FMMA><<<grid, 128, 0, st>>>((const T*)fin, (T*)fout, g, c, fa, ca);
+}
+
+template <int S, bool PULL>
+static void closure_sc(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                       const ForceArgs& fa, const ClosureArgs& ca, int grid, cudaStream_t st) {
+    if constexpr (S != CLBM_STORE_F32) {
+        if (closure_features_mma(S)) {
+            closure_sc_f<S, PULL, true>(fmode, fin, fout, g, c, fa, ca, grid, st);
+            return;
+        }
+    }
+    closure_sc_f<S, PULL, false>(fmode, fin, fout, g, c, fa, ca, grid, st);
 }
 
 // Persistent grid: the blocks that fit on an SM by registers (65,536 per SM) and by
@@ -219,8 +315,13 @@ int closure_grid(int storage) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncAttributes fa{};
     CLBM_CL_STORE(storage, {
-        if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand, true>) == cudaSuccess)
-            regs = fa.numRegs;
+        int r0 = 0, r1 = 0;
+        if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand, true, false>) == cudaSuccess)
+            r0 = fa.numRegs;
+        if constexpr (S_ != CLBM_STORE_F32)
+            if (cudaFuncGetAttributes(&fa, k_closure_stream_collide<S_, true, kForceSkipBand, true, true>) == cudaSuccess)
+                r1 = fa.numRegs;
+        regs = std::max(r0, r1);
     });
     cudaGetLastError();
     const int per_regs = regs > 0 ? 65536 / (128 * ((regs + 7) / 8 * 8)) : 4;

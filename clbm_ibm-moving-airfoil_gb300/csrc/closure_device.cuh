@@ -237,6 +237,51 @@ __device__ __forceinline__ void load_net(const float* __restrict__ p, NetSmem& n
     }
 }
 
+// Moment orders (p, q, r) of the raw-moment set M_raw, in its row order
+// (config_moving.py:62-68).
+// (each order packed as 2 bits: p | q << 2 | r << 4)
+__host__ __device__ constexpr int pqr_code(int i) {
+    return i == 0 ? 0x00 : i == 1 ? 0x01 : i == 2 ? 0x04 : i == 3 ? 0x10 : i == 4 ? 0x05
+         : i == 5 ? 0x11 : i == 6 ? 0x14 : i == 7 ? 0x02 : i == 8 ? 0x08 : i == 9 ? 0x20
+         : i == 10 ? 0x06 : i == 11 ? 0x09 : i == 12 ? 0x12 : i == 13 ? 0x18 : i == 14 ? 0x21
+         : i == 15 ? 0x24 : i == 16 ? 0x0A : i == 17 ? 0x22 : 0x28;
+}
+
+// Entry (moment i, population q) of M_raw: e_x^p e_y^q e_z^r, one of 0, +1, -1.
+__device__ __forceinline__ int mraw_entry(int i, int q) {
+    const int e[3] = {ex(q), ey(q), ez(q)};
+    const int code = pqr_code(i);
+    int v = 1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < ((code >> (2 * a)) & 3); ++k) v *= e[a];
+    return v;
+}
+
+// Raw moments of the stored deviations in the M_raw order (as the tensor cores return them:
+// m_i = sum_q M_raw[i][q] h_q) turned into the cell's moments about its own velocity, the
+// same arithmetic as moments_full<DEV = true> from there on.
+__device__ __forceinline__ void moments_from_mraw(const float (&m)[32], CMom& c) {
+    Raw r;
+    r.R0.x = m[0];
+    r.mx.x = m[1]; r.my.x = m[2]; r.mz.x = m[3];
+    r.pxy.x = m[4]; r.pxz.x = m[5]; r.pyz.x = m[6];
+    r.Pxx.x = m[7]; r.Pyy.x = m[8]; r.Pzz.x = m[9];
+    r.M210.x = m[10]; r.M120.x = m[11]; r.M201.x = m[12];
+    r.M021.x = m[13]; r.M102.x = m[14]; r.M012.x = m[15];
+    r.A220.x = m[16]; r.A202.x = m[17]; r.A022.x = m[18];
+    r.r.x = m[0] + 1.0f;
+    r.Mxx.x = m[7] + 1.0f / 3.0f;
+    r.Myy.x = m[8] + 1.0f / 3.0f;
+    r.Mzz.x = m[9] + 1.0f / 3.0f;
+    const float inv = 1.0f / r.r.x;
+    c.r = r.r.x;
+    c.u = r.mx.x * inv;
+    c.v = r.my.x * inv;
+    c.w = r.mz.x * inv;
+    central_moments(r, c.u, c.v, c.w, r.r.x, c.x);
+}
+
 // Standardised features of a cell, padded to 32 with zeros.
 __device__ __forceinline__ void standardise(const CMom& m, const NetSmem& n, float (&xs)[32]) {
 #pragma unroll

@@ -99,7 +99,14 @@ def _perturbed(shape, rng, u=0.04):
 
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("storage,tol", [("f32", 2e-3), ("f16", 5e-3)])
-def test_closure_solver_matches_oracle(built_pkg, oracle_mod, storage, tol, mode):
+@pytest.mark.parametrize("features", ["cores", "mma"])
+def test_closure_solver_matches_oracle(built_pkg, oracle_mod, monkeypatch, storage, tol, mode,
+                                       features):
+    """features = mma: the raw moments of the 16-bit stored deviations from one more
+    tensor-core MMA per tile (FP16 operands, FP32 accumulation)."""
+    if features == "mma" and storage == "f32":
+        pytest.skip("the feature MMA takes the 16-bit stored deviations")
+    monkeypatch.setenv("CLBM_CLOSURE_FEATURES", features)
     rng = np.random.default_rng(31)
     shape = (40, 12, 6)
     p = random_params(rng, span=0.9 if mode == 0 else 1.5, mode=mode)
