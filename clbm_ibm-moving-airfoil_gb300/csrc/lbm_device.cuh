@@ -857,7 +857,8 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
 // One cell of the full-grid pass: gather, force (per FMODE), collide, store.
 // kForceOnlyBand (box pass): only a cell inside the force box is collided and stored; with
 // ks, its clipped force in units of 2^-40 is added to ks[0], ks[1] (exact).
-template <int S, bool PULL, int FMODE>
+// IDX32: element indices in 32-bit unsigned arithmetic (valid while 19 * plane < 2^32).
+template <int S, bool PULL, int FMODE, bool IDX32 = false>
 __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __restrict__ fin,
                                                     typename Pop<S>::T* __restrict__ fout,
                                                     const Grid& g, const Coef& c,
@@ -866,7 +867,7 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
     // shifted storage: the collision works on the deviations (no per-population shift)
     constexpr bool DEV = Pop<S>::kShifted;
     float f[19];
-    gather<S, PULL, true>(fin, g, c, x, y, z, f);
+    gather<S, PULL, true, IDX32>(fin, g, c, x, y, z, f);
     if (FMODE == kForceSkipBand) {
         // bulk pass of an IBM step: the cells of the force box are done by the box pass.
         // Tested after the gather, so the box read does not delay the population loads.
@@ -896,7 +897,7 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
             collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
         }
     }
-    store_raw<S>(fout, g, cell, f);
+    store_raw<S, IDX32>(fout, g, cell, f);
 }
 
 // Forced stream-collide of box cell t of band b (the box pass, one cell). SUMS: also add

@@ -26,13 +26,13 @@ namespace clbm {
 
 constexpr int kBX = 128;  // threads per block along x
 
-template <int S, bool PULL, int FMODE>
+template <int S, bool PULL, int FMODE, bool IDX32>
 __global__ void __launch_bounds__(kBX) k_stream_collide(const typename Pop<S>::T* __restrict__ fin,
                                                         typename Pop<S>::T* __restrict__ fout,
                                                         Grid g, Coef c, ForceArgs fa) {
     const int x = blockIdx.x * kBX + threadIdx.x;
     if (x >= g.nx) return;
-    stream_collide_cell<S, PULL, FMODE>(fin, fout, g, c, fa, x, blockIdx.y, blockIdx.z);
+    stream_collide_cell<S, PULL, FMODE, IDX32>(fin, fout, g, c, fa, x, blockIdx.y, blockIdx.z);
 }
 
 // Forced pass over the cells of the IBM force box (the complement of the bulk pass), by
@@ -568,10 +568,23 @@ static void tma_launch(const void* fin, void* fout, const Grid& g, const Coef& c
     k_stream_collide_tma<S, PULL, FMODE><<<grid, g.seg / 2, smem, st>>>((const T*)fin, (T*)fout, g, c, fa);
 }
 
+template <int S, bool PULL, bool IDX32>
+static void cell_launch(int fmode, const void* fin, void* fout, const Grid& g, const Coef& c,
+                        const ForceArgs& fa, cudaStream_t st) {
+    using T = typename Pop<S>::T;
+    if (fmode == kForceNone)
+        k_stream_collide<S, PULL, kForceNone, IDX32><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceBand)
+        k_stream_collide<S, PULL, kForceBand, IDX32><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else if (fmode == kForceSkipBand)
+        k_stream_collide<S, PULL, kForceSkipBand, IDX32><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    else
+        k_stream_collide<S, PULL, kForceDense, IDX32><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+}
+
 template <int S, bool PULL>
 static void sc_launch(int fmode, int variant, const void* fin, void* fout, const Grid& g,
                       const Coef& c, const ForceArgs& fa, cudaStream_t st) {
-    using T = typename Pop<S>::T;
     if (variant == kVariantStaged) {
         if (fmode == kForceNone) tma_launch<S, PULL, kForceNone>(fin, fout, g, c, fa, st);
         else if (fmode == kForceBand) tma_launch<S, PULL, kForceBand>(fin, fout, g, c, fa, st);
@@ -584,14 +597,9 @@ static void sc_launch(int fmode, int variant, const void* fin, void* fout, const
         else pair_launch<S, PULL, 128>(fmode, fin, fout, g, c, fa, st);
         return;
     }
-    if (fmode == kForceNone)
-        k_stream_collide<S, PULL, kForceNone><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-    else if (fmode == kForceBand)
-        k_stream_collide<S, PULL, kForceBand><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-    else if (fmode == kForceSkipBand)
-        k_stream_collide<S, PULL, kForceSkipBand><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
-    else
-        k_stream_collide<S, PULL, kForceDense><<<cell_grid(g), kBX, 0, st>>>((const T*)fin, (T*)fout, g, c, fa);
+    // 32-bit element indices while every index of the 19 planes fits
+    if (19LL * g.plane <= 0xffffffffLL) cell_launch<S, PULL, true>(fmode, fin, fout, g, c, fa, st);
+    else cell_launch<S, PULL, false>(fmode, fin, fout, g, c, fa, st);
 }
 
 void launch_stream_collide(int storage, bool pull, int fmode, int variant, const void* fin,
