@@ -334,3 +334,37 @@ def test_float32_long_run_against_fp64_oracle(gpkg, oracle_mod):
     e_f = rel_l2(hist, ref_hist)
     print(f"1000 steps: rel L2 rho {e_rho:.2e}, u {e_u:.2e}, force history {e_f:.2e}")
     assert e_rho < 1e-5 and e_u < 1e-5 and e_f < 1e-4
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-5), ("f16", 2e-3), ("bf16", 2e-2)])
+def test_force_box_at_the_outlet_on_an_odd_lattice(gpkg, oracle_mod, storage, tol):
+    """A wing whose stencils reach the outlet column of a lattice with odd Nx (61): the force
+    box's rows start at odd and even x, the box pass's last cell pair is the single outlet
+    cell, and the bulk and box passes must still cover every cell once. Float32 against the
+    float32 oracle (rho, u within 1e-5, force history within 1e-4); the 16-bit forms against
+    the FP64 oracle within the shifted-storage tolerances."""
+    from dataclasses import replace
+    cfg = replace(gpkg.wing_case(61, 40, 6, 16, storage=storage, name="wing-61x40x6-outlet"),
+                  x0=61.0 - 0.75 * 16.0 - 1.0)
+    steps = 100
+    sim = gpkg.Simulation(cfg)
+    sim.run(steps)
+    got = sim.solver.read_macro()
+    hist = sim.ibm.force_history(steps)
+    box = sim.ibm.read_markers()
+    sim.close()
+    assert box["X"].max() > cfg.nx - 3   # the stencils reach the outlet column
+    ref = oracle_mod.Oracle(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                            cfg.X0, cfg.Y0, cfg.Z0, real="f32" if storage == "f32" else "f64")
+    ref_hist = ref.run(0, steps, cfg.motion())
+    rho, ux, uy, uz = ref.macro()
+    ref.close()
+    e_rho = rel_l2(got["rho"] - 1.0, rho - 1.0) if storage != "f32" else rel_l2(got["rho"], rho)
+    e_u = rel_l2(np.stack([got["ux"], got["uy"], got["uz"]]), np.stack([ux, uy, uz]))
+    e_f = rel_l2(hist, ref_hist)
+    print(f"{storage} odd lattice, box at the outlet: rho {e_rho:.2e}, u {e_u:.2e}, "
+          f"force history {e_f:.2e}")
+    if storage == "f32":
+        assert e_rho <= 1e-5 and e_u <= 1e-5 and e_f <= 1e-4
+    else:
+        assert e_u < tol and e_f < 10 * tol
