@@ -1283,7 +1283,7 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         e->m.push_back(motions[i]);
         clbm_ibm* b = e->ibm.back();
         if (b) {
-            e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + kMarkerBlock - 1) / kMarkerBlock);
+            e->max_marker_blocks = std::max(e->max_marker_blocks, (b->a.n + kEnsMarkerBlock - 1) / kEnsMarkerBlock);
             const long long warps = ((long long)b->a.n + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp;
             e->max_spread_blocks = std::max(e->max_spread_blocks,
                                             (int)((warps * 32 + kSpreadBlock - 1) / kSpreadBlock));

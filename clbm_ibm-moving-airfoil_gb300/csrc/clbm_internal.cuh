@@ -352,6 +352,9 @@ constexpr int kSpreadMarkersPerWarp = 2;   // markers interpolated and spread by
 // band-prepare, spreading and box-pass kernels therefore use blocks of 64 threads (the
 // 16-bit box pass with at most 64 registers).
 constexpr int kMarkerBlock = 64;
+// The batched marker kernel runs before the ensemble's bulk pass, not beside it: larger
+// blocks there (fewer block reductions, box atomics and last-block tickets per member).
+constexpr int kEnsMarkerBlock = 256;
 constexpr int kBoxBlock = 64;      // band-prepare and box pass of the single lattice
 constexpr int kSpreadBlock = 64;
 constexpr int kTiledBlock = 256;   // shared-memory tiled spreading: 8 warps per tile

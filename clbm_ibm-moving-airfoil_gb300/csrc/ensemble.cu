@@ -19,10 +19,10 @@
 
 namespace clbm {
 
-__global__ void __launch_bounds__(kMarkerBlock) kb_markers(const EnsDesc* __restrict__ d) {
+__global__ void __launch_bounds__(kEnsMarkerBlock) kb_markers(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
-    if (!D.has_ibm || (int)blockIdx.x * kMarkerBlock >= D.a.n) return;  // whole block
-    ibm_markers_body<true>(D.a, D.g, MotionF{}, D.m, blockIdx.x);
+    if (!D.has_ibm || (int)blockIdx.x * kEnsMarkerBlock >= D.a.n) return;  // whole block
+    ibm_markers_body<true, kEnsMarkerBlock>(D.a, D.g, MotionF{}, D.m, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kSpreadBlock) kb_interp_spread(const EnsDesc* __restrict__ d) {
@@ -296,7 +296,7 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
 
 void launch_ens_markers(const EnsDesc* d, int n, int blocks, cudaStream_t st) {
     if (blocks < 1) return;
-    kb_markers<<<dim3(blocks, n), kMarkerBlock, 0, st>>>(d);
+    kb_markers<<<dim3(blocks, n), kEnsMarkerBlock, 0, st>>>(d);
 }
 
 void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t st) {

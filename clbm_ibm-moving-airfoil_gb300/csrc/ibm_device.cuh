@@ -9,12 +9,13 @@
 namespace clbm {
 
 
-// Marker kinematics (airfoil_moving.py:100-127) of markers [bx * 256, bx * 256 + 256) and
-// the box that bounds their 4x4x4 Peskin stencils (block min, one atomicMin per entry).
-template <bool DEVM>
+// Marker kinematics (airfoil_moving.py:100-127) of markers [bx * B, bx * B + B), B threads
+// per block, and the box that bounds their 4x4x4 Peskin stencils (block min, one
+// atomicMin per entry).
+template <bool DEVM, int B = kMarkerBlock>
 __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid& g,
                                                  const MotionF& mf, const clbm_motion& m, int bx) {
-    __shared__ int sbox[kMarkerBlock / 32][6];
+    __shared__ int sbox[B / 32][6];
     __shared__ float smot[8];
     const long long s = a.dev->step + 1;
     if (threadIdx.x == 0) {
@@ -41,7 +42,7 @@ __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid&
     const float xc = smot[0], yc = smot[1], vx = smot[3], vy = smot[4], omega = smot[5];
     const float cos_t = smot[6], sin_t = smot[7];
     int b[6] = {kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty, kBoxEmpty};
-    const int i = bx * kMarkerBlock + threadIdx.x;
+    const int i = bx * B + threadIdx.x;
     if (i < a.n) {
         const float x0m = a.X0[i], y0m = a.Y0[i], zk = a.Z0[i];
         const float xk = xc + x0m * cos_t - y0m * sin_t;
@@ -68,7 +69,7 @@ __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid&
     __syncthreads();
     if (threadIdx.x < 6) {
         int v = sbox[0][threadIdx.x];
-        for (int w = 1; w < kMarkerBlock / 32; ++w) v = min(v, sbox[w][threadIdx.x]);
+        for (int w = 1; w < B / 32; ++w) v = min(v, sbox[w][threadIdx.x]);
         if (v != kBoxEmpty) atomicMin(&a.dev->box[s & 1][threadIdx.x], v);
         __threadfence();
     }
@@ -76,7 +77,7 @@ __device__ __forceinline__ void ibm_markers_body(const IbmArrays& a, const Grid&
     __shared__ bool last;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned int nbx = (unsigned int)((a.n + kMarkerBlock - 1) / kMarkerBlock);
+        const unsigned int nbx = (unsigned int)((a.n + B - 1) / B);
         last = atomicAdd(&a.dev->mticket, 1u) == nbx - 1;
     }
     __syncthreads();
