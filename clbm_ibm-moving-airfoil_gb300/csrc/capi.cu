@@ -1293,7 +1293,7 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e->flat_grid = 4 * std::max(sms, 1);
+        e->flat_grid = 16 * std::max(sms, 1);   // blocks of kBoxBlock threads
     }
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);

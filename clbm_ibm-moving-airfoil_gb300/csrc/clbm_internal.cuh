@@ -399,7 +399,7 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
                           const EnsDesc* d, const long long* tile0, int n, long long ntiles,
                           int parity, int grid, cudaStream_t st);
 // Force-box cells of all members as one flat list (offsets per member, n + 1 each), then
-// band-prepare and box pass over it with `grid` blocks of 256 threads.
+// band-prepare and box pass over it with `grid` blocks of kBoxBlock threads.
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st);
 void launch_ens_band_prepare_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new,
                                   const long long* off_old, int parity, bool compute_macro, int grid,

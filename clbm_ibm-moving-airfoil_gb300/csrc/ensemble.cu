@@ -93,7 +93,7 @@ __device__ __forceinline__ int member_of(const long long* __restrict__ off, int 
 }
 
 template <int S, bool PULL>
-__global__ void __launch_bounds__(256) kb_band_prepare_flat(const EnsDesc* __restrict__ d, int n,
+__global__ void __launch_bounds__(kBoxBlock) kb_band_prepare_flat(const EnsDesc* __restrict__ d, int n,
                                                             const long long* __restrict__ off_new,
                                                             const long long* __restrict__ off_old,
                                                             int parity, bool compute_macro) {
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) kb_band_prepare_flat(const EnsDesc* __res
 }
 
 template <int S, bool PULL>
-__global__ void __launch_bounds__(256) kb_box_flat(const EnsDesc* __restrict__ d, int n,
+__global__ void __launch_bounds__(kBoxBlock) kb_box_flat(const EnsDesc* __restrict__ d, int n,
                                                    const long long* __restrict__ off_new, int parity) {
     using T = typename Pop<S>::T;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -325,16 +325,16 @@ void launch_ens_band_prepare_flat(int storage, bool pull, const EnsDesc* d, int 
                                   const long long* off_old, int parity, bool compute_macro, int grid,
                                   cudaStream_t st) {
     CLBM_ENS_STORE(storage, {
-        if (pull) kb_band_prepare_flat<S_, true><<<grid, 256, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
-        else kb_band_prepare_flat<S_, false><<<grid, 256, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
+        if (pull) kb_band_prepare_flat<S_, true><<<grid, kBoxBlock, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
+        else kb_band_prepare_flat<S_, false><<<grid, kBoxBlock, 0, st>>>(d, n, off_new, off_old, parity, compute_macro);
     });
 }
 
 void launch_ens_box_flat(int storage, bool pull, const EnsDesc* d, int n, const long long* off_new, int parity,
                          int grid, cudaStream_t st) {
     CLBM_ENS_STORE(storage, {
-        if (pull) kb_box_flat<S_, true><<<grid, 256, 0, st>>>(d, n, off_new, parity);
-        else kb_box_flat<S_, false><<<grid, 256, 0, st>>>(d, n, off_new, parity);
+        if (pull) kb_box_flat<S_, true><<<grid, kBoxBlock, 0, st>>>(d, n, off_new, parity);
+        else kb_box_flat<S_, false><<<grid, kBoxBlock, 0, st>>>(d, n, off_new, parity);
     });
 }
 
