@@ -38,10 +38,10 @@ __global__ void __launch_bounds__(kTiledBlock) kb_interp_spread_tiled(const EnsD
     ibm_interp_spread_tiled_body(D.a, D.g, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(kFinishBlock) kb_finish(const EnsDesc* __restrict__ d) {
+__global__ void __launch_bounds__(kBoxBlock) kb_finish(const EnsDesc* __restrict__ d) {
     const EnsDesc& D = d[blockIdx.y];
     if (!D.has_ibm) return;
-    ibm_finish_body(D.a, D.g, blockIdx.x, gridDim.x);
+    ibm_finish_body<kBoxBlock>(D.a, D.g, blockIdx.x, gridDim.x);
 }
 
 // Force boxes of all members as one flat list: off_new[i] (off_old[i]) is the first flat
@@ -312,9 +312,9 @@ void launch_ens_interp_spread(const EnsDesc* d, int n, int blocks, cudaStream_t 
 }
 
 void launch_ens_finish(const EnsDesc* d, int n, cudaStream_t st) {
-    // a quarter of the single-lattice blocks per member: the members' boxes are small and
-    // the blocks of all members fill the GPU (fewer block reductions)
-    kb_finish<<<dim3(kFinishBlocks / 4, n), kFinishBlock, 0, st>>>(d);
+    // 64-thread blocks (they run beside the bulk pass, whose blocks free room for them one
+    // at a time), kFinishBlocks per member: the same threads per member as 16 blocks of 256
+    kb_finish<<<dim3(kFinishBlocks, n), kBoxBlock, 0, st>>>(d);
 }
 
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st) {

@@ -301,14 +301,15 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Double sums of the clipped Eulerian force over the box and of the marker forces into the
 // history ring, then the device call counter advances. Block bx of nbx writes its partial;
 // the last block to finish sums the partials in block order (scheduling-independent).
+template <int B = kFinishBlock>
 __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& g, int bx, int nbx) {
-    __shared__ double red[kFinishBlock / 32][4];
+    __shared__ double red[B / 32][4];
     __shared__ bool last;
     IbmDev* dev = a.dev;
     const long long s = dev->step + 1;
     const Band b = load_band(dev, (int)(s & 1));
     const int cells = b.ilen * b.jlen * b.klen;
-    const int stride = nbx * kFinishBlock;
+    const int stride = nbx * B;
     // Every clipped Eulerian value is an integer multiple of 2^-40 (a float of the int64
     // field times 2^-40, or the float 0.05f = 13421773 * 2^-28) of magnitude <= 0.05. The
     // integers k = value * 2^40 are summed exactly in int64 and converted once: the exact
@@ -317,14 +318,14 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     // the slow double-precision adds of this part to one per block.
     long long kx = 0, ky = 0;
     double mx = 0.0, my = 0.0;
-    for (int t = bx * kFinishBlock + threadIdx.x; t < cells; t += stride) {
+    for (int t = bx * B + threadIdx.x; t < cells; t += stride) {
         int x, y, z;
         box_cell(b, g.ny, g.nz, t, x, y, z);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
         kx += (long long)(fminf(fmaxf(qforce(a.fx[c]), -0.05f), 0.05f) * kForceScale);
         ky += (long long)(fminf(fmaxf(qforce(a.fy[c]), -0.05f), 0.05f) * kForceScale);
     }
-    for (int t = bx * kFinishBlock + threadIdx.x; t < a.n; t += stride) {
+    for (int t = bx * B + threadIdx.x; t < a.n; t += stride) {
         mx += (double)a.FXk[t];
         my += (double)a.FYk[t];
     }
@@ -340,7 +341,7 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     __syncthreads();
     if (threadIdx.x < 4) {
         double v = 0.0;
-        for (int w = 0; w < kFinishBlock / 32; ++w) v += red[w][threadIdx.x];
+        for (int w = 0; w < B / 32; ++w) v += red[w][threadIdx.x];
         a.part[4 * bx + threadIdx.x] = v;
         __threadfence();
     }
@@ -353,7 +354,7 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     if (!last) return;
     __threadfence();
     double v[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int blk = threadIdx.x; blk < nbx; blk += kFinishBlock)
+    for (int blk = threadIdx.x; blk < nbx; blk += B)
         for (int e = 0; e < 4; ++e) v[e] += __ldcg(a.part + 4 * blk + e);
     for (int e = 0; e < 4; ++e) v[e] = warp_sum(v[e]);
     __syncthreads();
@@ -362,7 +363,7 @@ __device__ __forceinline__ void ibm_finish_body(const IbmArrays& a, const Grid& 
     __syncthreads();
     if (threadIdx.x < 4) {
         double t = 0.0;
-        for (int w = 0; w < kFinishBlock / 32; ++w) t += red[w][threadIdx.x];
+        for (int w = 0; w < B / 32; ++w) t += red[w][threadIdx.x];
         a.hist[4 * ((s - 1) % a.hist_cap) + threadIdx.x] = t;
     }
     if (threadIdx.x == 0) {
