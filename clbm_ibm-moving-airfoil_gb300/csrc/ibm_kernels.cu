@@ -1,21 +1,24 @@
 // ibm_kernels.cu -- direct-forcing immersed boundary on the GPU.
 //
-// One compute_force call (airfoil_moving.py:230-255) is four launches:
+// One compute_force call (airfoil_moving.py:230-255) is three launches, and the step that
+// follows completes it:
 //   k_ibm_markers        marker kinematics (airfoil_moving.py:100-127) and the box that
 //                        bounds every 4x4x4 Peskin stencil of this call (block min/max,
-//                        one atomicMin per block and entry)
+//                        one atomicMin per block and entry); the last block writes the band
 //   k_band_prepare       (lbm_kernels.cu) zero the previous call's force box
 //                        (_zero_forces, airfoil_moving.py:132-137, restricted to where
 //                        forces can be non-zero) and compute _macro_post velocities of the
 //                        current state inside this call's box
-//   k_ibm_interp_spread  one warp per marker: 64 stencil taps, two per lane, interpolation
-//                        reduced with warp shuffles (airfoil_moving.py:142-170), marker
-//                        force clip (airfoil_moving.py:175-183), spreading with float
-//                        atomics into the Eulerian fields (airfoil_moving.py:188-214)
-//   k_ibm_finish         double sums of the clipped Eulerian force over the box and of the
-//                        marker forces into the history ring (lift/drag), then advance the
-//                        device call counter. The clip itself (_clip_forces,
-//                        airfoil_moving.py:219-225) is applied where the fields are read.
+//   k_ibm_interp_spread  two markers per warp: 64 stencil taps each, two per lane,
+//                        interpolation reduced with warp shuffles (airfoil_moving.py:142-170),
+//                        marker force clip (airfoil_moving.py:175-183), spreading as exact
+//                        fixed-point reductions into the Eulerian fields
+//                        (airfoil_moving.py:188-214)
+// The step's box pass (lbm_kernels.cu, k_box_rows_*) sums the clipped Eulerian force of
+// the box and the marker forces into the history ring (lift/drag) and advances the device
+// call counter; k_ibm_finish does the same when the history is read, or another
+// compute_force comes, before that step. The clip itself (_clip_forces,
+// airfoil_moving.py:219-225) is applied where the fields are read.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>

@@ -158,9 +158,10 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
 
 /* Batched ensemble (no counterpart in the reference, which runs one case per process):
  * many independent solvers, each with its own IBM (or NULL) and motion law, stepped
- * together -- each step is six launches over all members (markers, band macro,
- * interpolation/spreading, force sums, force-box pass, and one persistent bulk
- * stream-collide over a flat tile list of every member). Members keep their buffers and
+ * together -- each step is seven launches over all members (markers, force-box offsets,
+ * band macro, interpolation/spreading, force sums, force-box pass, and the bulk
+ * stream-collide over every member's cells: one launch over a flat tile list, or one
+ * launch per row width, run concurrently). Members keep their buffers and
  * all per-member reads (clbm_read_macro, ibm_read_force_history, ...) keep working; the
  * members must be fresh or at the same step, share storage form and device, and outlive
  * the ensemble. clbm_ensemble_create times the bulk-pass tile width and block schedule
