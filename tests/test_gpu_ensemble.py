@@ -18,7 +18,7 @@ def _cases(pkg, storage, n=5, lattices=SMALL):
     return [pkg.config.ensemble_case(seed, storage=storage, lattices=lattices) for seed in range(n)]
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", ["cell", "pair"])
 @pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
