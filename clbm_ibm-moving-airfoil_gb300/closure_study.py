@@ -62,14 +62,29 @@ def _window(steps, period):
     return max(1, min(int(round(STAT_PERIODS * period)), steps // 2))
 
 
+def _divergence_stats(sim):
+    """Field statistics of a run that diverged (the check reports them with its error)."""
+    try:
+        return sim.solver.check(rho_floor=0.5)
+    except DivergedError as e:
+        return e.stats
+
+
 def _run(sim, steps, chunk, on_chunk=None):
-    """Advance in graph-replayed chunks; wall time of the stepping only (synchronised)."""
+    """Advance in graph-replayed chunks; wall time of the stepping only (synchronised).
+    A run that diverges stops in the chunk where the collisions' divergence monitor trips,
+    or at the statistics check after the chunk (density floor 0.5)."""
     done, wall = 0, 0.0
     while done < steps:
         k = min(chunk, steps - done)
         t0 = time.perf_counter()
-        sim.run(k, graph=True)
-        sim.solver.synchronize()
+        try:
+            sim.run(k, graph=True)
+            sim.solver.synchronize()
+        except DivergedError:
+            wall += time.perf_counter() - t0
+            done += k
+            return wall, done, dict(_divergence_stats(sim), step=done)
         wall += time.perf_counter() - t0
         done += k
         try:

@@ -19,6 +19,7 @@ import time
 
 import numpy as np
 
+from ._lib import DivergedError
 from .config import force_coefficients
 from .solver import Simulation
 
@@ -66,11 +67,17 @@ def run(cfg, n_steps, vis_interval, data_dir, graph=True, geometry=None, templat
     try:
         while step < n_steps:
             k = min(vis_interval - (step % vis_interval), n_steps - step)
-            sim.run(k, graph=graph)
+            tripped = False
+            try:
+                sim.run(k, graph=graph)
+            except DivergedError:
+                # the collisions' divergence monitor stopped the run (main_moving.py:143-145
+                # stops at its next vis step); the check below reports it
+                tripped = True
             if sim.ibm is not None:
                 sums.append(sim.ibm.force_history(k))
             step += k
-            if step % vis_interval:
+            if step % vis_interval and not tripped:
                 continue
             xc, yc, theta = cfg.motion_state(step)[:3]
             try:
@@ -81,6 +88,7 @@ def run(cfg, n_steps, vis_interval, data_dir, graph=True, geometry=None, templat
                                                      "rho_max": float("nan"),
                                                      "u_max": float("nan")}
                 bad = True
+            bad = bad or tripped
             now = time.perf_counter()
             rate = vis_interval / (now - last)
             last = now

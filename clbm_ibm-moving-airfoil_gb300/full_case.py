@@ -54,14 +54,21 @@ def run_form(storage, steps, chunk=2000, perturb=0.0, seed=0, log=print):
         while done < steps:
             k = min(chunk, steps - done)
             t0 = time.perf_counter()
-            sim.run(k, graph=True)
-            sim.solver.synchronize()
+            tripped = False
+            try:
+                sim.run(k, graph=True)   # the collisions' divergence monitor may stop it
+                sim.solver.synchronize()
+            except DivergedError:
+                tripped = True
             wall += time.perf_counter() - t0
             done += k
             try:
-                stats = sim.solver.check(rho_floor=0.3)
+                stats = sim.solver.check(rho_floor=0.3)   # raises after a tripped monitor
             except DivergedError as e:
                 diverged = dict(e.stats, step=done)
+                break
+            if tripped:
+                diverged = dict(stats, step=done)
                 break
         coeffs = force_coefficients(sim.ibm.force_history(done), cfg)
         fields = sim.solver.read_macro()

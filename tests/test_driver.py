@@ -78,3 +78,23 @@ def test_driver_frames_and_meta_match_oracle(built_pkg, oracle_mod, tmp_path):
     forces = np.load(os.path.join(tmp_path, "forces.npz"))
     assert forces["sums"].shape == (30, 4)
     assert rel_l2(forces["sums"], np.concatenate(hist)) < 1e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [True, False])
+def test_runs_that_diverge_are_reported_not_raised(built_pkg, tmp_path, graph):
+    """A case that diverges within a few hundred steps (64x32x4, Re 1e5, U = 0.2: s_v
+    within 2e-4 of 2; the float32 oracle's density leaves [0.3, inf) by step 150): the
+    collisions' divergence monitor stops the steps, and the output driver and the study
+    drivers report the divergence with the step it was found at, as main_moving.py:143-145
+    does, instead of raising."""
+    from importlib import import_module
+    pkg = built_pkg
+    cfg = pkg.wing_case(64, 32, 4, 8, re=1e5, u_inf=0.2, name="diverging")
+    out = pkg.driver.run(cfg, 2000, 100, str(tmp_path), graph=graph, log=lambda m: None)
+    assert out["diverged"] and out["steps"] < 2000
+    study = import_module(pkg.__name__ + ".closure_study")
+    sim = pkg.Simulation(cfg)
+    wall, done, bad = study._run(sim, 2000, 200)
+    sim.close()
+    assert bad is not None and done < 2000 and "rho_min" in bad
