@@ -102,3 +102,35 @@ def test_trace_fixtures_are_consistent():
         assert int(fix["n_frames"]) == n // int(fix["vis_interval"])
         steps = fix["meta_step"]
         assert np.array_equal(steps, np.arange(1, len(steps) + 1) * int(fix["vis_interval"]))
+
+
+def test_fish_dropin_modules_load_under_their_configuration(tmp_path, monkeypatch):
+    """fish/main_fish.py imports ``clbm_fish.CLBMSolver`` and ``ibm_fish.FishIBM``, which read
+    ``config_fish``: the drop-in modules load the clbm_moving / airfoil_moving drop-ins with
+    that module standing in for ``config_moving`` and remove the alias afterwards."""
+    import types
+    import numpy as np
+    cfg = types.ModuleType("config_fish")
+    X = np.arange(12, dtype=np.float32)
+    cfg.Nx, cfg.Ny, cfg.Nz, cfg.cs2, cfg.s_v, cfg.s_e, cfg.s_q, cfg.s_pi = 32, 16, 2, 1 / 3, 1.5, 1.0, 1.0, 1.0
+    cfg.U_inf, cfg.AoA0_deg, cfg.M_raw_inv_np = 0.05, 0.0, np.eye(19)
+    cfg.N_MARKERS_2D, cfg.N_MARKERS = 6, 12
+    cfg.X_marker_np, cfg.Y_marker_np, cfg.Z_marker_np = X, X, X
+    saved = dict(sys.modules)
+    try:
+        for name in ("clbm_fish", "ibm_fish", "config_fish", "config_moving", "_variant",
+                     "_clbm_gb300_pkg"):
+            sys.modules.pop(name, None)
+        monkeypatch.syspath_prepend(COMPAT)
+        sys.modules["config_fish"] = cfg
+        import clbm_fish
+        import ibm_fish
+        assert clbm_fish.__file__.startswith(COMPAT) and ibm_fish.__file__.startswith(COMPAT)
+        assert isinstance(clbm_fish.CLBMSolver, type) and isinstance(ibm_fish.FishIBM, type)
+        assert ibm_fish.N == 12
+        assert "config_moving" not in sys.modules
+    finally:
+        for name in list(sys.modules):
+            if name not in saved:
+                del sys.modules[name]
+        sys.modules.update(saved)

@@ -33,7 +33,7 @@ def dropin_env():
     saved = dict(sys.modules)
     path = list(sys.path)
     for name in ("taichi", "clbm_moving", "airfoil_moving", "config_moving", "config_highRe",
-                 "_clbm_gb300_pkg"):
+                 "_clbm_gb300_pkg", "clbm_fish", "ibm_fish", "config_fish", "_variant"):
         sys.modules.pop(name, None)
     sys.path.insert(0, COMPAT)
     yield
@@ -131,3 +131,53 @@ def test_highre_airplane_variant_against_oracle(built_pkg, oracle_mod):
     """The high-Re airplane of config_highRe.py (800x260x220, chord 120, Re 1000, 8 degree
     inflow, the reference's own marker set) stepped on the GPU, against the oracle."""
     _variant_against_oracle(built_pkg, oracle_mod, built_pkg.highre_airplane_case(), 3)
+
+
+def small_fish_config(pkg, m_raw_inv):
+    """An in-memory ``config_fish`` (the names fish/clbm_fish.py and fish/ibm_fish.py import)
+    for a reduced swimmer: 120x48x6, 4:1 ellipse of chord 24, Re 300, heave 0.25c, pitch
+    15 deg, k = 0.8 (the motion law of fish/config_fish.py); and the same case as a
+    SimConfig for the oracle."""
+    X2, Y2 = pkg.config.ellipse_section(24.0, 6.0, 0.7)
+    X, Y, Z = pkg.config.extrude_layers(X2, Y2, 6)
+    ref = pkg.config.SimConfig(nx=120, ny=48, nz=6, chord=24.0, u_inf=0.05, re=300.0, x0=48.0,
+                               y0=24.0, a_heave=6.0, a_pitch=float(np.radians(15.0)),
+                               phi_pitch=float(np.pi / 2.0), aoa0=0.0, k_reduced=0.8,
+                               span=6.0, name="fish-120x48x6", X0=X, Y0=Y, Z0=Z)
+    m = types.ModuleType("config_fish")
+    m.Nx, m.Ny, m.Nz = ref.nx, ref.ny, ref.nz
+    m.cs2, m.s_v, m.s_e, m.s_q, m.s_pi = 1.0 / 3.0, ref.s_v, 1.0, 1.0, 1.0
+    m.U_inf, m.AoA0_deg, m.M_raw_inv_np = 0.05, 0.0, m_raw_inv
+    m.N_MARKERS_2D, m.N_MARKERS = len(X2), len(X)
+    m.X_marker_np, m.Y_marker_np, m.Z_marker_np = X, Y, Z
+    return m, ref
+
+
+def test_fish_dropin_modules_against_oracle(built_pkg, oracle_mod, dropin_env):
+    """fish/main_fish.py's solver and IBM modules (``from clbm_fish import CLBMSolver``,
+    ``from ibm_fish import FishIBM``, main_fish.py:51-52) through the drop-in modules, called
+    as that driver calls them, against the oracle of the same case."""
+    fix = np.load(os.path.join(GOLDEN, "dropin_main_moving.npz"))
+    cfg_mod, ref = small_fish_config(built_pkg, fix["cfg_M_raw_inv_np"])
+    sys.modules["config_fish"] = cfg_mod
+    clbm_fish = importlib.import_module("clbm_fish")
+    ibm_fish = importlib.import_module("ibm_fish")
+    assert clbm_fish.__file__.startswith(COMPAT) and ibm_fish.__file__.startswith(COMPAT)
+    assert "config_moving" not in sys.modules   # the alias is only held while loading
+    lbm = clbm_fish.CLBMSolver()
+    ibm = ibm_fish.FishIBM()
+    o = oracle_mod.Oracle(ref.nx, ref.ny, ref.nz, ref.s_v, ref.s_e, ref.ux_in, ref.uy_in,
+                          ref.X0, ref.Y0, ref.Z0)
+    for step in range(1, 21):
+        ms = ref.motion_state(step)
+        fx, fy, fz = ibm.compute_force(lbm.ux, lbm.uy, *ms)
+        lbm.step(fx, fy, fz)
+        o.compute_force(*ms)
+        o.lbm_step()
+    rho, ux, uy, uz = o.macro()
+    o.close()
+    got = {n: getattr(lbm, n).to_numpy() for n in FIELDS}
+    assert rel_l2(got["rho"], rho) < 1e-5
+    assert rel_l2(np.stack([got["ux"], got["uy"], got["uz"]]), np.stack([ux, uy, uz])) < 1e-5
+    assert ibm.X_marker.to_numpy().shape == (cfg_mod.N_MARKERS,)
+    lbm._solver.close()
