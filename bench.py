@@ -241,6 +241,32 @@ def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
                              "algorithmic_bytes": alg, "how": "bulk pass alone at creation, "
                              "all members' cells"}}
     ens.close()
+    out["persistent"] = measure_ensemble_persistent(pkg, torch, device, cases, steps, warmup)
+    return out
+
+
+def measure_ensemble_persistent(pkg, torch, device, cases, steps, warmup):
+    """The same ensemble with each step one persistent cooperative launch (the IBM phases
+    separated by a grid barrier, the bulk tiles shared out over them), as a replayed CUDA
+    graph; CUDA events on the ensemble's stream."""
+    os.environ["CLBM_ENS_STEP"] = "persistent"
+    try:
+        ens = pkg.Ensemble(cases, device=device)
+    finally:
+        del os.environ["CLBM_ENS_STEP"]
+    stream = torch.cuda.ExternalStream(ens.stream_handle(), device=torch.device("cuda", device))
+    ens.run(warmup)
+    ens.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ens.run(steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"ms_per_step": ms / steps, "mlups": ens.cells * steps / (ms / 1e3) / 1e6,
+           "blocks": ens.schedule()["blocks"], "launches_per_step": 1,
+           "phase_us_last_step": ens.phase_times()}
+    ens.close()
     return out
 
 

@@ -27,7 +27,9 @@ EXPORTED = (
     "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
-    "clbm_ensemble_tuning", "clbm_ensemble_destroy",
+    "clbm_ensemble_tuning", "clbm_ensemble_schedule", "clbm_ensemble_phase_times",
+    "clbm_selftest_grid_barrier",
+    "clbm_ensemble_destroy",
     "clbm_closure_layout", "clbm_closure_set", "clbm_trainer_create", "clbm_trainer_destroy",
     "clbm_trainer_capture", "clbm_trainer_read_slot", "clbm_trainer_extract", "clbm_trainer_count",
     "clbm_trainer_write_samples", "clbm_trainer_read_samples", "clbm_trainer_stats",
@@ -119,6 +121,9 @@ def lib():
             "clbm_ensemble_tuning": [vp, ctypes.POINTER(i32), ctypes.POINTER(i32),
                                      ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_float),
                                      ctypes.POINTER(i32)],
+            "clbm_ensemble_schedule": [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)],
+            "clbm_selftest_grid_barrier": [i32],
+            "clbm_ensemble_phase_times": [vp, ctypes.POINTER(ctypes.c_double)],
             "clbm_ensemble_destroy": [vp],
             "clbm_closure_layout": [P],
             "clbm_closure_set": [vp, P],

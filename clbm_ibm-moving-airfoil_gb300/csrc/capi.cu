@@ -1006,6 +1006,16 @@ struct clbm_ensemble {
     cudaGraphExec_t gexec = nullptr;
     int g_cur = -1;
     long long launches = 0;
+    // the whole step as one persistent cooperative launch (CLBM_ENS_STEP=persistent at
+    // creation): EnsPersArgs template, grid, and its device arrays
+    bool pers = false;
+    bool pers_idx32 = true;
+    int pers_grid = 0;
+    long long* d_pers = nullptr;   // mk0, sw0, wt0, off_rows: [n + 1] each
+    unsigned* d_bar = nullptr;     // grid barrier: arrivals, generation, error bits
+    IbmDev* d_nodev = nullptr;     // zeroed (empty force band)
+    unsigned long long* d_stamps = nullptr;   // phase clock of the last persistent step
+    EnsPersArgs pa{};
 };
 
 namespace {
@@ -1213,8 +1223,107 @@ int ens_tune(clbm_ensemble* e) {
     return ens_upload(e, best_bx);
 }
 
+// Set up the persistent step: per-member offsets of the virtual marker blocks, spreading
+// warps and bulk warp tiles, the share of bulk tiles done in each phase
+// (CLBM_ENS_PERS_SPLIT="a,b,c": the cumulative fractions done by the ends of phases 2, 3
+// and 4; default 0.05,0.25,0.6) and the grid: every block resident (the cooperative
+// launch refuses a larger grid).
+int ens_pers_setup(clbm_ensemble* e) {
+    const int n = e->n;
+    std::vector<long long> h(4 * (size_t)(n + 1), 0);
+    long long* mk0 = h.data();
+    long long* sw0 = mk0 + n + 1;
+    long long* wt0 = sw0 + n + 1;
+    bool idx32 = true;
+    for (int i = 0; i < n; ++i) {
+        const clbm_solver* s = e->s[i];
+        const clbm_ibm* b = e->ibm[i];
+        const long long nm = b ? b->a.n : 0;
+        mk0[i + 1] = mk0[i] + (nm + kEnsMarkerBlock - 1) / kEnsMarkerBlock;
+        sw0[i + 1] = sw0[i] + (nm + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp;
+        const long long cells = (long long)s->g.nx * s->g.ny * s->g.nz;
+        wt0[i + 1] = wt0[i] + (e->storage == CLBM_STORE_F32 ? (cells + 31) / 32
+                                                           : (long long)((s->g.nx + 63) / 64) * s->g.ny * s->g.nz);
+        idx32 = idx32 && 19LL * s->g.plane <= 0xffffffffLL;
+    }
+    double f[3] = {0.05, 0.25, 0.6};
+    if (const char* env = std::getenv("CLBM_ENS_PERS_SPLIT")) {
+        double a = 0, b = 0, c = 0;
+        if (std::sscanf(env, "%lf,%lf,%lf", &a, &b, &c) == 3 && 0 <= a && a <= b && b <= c && c <= 1) {
+            f[0] = a; f[1] = b; f[2] = c;
+        }
+    }
+    const long long wt = wt0[n];
+    if (wt >= (1LL << 30))
+        return fail(CLBM_ERR_ARG, "clbm_ensemble_create: too many cells for the persistent step");
+    EnsPersArgs& p = e->pa;
+    p.wt_split[0] = 0;
+    for (int k = 0; k < 3; ++k) p.wt_split[k + 1] = (long long)(f[k] * (double)wt);
+    p.wt_split[4] = wt;
+    p.mk_total = mk0[n];
+    p.sw_total = sw0[n];
+    p.n = n;
+    p.fin_blocks = kFinishBlocks / 4;   // 256-thread blocks: the threads of 64 of 64
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = ens_persistent_blocks_per_sm(e->storage, idx32);
+    if (per_sm < 1 || sms < 1)
+        return fail(CLBM_ERR_CUDA, "clbm_ensemble_create: no resident block for the persistent step");
+    CK(cudaMalloc(&e->d_pers, sizeof(long long) * h.size()));
+    CK(cudaMalloc(&e->d_bar, 4 * sizeof(unsigned)));
+    CK(cudaMalloc(&e->d_nodev, sizeof(IbmDev)));
+    CK(cudaMalloc(&e->d_stamps, 6 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(e->d_stamps, 0, 6 * sizeof(unsigned long long), e->st));
+    CK(cudaMemsetAsync(e->d_nodev, 0, sizeof(IbmDev), e->st));
+    CK(cudaMemcpyAsync(e->d_pers, h.data(), sizeof(long long) * h.size(), cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemsetAsync(e->d_bar, 0, 4 * sizeof(unsigned), e->st));
+    CK(cudaStreamSynchronize(e->st));
+    p.mk0 = e->d_pers;
+    p.sw0 = e->d_pers + n + 1;
+    p.wt0 = e->d_pers + 2 * (n + 1);
+    p.off_rows = e->d_pers + 3 * (n + 1);
+    p.off_new = e->d_off;
+    p.off_old = e->d_off + n + 1;
+    p.bar = e->d_bar;
+    p.nodev = e->d_nodev;
+    p.stamps = e->d_stamps;
+    e->pers_idx32 = idx32;
+    e->pers_grid = per_sm * sms;
+    e->pers = true;
+    return CLBM_OK;
+}
+
+// Error bits of the persistent step's barrier (a wait ran out): reported once, then
+// cleared.
+int ens_pers_check(clbm_ensemble* e, const char* who) {
+    if (!e->pers) return CLBM_OK;
+    unsigned err = 0;
+    CK(cudaMemcpyAsync(&err, e->d_bar + 2, sizeof(err), cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    if (!err) return CLBM_OK;
+    CK(cudaMemsetAsync(e->d_bar, 0, 4 * sizeof(unsigned), e->st));
+    CK(cudaStreamSynchronize(e->st));
+    return fail(CLBM_ERR_STATE, "%s: a grid-barrier wait of the persistent step ran out "
+                "(bits %u); the members' state is not valid", who, err);
+}
+
 int ens_step(clbm_ensemble* e) {
     const bool pull = !e->local;
+    if (e->pers) {
+        EnsPersArgs p = e->pa;
+        p.parity = e->cur;
+        p.compute_macro = !e->macro_full;
+        const cudaError_t err = launch_ens_persistent(e->storage, pull, e->pers_idx32, e->d_desc, p,
+                                                      e->pers_grid, e->st);
+        if (err != cudaSuccess)
+            return fail(CLBM_ERR_CUDA, "ensemble persistent step: %s", cudaGetErrorString(err));
+        e->launches += 1;
+        e->cur ^= 1;
+        e->local = false;
+        e->macro_full = false;
+        return CLBM_OK;
+    }
     launch_ens_markers(e->d_desc, e->n, e->max_marker_blocks, e->st);
     CK(cudaEventRecord(e->ev_box, e->st));
     long long* off_new = e->d_off;
@@ -1312,7 +1421,14 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
             cudaStreamWaitEvent(e->st, e->ev_sync, 0) != cudaSuccess)
             return bail(fail(CLBM_ERR_CUDA, "clbm_ensemble_create: stream ordering failed"));
     }
-    if (int rc = ens_tune(e)) return bail(rc);
+    const char* step_env = std::getenv("CLBM_ENS_STEP");
+    if (step_env && !std::strcmp(step_env, "persistent")) {
+        // descriptors only: the persistent step has its own bulk tiles
+        if (int rc = ens_upload(e, 128)) return bail(rc);
+        if (int rc = ens_pers_setup(e)) return bail(rc);
+    } else if (int rc = ens_tune(e)) {
+        return bail(rc);
+    }
     *out = e;
     return CLBM_OK;
 }
@@ -1323,6 +1439,7 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
         if (e->s[i]->cur != e->cur || (e->ibm[i] && e->ibm[i]->s != e->s[i]))
             return fail(CLBM_ERR_STATE, "clbm_ensemble_run: member %d was stepped or destroyed "
                         "outside the ensemble", i);
+    if (int rc = ens_pers_check(e, "clbm_ensemble_run")) return rc;
     for (int i = 0; i < e->n; ++i) {
         clbm_solver* s = e->s[i];
         if (int rc = join_bulk(s)) return rc;
@@ -1363,7 +1480,7 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
         while (nsteps - done >= 2) {
             CK(cudaGraphLaunch(e->gexec, e->st));
             done += 2;
-            e->launches += 12;
+            e->launches += e->pers ? 2 : 12;
         }
     }
     while (done < nsteps) {
@@ -1405,6 +1522,46 @@ int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* b
     return CLBM_OK;
 }
 
+int clbm_ensemble_schedule(const clbm_ensemble* e, int32_t* persistent, int32_t* blocks) {
+    if (!e) return fail(CLBM_ERR_ARG, "clbm_ensemble_schedule: null ensemble");
+    if (persistent) *persistent = e->pers ? 1 : 0;
+    if (blocks) *blocks = e->pers ? e->pers_grid : 0;
+    return CLBM_OK;
+}
+
+int clbm_ensemble_phase_times(clbm_ensemble* e, double* us) {
+    if (!e || !us) return fail(CLBM_ERR_ARG, "clbm_ensemble_phase_times: null argument");
+    if (!e->pers) return fail(CLBM_ERR_STATE, "clbm_ensemble_phase_times: not the persistent step");
+    unsigned long long t[6] = {0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(t, e->d_stamps, sizeof(t), cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    for (int k = 0; k < 5; ++k) us[k] = (t[k + 1] >= t[k]) ? (double)(t[k + 1] - t[k]) * 1e-3 : 0.0;
+    return CLBM_OK;
+}
+
+int clbm_selftest_grid_barrier(int32_t blocks) {
+    if (blocks < 1 || blocks > 16) return fail(CLBM_ERR_ARG, "clbm_selftest_grid_barrier: blocks in [1, 16]");
+    unsigned* bar = nullptr;
+    cudaStream_t st = nullptr;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    if (cudaMalloc(&bar, 4 * sizeof(unsigned)) != cudaSuccess) {
+        cudaStreamDestroy(st);
+        return fail(CLBM_ERR_CUDA, "clbm_selftest_grid_barrier: allocation failed");
+    }
+    unsigned h[4] = {0, 0, 0, 0};
+    cudaError_t err = cudaMemsetAsync(bar, 0, sizeof(h), st);
+    if (err == cudaSuccess) err = launch_ens_barrier_selftest(bar, blocks, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(h, bar, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cudaFree(bar);
+    cudaStreamDestroy(st);
+    if (err != cudaSuccess) return fail(CLBM_ERR_CUDA, "clbm_selftest_grid_barrier: %s", cudaGetErrorString(err));
+    if (h[2])
+        return fail(CLBM_ERR_STATE, "clbm_selftest_grid_barrier: bounded barrier wait gave up as "
+                    "intended (bits %u, %u arrivals)", h[2], h[0]);
+    return fail(CLBM_ERR_CUDA, "clbm_selftest_grid_barrier: the barrier did not report a timeout");
+}
+
 int clbm_ensemble_destroy(clbm_ensemble* e) {
     if (!e) return CLBM_OK;
     if (e->st) cudaStreamSynchronize(e->st);
@@ -1416,6 +1573,10 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     for (cudaEvent_t ev : e->gev) cudaEventDestroy(ev);
     if (e->d_tile0) cudaFree(e->d_tile0);
     if (e->d_off) cudaFree(e->d_off);
+    if (e->d_pers) cudaFree(e->d_pers);
+    if (e->d_bar) cudaFree(e->d_bar);
+    if (e->d_nodev) cudaFree(e->d_nodev);
+    if (e->d_stamps) cudaFree(e->d_stamps);
     cudaEvent_t evs[] = {e->ev_box, e->ev_bulk, e->ev_sync};
     for (cudaEvent_t ev : evs)
         if (ev) cudaEventDestroy(ev);

@@ -398,6 +398,38 @@ void launch_ens_bulk(int storage, bool pull, int bx, const EnsDesc* d, const lon
 void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile, bool idx32,
                           const EnsDesc* d, const long long* tile0, int n, long long ntiles,
                           int parity, int grid, cudaStream_t st);
+// The whole ensemble step as one cooperative launch of `grid` blocks of 256 threads
+// (ensemble.cu, kb_step_persistent). Offsets per member (n + 1 entries each): mk0 virtual
+// marker blocks of 256 markers, sw0 spreading warps, wt0 bulk warp tiles (64-cell row
+// segments in the 16-bit forms, 32-cell runs in float32); the bulk tiles
+// [wt_split[k], wt_split[k + 1]) are done in phase k + 2; off_rows (written by the launch):
+// box-pass warp items of this call's boxes (16-bit forms); bar: arrivals, generation, error
+// bits of the grid barrier (arrivals zero at launch).
+struct EnsPersArgs {
+    long long* off_new;
+    long long* off_old;
+    long long* off_rows;
+    const long long* mk0;
+    const long long* sw0;
+    const long long* wt0;
+    long long mk_total, sw_total;
+    long long wt_split[5];
+    unsigned* bar;
+    const IbmDev* nodev;   // zeroed: an empty force band, for members without a body
+    unsigned long long* stamps;   // optional phase clock: global timer at the start, after
+                                  // each barrier and at block 0's end (6 entries)
+    int n;
+    int parity;
+    int compute_macro;
+    int fin_blocks;
+};
+// Resident blocks per SM of the persistent step (0 when the query fails).
+int ens_persistent_blocks_per_sm(int storage, bool idx32);
+cudaError_t launch_ens_persistent(int storage, bool pull, bool idx32, const EnsDesc* d,
+                                  const EnsPersArgs& p, int grid, cudaStream_t st);
+// Cooperative launch whose barrier waits for one block more than it has: every wait runs
+// out after its bound and sets bar[2] (failure detection without a fault).
+cudaError_t launch_ens_barrier_selftest(unsigned* bar, int grid, cudaStream_t st);
 // Force-box cells of all members as one flat list (offsets per member, n + 1 each), then
 // band-prepare and box pass over it with `grid` blocks of kBoxBlock threads.
 void launch_ens_box_scan(const EnsDesc* d, int n, long long* off_new, long long* off_old, cudaStream_t st);

@@ -287,6 +287,345 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
 #undef CLBM_ENS_ROW
 }
 
+// ---------------------------------------------------------------- one persistent launch
+// The whole ensemble step as one cooperative launch (every block resident at once), the
+// form that one CUDA graph node replays: the IBM chain's dependent phases are separated by
+// a grid barrier, and the bulk pass's tiles are shared out over the phases, so that every
+// block does its part of the latency-bound chain and then bulk tiles until the next
+// barrier:
+//   1 markers of all members (the last virtual block of a member writes its force band)
+//   2 flat offsets of all force boxes (warp 0 of block 0)           + bulk tiles
+//   3 band prepare over the flat box-cell list                     + bulk tiles
+//   4 interpolation and spreading, two markers per warp            + bulk tiles
+//   5 force sums (virtual blocks per member) and the box pass (16-bit: by box rows, a
+//     64-cell segment per warp)                                     + the remaining bulk tiles
+// Bulk tiles are warp tiles: a 64-cell row segment (16-bit forms: the two-cell body, x
+// shifts by warp shuffles) or a run of 32 consecutive cells across row ends (float32),
+// with the member found per tile. Every per-cell and per-marker computation is the body the separate
+// launches use; data written earlier in the launch (bands, offsets, macro fields, marker
+// positions and forces, force fields) is read with plain or L2 loads after a barrier,
+// never through the read-only path (the populations read are those of the previous step).
+constexpr int kPersThreads = 256;
+constexpr int kPersWarps = kPersThreads / 32;
+constexpr int kBarrierPolls = 1 << 20;   // with 32 ns sleeps and an L2 round trip per poll: under a second
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// Barrier of the blocks of a cooperative launch: bar[0] arrivals, bar[1] generation,
+// bar[2] error bits. `expect` blocks must arrive (gridDim.x; a larger value is the
+// timeout self-test). A block waits at most kBarrierPolls polls; then it sets bar[2] and
+// goes on (the step's results are invalid and the host reports the error).
+__device__ __forceinline__ void grid_barrier(unsigned* bar, unsigned expect) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = ld_acquire_u32(bar + 1);
+        __threadfence();
+        const unsigned arrived = atom_add_acq_rel_u32(bar, 1u) + 1u;
+        if (arrived == expect) {
+            bar[0] = 0u;                       // ordered before the release below
+            st_release_u32(bar + 1, gen + 1u);
+        } else {
+            bool ok = false;
+            for (int it = 0; it < kBarrierPolls; ++it) {
+                if (ld_acquire_u32(bar + 1) != gen) { ok = true; break; }
+                __nanosleep(32);
+            }
+            if (!ok) atomicOr(bar + 2, 1u);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Phase clock of the persistent step: thread 0 of block 0 records the global timer (ns)
+// at the start and after each barrier into p.stamps[0..5] (when p.stamps is set).
+__device__ __forceinline__ void pers_stamp(const EnsPersArgs& p, int k) {
+    if (p.stamps && blockIdx.x == 0 && threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        p.stamps[k] = t;
+    }
+}
+
+// Member of flat index t over offsets written earlier in this launch (L2 loads).
+__device__ __forceinline__ int member_of_cg(const long long* off, int n, long long t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldcg(off + mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Warp tiles [t0, t1) of the bulk pass, one tile per warp at a time with its member found
+// by a binary search (little state stays live across the body; tile indices fit in 32
+// bits: the host checks the total).
+template <int S, bool PULL, bool IDX32>
+__device__ __forceinline__ void pers_bulk(const EnsDesc* __restrict__ d, const EnsPersArgs& p,
+                                          long long t0l, long long t1l) {
+    using T = typename Pop<S>::T;
+    const int lane = threadIdx.x & 31;
+    const int t0 = (int)t0l, t1 = (int)t1l;
+    const int gw = (int)blockIdx.x * kPersWarps + (int)(threadIdx.x >> 5);
+    const int nw = (int)gridDim.x * kPersWarps;
+    for (int t = t0 + gw; t < t1; t += nw) {
+        {
+            const int i = member_of(p.wt0, p.n, t);
+            const int first = (int)__ldg(p.wt0 + i);
+            const EnsDesc& D = d[i];
+            const Grid& g = D.g;   // by reference: read where used, not held in registers
+            const Coef& c = D.c;
+            const unsigned local = (unsigned)(t - first);
+            const T* fin = (const T*)D.f[p.parity];
+            T* fout = (T*)D.f[p.parity ^ 1];
+            // members without a body skip the empty band of p.nodev: one body for all
+            ForceArgs fa{};
+            fa.dev = D.has_ibm ? D.a.dev : p.nodev;
+            fa.slot = (int)(fa.dev->cur & 1);
+            if constexpr (S == CLBM_STORE_F32) {
+                const unsigned k = local * 32u + (unsigned)lane;
+                if (k < (unsigned)D.cells) {
+                    const unsigned row = k / (unsigned)g.nx;
+                    const int x = (int)(k - row * (unsigned)g.nx);
+                    const int y = (int)(row % (unsigned)g.ny), z = (int)(row / (unsigned)g.ny);
+                    stream_collide_cell<S, PULL, kForceSkipBand, IDX32>(fin, fout, g, c, fa, x, y, z);
+                }
+            } else {
+                const unsigned nseg = (unsigned)(g.nx + 63) / 64u;
+                const unsigned r = local / nseg;   // row z * ny + y
+                const int x0 = (int)(local - r * nseg) * 64 + 2 * lane;
+                const int y = (int)(r % (unsigned)g.ny), z = (int)(r / (unsigned)g.ny);
+                pair_body<S, PULL, kForceSkipBand, IDX32>(fin, fout, g, c, fa, x0, y, z);
+            }
+        }
+    }
+}
+
+template <int S, bool PULL, bool IDX32>
+__global__ void __launch_bounds__(kPersThreads, S == CLBM_STORE_F32 ? 2 : 3)
+kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
+    using T = typename Pop<S>::T;
+    const int n = p.n;
+    const unsigned nb = gridDim.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long gthread = (long long)blockIdx.x * kPersThreads + threadIdx.x;
+    const long long nthread = (long long)gridDim.x * kPersThreads;
+    pers_stamp(p, 0);
+    // 1: markers, virtual blocks of kEnsMarkerBlock markers (block-uniform branches)
+    for (long long v = blockIdx.x; v < p.mk_total; v += nb) {
+        const int i = member_of(p.mk0, n, v);
+        const EnsDesc& D = d[i];
+        ibm_markers_body<true, kEnsMarkerBlock>(D.a, D.g, MotionF{}, D.m, (int)(v - __ldg(p.mk0 + i)));
+    }
+    grid_barrier(p.bar, nb);
+    pers_stamp(p, 1);
+    // 2: flat offsets of this call's and the previous call's boxes
+    if (blockIdx.x == 0 && warp == 0) {
+        long long sa = 0, sb = 0, sr = 0;
+        for (int base = 0; base < n; base += 32) {
+            const int i = base + lane;
+            long long a = 0, b = 0, rw = 0;
+            if (i < n && d[i].has_ibm) {
+                const IbmDev* dev = d[i].a.dev;
+                const long long s = dev->step + 1;
+                const Band nbd = load_band(dev, (int)(s & 1));
+                const Band obd = load_band(dev, (int)((s - 1) & 1));
+                a = (long long)nbd.ilen * nbd.jlen * nbd.klen;
+                b = (long long)obd.ilen * obd.jlen * obd.klen;
+                // box pass by rows: 64-cell segments from i0 rounded down to even
+                if (nbd.ilen > 0)
+                    rw = (long long)((nbd.i0 + nbd.ilen - (nbd.i0 & ~1) + 63) / 64) * nbd.jlen * nbd.klen;
+            }
+            long long ia = a, ib = b, ir = rw;   // inclusive warp scans
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long ua = __shfl_up_sync(0xffffffffu, ia, o);
+                const long long ub = __shfl_up_sync(0xffffffffu, ib, o);
+                const long long ur = __shfl_up_sync(0xffffffffu, ir, o);
+                if (lane >= o) { ia += ua; ib += ub; ir += ur; }
+            }
+            if (i < n) {
+                p.off_new[i] = sa + ia - a;
+                p.off_old[i] = sb + ib - b;
+                p.off_rows[i] = sr + ir - rw;
+            }
+            sa += __shfl_sync(0xffffffffu, ia, 31);
+            sb += __shfl_sync(0xffffffffu, ib, 31);
+            sr += __shfl_sync(0xffffffffu, ir, 31);
+        }
+        if (lane == 0) {
+            p.off_new[n] = sa;
+            p.off_old[n] = sb;
+            p.off_rows[n] = sr;
+        }
+    }
+    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[0], p.wt_split[1]);
+    grid_barrier(p.bar, nb);
+    pers_stamp(p, 2);
+    // 3: band prepare over the flat list (zero the previous box, macro on the new one)
+    {
+        const long long total_old = __ldcg(p.off_old + n);
+        for (long long t = gthread; t < total_old; t += nthread) {
+            const int i = member_of_cg(p.off_old, n, t);
+            const EnsDesc& D = d[i];
+            const long long s = D.a.dev->step + 1;
+            const Band ob = load_band(D.a.dev, (int)((s - 1) & 1));
+            band_zero_cell(D.g, D.a.fx, D.a.fy, ob, (int)(t - __ldcg(p.off_old + i)));
+        }
+        if (p.compute_macro) {
+            const long long total_new = __ldcg(p.off_new + n);
+            for (long long t = gthread; t < total_new; t += nthread) {
+                const int i = member_of_cg(p.off_new, n, t);
+                const EnsDesc& D = d[i];
+                const long long s = D.a.dev->step + 1;
+                const Band nbd = load_band(D.a.dev, (int)(s & 1));
+                band_macro_cell<S, PULL>((const T*)D.f[p.parity], D.g, D.c, D.rho, D.ux, D.uy, D.uz,
+                                         nbd, (int)(t - __ldcg(p.off_new + i)));
+            }
+        }
+    }
+    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[1], p.wt_split[2]);
+    grid_barrier(p.bar, nb);
+    pers_stamp(p, 3);
+    // 4: interpolation and spreading, kSpreadMarkersPerWarp markers per warp
+    {
+        const long long gw = (long long)blockIdx.x * kPersWarps + warp;
+        for (long long w = gw; w < p.sw_total; w += (long long)nb * kPersWarps) {
+            const int i = member_of(p.sw0, n, w);
+            const EnsDesc& D = d[i];
+            ibm_interp_spread_body<kSpreadMarkersPerWarp>(
+                D.a, D.g, (int)(w - __ldg(p.sw0 + i)) * kSpreadMarkersPerWarp, lane);
+        }
+    }
+    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[2], p.wt_split[3]);
+    grid_barrier(p.bar, nb);
+    pers_stamp(p, 4);
+    // 5: force sums (virtual blocks of kPersThreads threads per member) and the box pass
+    for (long long v = blockIdx.x; v < (long long)n * p.fin_blocks; v += nb) {
+        const int i = (int)(v / p.fin_blocks);
+        const EnsDesc& D = d[i];
+        if (D.has_ibm) ibm_finish_body<kPersThreads>(D.a, D.g, (int)(v % p.fin_blocks), p.fin_blocks);
+    }
+    if constexpr (S == CLBM_STORE_F32) {
+        // one box cell per thread (the flat box pass of the separate launches)
+        const long long total = __ldcg(p.off_new + n);
+        for (long long t = gthread; t < total; t += nthread) {
+            const int i = member_of_cg(p.off_new, n, t);
+            const EnsDesc& D = d[i];
+            ForceArgs fa{};
+            fa.qx = D.a.fx;
+            fa.qy = D.a.fy;
+            fa.dev = D.a.dev;
+            const Band b = load_band(D.a.dev, (int)(D.a.dev->cur & 1));
+            box_pass_cell<S, PULL>((const T*)D.f[p.parity], (T*)D.f[p.parity ^ 1], D.g, D.c, fa, b,
+                                   (int)(t - __ldcg(p.off_new + i)));
+        }
+    } else {
+        // by rows of the box, a 64-cell segment per warp with the two-cell body (the single
+        // lattice's box pass; the same bits as one cell per thread)
+        const long long total = __ldcg(p.off_rows + n);
+        for (long long w = (long long)blockIdx.x * kPersWarps + warp; w < total; w += (long long)nb * kPersWarps) {
+            const int i = member_of_cg(p.off_rows, n, w);
+            const EnsDesc& D = d[i];
+            ForceArgs fa{};
+            fa.qx = D.a.fx;
+            fa.qy = D.a.fy;
+            fa.dev = D.a.dev;
+            fa.slot = (int)(D.a.dev->cur & 1);
+            const Band b = load_band(D.a.dev, fa.slot);
+            const int xa = b.i0 & ~1;
+            const int nseg = (b.i0 + b.ilen - xa + 63) / 64;
+            const int local = (int)(w - __ldcg(p.off_rows + i));
+            const int seg = local % nseg, r = local / nseg;
+            const int y = pmod(b.j0 + r % b.jlen, D.g.ny), z = pmod(b.k0 + r / b.jlen, D.g.nz);
+            pair_body<S, PULL, kForceOnlyBand, IDX32>((const T*)D.f[p.parity], (T*)D.f[p.parity ^ 1], D.g,
+                                                      D.c, fa, xa + seg * 64 + 2 * lane, y, z);
+        }
+    }
+    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[3], p.wt_split[4]);
+    pers_stamp(p, 5);
+}
+
+// Self-test of the bounded barrier: every block waits for one block more than the launch
+// has, so each wait runs out and sets the error bit.
+__global__ void __launch_bounds__(kPersThreads) kb_barrier_selftest(unsigned* bar) {
+    grid_barrier(bar, gridDim.x + 1);
+}
+
+template <int S, bool PULL, bool IDX32>
+static int pers_occupancy() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kb_step_persistent<S, PULL, IDX32>, kPersThreads, 0) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+template <int S, bool PULL, bool IDX32>
+static cudaError_t pers_launch(const EnsDesc* d, const EnsPersArgs& p, int grid, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kPersThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kb_step_persistent<S, PULL, IDX32>, d, p);
+}
+
+int ens_persistent_blocks_per_sm(int storage, bool idx32) {
+    int a = 0, b = 0;
+#define CLBM_PERS_OCC(S_)                                                              \
+    if (idx32) { a = pers_occupancy<S_, true, true>(); b = pers_occupancy<S_, false, true>(); } \
+    else { a = pers_occupancy<S_, true, false>(); b = pers_occupancy<S_, false, false>(); }
+    if (storage == CLBM_STORE_F32) { CLBM_PERS_OCC(CLBM_STORE_F32) }
+    else if (storage == CLBM_STORE_F16S) { CLBM_PERS_OCC(CLBM_STORE_F16S) }
+    else { CLBM_PERS_OCC(CLBM_STORE_BF16S) }
+#undef CLBM_PERS_OCC
+    return std::min(a, b);
+}
+
+cudaError_t launch_ens_persistent(int storage, bool pull, bool idx32, const EnsDesc* d,
+                                  const EnsPersArgs& p, int grid, cudaStream_t st) {
+#define CLBM_PERS_GO(S_)                                                                  \
+    if (pull && idx32) return pers_launch<S_, true, true>(d, p, grid, st);               \
+    if (pull) return pers_launch<S_, true, false>(d, p, grid, st);                       \
+    if (idx32) return pers_launch<S_, false, true>(d, p, grid, st);                      \
+    return pers_launch<S_, false, false>(d, p, grid, st);
+    if (storage == CLBM_STORE_F32) { CLBM_PERS_GO(CLBM_STORE_F32) }
+    else if (storage == CLBM_STORE_F16S) { CLBM_PERS_GO(CLBM_STORE_F16S) }
+    else { CLBM_PERS_GO(CLBM_STORE_BF16S) }
+#undef CLBM_PERS_GO
+}
+
+cudaError_t launch_ens_barrier_selftest(unsigned* bar, int grid, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kPersThreads);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kb_barrier_selftest, bar);
+}
+
 #define CLBM_ENS_STORE(storage, ...)                                                         \
     switch (storage) {                                                                       \
         case CLBM_STORE_F32: { constexpr int S_ = CLBM_STORE_F32; __VA_ARGS__; } break;     \

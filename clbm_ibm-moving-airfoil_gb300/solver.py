@@ -354,6 +354,34 @@ class Ensemble:
         return dict(tile_width=w.value, blocks=b.value, tiles=t.value, bulk_us=round(ms.value * 1e3, 2),
                     rows_per_block=r.value)
 
+    @staticmethod
+    def selftest_grid_barrier(blocks=2):
+        """Make the persistent step's grid barrier wait for a block that does not exist, so
+        every bounded wait runs out on purpose; returns the error the library reports (a
+        CLBMError with code CLBM_ERR_STATE is the expected outcome)."""
+        rc = lib().clbm_selftest_grid_barrier(int(blocks))
+        try:
+            check(rc)
+        except _lib.CLBMError as e:
+            return e
+        return None
+
+    def schedule(self):
+        """Step form chosen at creation: persistent (one cooperative launch per step,
+        CLBM_ENS_STEP=persistent) with its grid, or the seven launches (blocks 0)."""
+        p, b = ctypes.c_int32(), ctypes.c_int32()
+        check(lib().clbm_ensemble_schedule(self._h, ctypes.byref(p), ctypes.byref(b)))
+        return dict(persistent=bool(p.value), blocks=b.value)
+
+    def phase_times(self):
+        """Phase clock of the last persistent step in microseconds: markers, offsets,
+        band prepare, spreading, and force sums + box pass + the rest of the bulk pass (as
+        seen by block 0)."""
+        us = (ctypes.c_double * 5)()
+        check(lib().clbm_ensemble_phase_times(self._h, us))
+        return dict(zip(("markers", "offsets", "band_prepare", "spreading", "sums_box_rest"),
+                        (round(v, 2) for v in us)))
+
     def synchronize(self):
         for s in self.sims:
             s.solver.synchronize()

@@ -161,7 +161,8 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
  * together -- each step is seven launches over all members (markers, force-box offsets,
  * band macro, interpolation/spreading, force sums, force-box pass, and the bulk
  * stream-collide over every member's cells: one launch over a flat tile list, or one
- * launch per row width, run concurrently). Members keep their buffers and
+ * launch per row width, run concurrently), or one persistent launch when the ensemble is
+ * created with CLBM_ENS_STEP=persistent (clbm_ensemble_schedule). Members keep their buffers and
  * all per-member reads (clbm_read_macro, ibm_read_force_history, ...) keep working; the
  * members must be fresh or at the same step, share storage form and device, and outlive
  * the ensemble. clbm_ensemble_create times the bulk-pass tile width and block schedule
@@ -179,6 +180,20 @@ int clbm_ensemble_stream(const clbm_ensemble* e, void** out);
  * one block computes per tile (0 otherwise). Any pointer may be NULL. */
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,
                          int64_t* tiles, float* bulk_ms, int32_t* rows_per_block);
+/* Step form of the ensemble: *persistent = 1 when each step is one persistent cooperative
+ * launch (every block resident; the IBM phases separated by a grid barrier with bounded
+ * waits, the bulk pass's tiles shared out over the phases), chosen by the environment
+ * variable CLBM_ENS_STEP=persistent when the ensemble is created, with *blocks its grid;
+ * 0 and 0 for the seven launches. Both forms give the same bits. A barrier wait that ran
+ * out is reported by the next clbm_ensemble_run (CLBM_ERR_STATE). Any pointer may be
+ * NULL. */
+int clbm_ensemble_schedule(const clbm_ensemble* e, int32_t* persistent, int32_t* blocks);
+/* Phase clock of the last persistent step, in microseconds (5 entries): markers; box
+ * offsets + bulk share; band prepare + bulk share; interpolation/spreading + bulk share; and
+ * force sums, box pass and the rest of the bulk pass as seen by block 0 (the launch ends
+ * when its last block does). Waits for the ensemble's stream. CLBM_ERR_STATE for the seven
+ * launches. */
+int clbm_ensemble_phase_times(clbm_ensemble* e, double* us);
 int clbm_ensemble_destroy(clbm_ensemble* e);
 
 /* Wait for all queued work of the solver. Returns CLBM_ERR_STATE when a bounded device
@@ -201,6 +216,13 @@ int clbm_set_rho_floor(clbm_solver* s, double rho_floor);
  * CLBM_ERR_STATE when the timeout was reported (the expected outcome), leaves the state
  * unchanged (no block writes results) and clears the status word. */
 int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit);
+
+/* Failure-detection self test of the persistent ensemble step's grid barrier: a
+ * cooperative launch of `blocks` (1..16) blocks whose barrier waits for one block more than
+ * the launch has, so every block's bounded wait gives up (well under a second) and sets the
+ * error bits instead of hanging. Returns CLBM_ERR_STATE when the timeout was reported (the
+ * expected outcome). */
+int clbm_selftest_grid_barrier(int32_t blocks);
 
 /* The solver's CUDA stream (cudaStream_t), for callers that record events or order their
  * own work against the solver. The stream stays owned by the solver. An IBM step runs its

@@ -89,21 +89,30 @@ def test_ensemble_tiled_spreading_is_bit_identical(built_pkg, monkeypatch):
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_ensemble_at_its_real_sizes(built_pkg, oracle_mod, storage):
+@pytest.mark.parametrize("form", ["launches", "persistent"])
+def test_ensemble_at_its_real_sizes(built_pkg, oracle_mod, monkeypatch, storage, form):
     """The batched ensemble as the bench runs it: 64 members drawn with seeds 0..63 from the
     lattices 150x60x12, 200x80x16 and 300x100x24 (chord Nx / 6.25, Re, heave, pitch, phase
-    and k drawn per seed), with the schedule the autotuner picks for them, 50 steps. The
-    first member of each lattice and the last member give the bits of the same case stepped
-    alone; in float32 one member (300x100x24) matches the oracle within the plain-path
-    bounds."""
+    and k drawn per seed), with the schedule the autotuner picks for them (or the whole
+    step as one persistent launch), 50 steps. The first member of each lattice and the last
+    member give the bits of the same case stepped alone; in float32 one member (300x100x24)
+    matches the oracle within the plain-path bounds."""
     pkg = built_pkg
     cases = [pkg.config.ensemble_case(seed, storage=storage) for seed in range(64)]
     steps = 50
+    if form == "persistent":
+        monkeypatch.setenv("CLBM_ENS_STEP", "persistent")
     ens = pkg.Ensemble(cases)
+    monkeypatch.delenv("CLBM_ENS_STEP", raising=False)
     ens.run(steps)
     ens.synchronize()
-    t = ens.tuning()
-    assert t["blocks"] > 0 and t["tiles"] > 0 and t["bulk_us"] > 0
+    sch = ens.schedule()
+    assert sch["persistent"] == (form == "persistent")
+    if form == "persistent":
+        assert sch["blocks"] >= 152
+    else:
+        t = ens.tuning()
+        assert t["blocks"] > 0 and t["tiles"] > 0 and t["bulk_us"] > 0
     firsts = {}
     for i, c in enumerate(cases):
         firsts.setdefault((c.nx, c.ny, c.nz), i)
@@ -131,3 +140,44 @@ def test_ensemble_at_its_real_sizes(built_pkg, oracle_mod, storage):
         assert rel_l2(np.stack([got["ux"], got["uy"], got["uz"]]), np.stack([ux, uy, uz])) <= 1e-5
         assert rel_l2(ens.sims[i].ibm.force_history(steps), ref_hist) <= 1e-4
     ens.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
+def test_persistent_step_equals_separate_launches(built_pkg, monkeypatch, storage, graph, lattices):
+    """The whole ensemble step as one persistent cooperative launch (grid barrier between
+    the IBM phases, bulk tiles shared out over the phases) gives the populations of the
+    seven separate launches bit for bit; the force history is the same sums (the marker
+    forces added in another fixed order)."""
+    pkg = built_pkg
+    cases = _cases(pkg, storage, lattices=lattices)
+    out = {}
+    for form in ("persistent", "launches"):
+        if form == "persistent":
+            monkeypatch.setenv("CLBM_ENS_STEP", "persistent")
+        else:
+            monkeypatch.delenv("CLBM_ENS_STEP", raising=False)
+        ens = pkg.Ensemble(cases)
+        assert ens.schedule()["persistent"] == (form == "persistent")
+        ens.run(24, graph=graph)
+        out[form] = [(m.solver.read_populations(), m.ibm.force_history(24), m.ibm.step_count())
+                     for m in ens.sims]
+        ens.close()
+    for (fa, ha, na), (fb, hb, nb) in zip(out["persistent"], out["launches"]):
+        np.testing.assert_array_equal(fa, fb)
+        np.testing.assert_allclose(ha, hb, rtol=1e-12, atol=1e-14)
+        assert na == nb == 24
+
+
+def test_grid_barrier_timeout_is_reported(built_pkg):
+    """Failure detection of the persistent step without a fault: a cooperative launch whose
+    grid barrier waits for a block that does not exist gives up after its bounded wait and
+    reports it; the device stays usable."""
+    pkg = built_pkg
+    err = pkg.Ensemble.selftest_grid_barrier(2)
+    assert err is not None and err.code == 4, err
+    s = pkg.Solver(40, 8, 4, 1.5)
+    s.step()
+    s.synchronize()
+    s.close()
