@@ -24,7 +24,7 @@ EXPORTED = (
     "ibm_destroy", "ibm_compute_force", "ibm_compute_force_motion", "ibm_read_forces",
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
     "clbm_synchronize", "clbm_set_rho_floor", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
-    "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant",
+    "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant", "clbm_binary_version",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
     "clbm_ensemble_tuning", "clbm_ensemble_schedule", "clbm_ensemble_phase_times",
@@ -112,6 +112,7 @@ def lib():
                                         ctypes.POINTER(d), ctypes.POINTER(i64)],
             "clbm_device_bytes": [vp, ctypes.POINTER(i64)],
             "clbm_kernel_variant": [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float)],
+            "clbm_binary_version": [ctypes.POINTER(i32), ctypes.POINTER(i32)],
             "clbm_host_alloc": [i64, pvp],
             "clbm_host_free": [vp],
             "ibm_force_sums_noalloc": [P, P, i32, i32, i32, P, P, i32, vp, P],

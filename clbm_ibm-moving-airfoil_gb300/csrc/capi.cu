@@ -936,6 +936,16 @@ int clbm_closure_set(clbm_solver* s, const float* params) {
     return CLBM_OK;
 }
 
+int clbm_binary_version(int32_t* binary, int32_t* ptx) {
+    if (!binary || !ptx) return fail(CLBM_ERR_ARG, "clbm_binary_version: null argument");
+    int b = 0, p = 0;
+    const cudaError_t err = stream_collide_binary_version(&b, &p);
+    if (err != cudaSuccess) return fail(CLBM_ERR_CUDA, "clbm_binary_version: %s", cudaGetErrorString(err));
+    *binary = b;
+    *ptx = p;
+    return CLBM_OK;
+}
+
 int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_launch) {
     if (!s || !variant) return fail(CLBM_ERR_ARG, "clbm_kernel_variant: invalid argument");
     *variant = s->variant;

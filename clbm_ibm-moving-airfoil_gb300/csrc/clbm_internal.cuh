@@ -271,6 +271,8 @@ struct ForceArgs {
 int knob(const char* name, int def);  // integer tuning parameter from the environment
 bool spread_tiled();                  // IBM spreading through shared-memory tiles (CLBM_SPREAD)
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
+// binaryVersion / ptxVersion of the float32 bulk stream-collide kernel (cudaFuncGetAttributes).
+cudaError_t stream_collide_binary_version(int* binary, int* ptx);
 // Stream-collide kernel variants for the full-grid pass:
 //   kVariantCell    one cell per thread, direct loads (float32 parity kernel)
 //   kVariantPair    two cells per thread, half2 loads, warp-shuffle x shifts (16-bit only)

@@ -554,6 +554,17 @@ static int macro_full_blocks() {
         default: { constexpr int S_ = CLBM_STORE_BF16S; __VA_ARGS__; } break;             \
     }
 
+// Architecture the bulk stream-collide kernel was compiled for, as the CUDA runtime reports
+// it (major * 10 + minor of the SASS it loaded), and its PTX version.
+cudaError_t stream_collide_binary_version(int* binary, int* ptx) {
+    cudaFuncAttributes fa{};
+    const cudaError_t err = cudaFuncGetAttributes(&fa, k_stream_collide<CLBM_STORE_F32, true, kForceSkipBand, true>);
+    if (err != cudaSuccess) return err;
+    *binary = fa.binaryVersion;
+    *ptx = fa.ptxVersion;
+    return cudaSuccess;
+}
+
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st) {
     CLBM_DISPATCH_STORE(storage, (k_init<S_><<<cell_grid(g), kBX, 0, st>>>(
                                      (typename Pop<S_>::T*)f, g, c)));

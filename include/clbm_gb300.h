@@ -256,6 +256,11 @@ int clbm_device_bytes(const clbm_solver* s, int64_t* out);
  * counterpart: the reference has one kernel per phase (clbm_moving.py:326-343). */
 int clbm_kernel_variant(const clbm_solver* s, int32_t* variant, float* ms_per_launch);
 
+/* Architecture of the loaded device code as the CUDA runtime reports it for the bulk
+ * stream-collide kernel (cudaFuncGetAttributes): *binary = major * 10 + minor of the SASS
+ * (103 for sm_103a), *ptx the PTX version it was generated from. Needs a GPU. */
+int clbm_binary_version(int32_t* binary, int32_t* ptx);
+
 /* ---- Learned sub-grid closure --------------------------------------------------------
  * A 19 -> 32 -> 32 -> 1 network (GELU, BF16 weights, FP32 accumulation) maps the 19
  * normalised non-equilibrium central moments of a cell to the relaxation rate s_h of its

@@ -368,3 +368,12 @@ def test_force_box_at_the_outlet_on_an_odd_lattice(gpkg, oracle_mod, storage, to
         assert e_rho <= 1e-5 and e_u <= 1e-5 and e_f <= 1e-4
     else:
         assert e_u < tol and e_f < 10 * tol
+
+
+def test_loaded_device_code_is_sm_103a(gpkg):
+    """The CUDA runtime reports the loaded kernels as compiled for compute capability 10.3
+    (the sm_103a SASS of the library, not a PTX JIT for another target)."""
+    import ctypes
+    b, p = ctypes.c_int32(), ctypes.c_int32()
+    assert gpkg.lib().clbm_binary_version(ctypes.byref(b), ctypes.byref(p)) == 0
+    assert b.value == 103, (b.value, p.value)
