@@ -1021,7 +1021,8 @@ struct clbm_ensemble {
     bool pers = false;
     bool pers_idx32 = true;
     int pers_grid = 0;
-    long long* d_pers = nullptr;   // mk0, sw0, wt0, off_rows: [n + 1] each
+    long long* d_pers = nullptr;   // mk0, sw0, off_rows: [n + 1] each
+    std::unique_ptr<EnsPersTable> ptab;   // parameter table of the bulk tiles
     unsigned* d_bar = nullptr;     // grid barrier: arrivals, generation, error bits
     IbmDev* d_nodev = nullptr;     // zeroed (empty force band)
     unsigned long long* d_stamps = nullptr;   // phase clock of the last persistent step
@@ -1233,43 +1234,61 @@ int ens_tune(clbm_ensemble* e) {
     return ens_upload(e, best_bx);
 }
 
-// Set up the persistent step: per-member offsets of the virtual marker blocks, spreading
-// warps and bulk warp tiles, the share of bulk tiles done in each phase
-// (CLBM_ENS_PERS_SPLIT="a,b,c": the cumulative fractions done by the ends of phases 2, 3
-// and 4; default 0.05,0.25,0.6) and the grid: every block resident (the cooperative
-// launch refuses a larger grid).
+// Set up the persistent step: per-member offsets of the virtual marker blocks and
+// spreading warps, the parameter table of the bulk tiles (members' constants and first
+// block tiles), the share of the bulk pass done in each phase (CLBM_ENS_PERS_SPLIT="a,b,c":
+// the cumulative fractions done by the ends of phases 2, 3 and 4; default 0.1,0.3,0.7)
+// and the grid: every block resident (the cooperative launch refuses a larger grid).
 int ens_pers_setup(clbm_ensemble* e) {
     const int n = e->n;
-    std::vector<long long> h(4 * (size_t)(n + 1), 0);
+    if (n > kPersMaxMembers)
+        return fail(CLBM_ERR_ARG, "clbm_ensemble_create: the persistent step takes at most %d members",
+                    kPersMaxMembers);
+    std::vector<long long> h(3 * (size_t)(n + 1), 0);
     long long* mk0 = h.data();
     long long* sw0 = mk0 + n + 1;
-    long long* wt0 = sw0 + n + 1;
+    e->ptab.reset(new EnsPersTable());
+    EnsPersTable& tb = *e->ptab;
+    CK(cudaMalloc(&e->d_nodev, sizeof(IbmDev)));
+    CK(cudaMemsetAsync(e->d_nodev, 0, sizeof(IbmDev), e->st));
     bool idx32 = true;
+    long long bt = 0;
     for (int i = 0; i < n; ++i) {
         const clbm_solver* s = e->s[i];
         const clbm_ibm* b = e->ibm[i];
         const long long nm = b ? b->a.n : 0;
         mk0[i + 1] = mk0[i] + (nm + kEnsMarkerBlock - 1) / kEnsMarkerBlock;
         sw0[i + 1] = sw0[i] + (nm + kSpreadMarkersPerWarp - 1) / kSpreadMarkersPerWarp;
+        const EnsDesc D = member_desc(e, i);
         const long long cells = (long long)s->g.nx * s->g.ny * s->g.nz;
-        wt0[i + 1] = wt0[i] + (e->storage == CLBM_STORE_F32 ? (cells + 31) / 32
-                                                           : (long long)((s->g.nx + 63) / 64) * s->g.ny * s->g.nz);
+        const long long wt = e->storage == CLBM_STORE_F32 ? (cells + 31) / 32
+                                                         : (long long)((s->g.nx + 63) / 64) * s->g.ny * s->g.nz;
+        EnsMember& M = tb.m[i];
+        M.g = D.g;
+        M.c = D.c;
+        M.f[0] = D.f[0];
+        M.f[1] = D.f[1];
+        M.dev = D.has_ibm ? D.a.dev : e->d_nodev;
+        M.cells = D.cells;
+        M.wtiles = (int)wt;
+        tb.bt0[i] = (int)bt;
+        bt += (wt + kPersTileWarps - 1) / kPersTileWarps;
         idx32 = idx32 && 19LL * s->g.plane <= 0xffffffffLL;
     }
-    double f[3] = {0.05, 0.25, 0.6};
+    if (bt >= (1LL << 30))
+        return fail(CLBM_ERR_ARG, "clbm_ensemble_create: too many cells for the persistent step");
+    tb.bt0[n] = (int)bt;
+    double f[3] = {0.1, 0.3, 0.7};
     if (const char* env = std::getenv("CLBM_ENS_PERS_SPLIT")) {
         double a = 0, b = 0, c = 0;
         if (std::sscanf(env, "%lf,%lf,%lf", &a, &b, &c) == 3 && 0 <= a && a <= b && b <= c && c <= 1) {
             f[0] = a; f[1] = b; f[2] = c;
         }
     }
-    const long long wt = wt0[n];
-    if (wt >= (1LL << 30))
-        return fail(CLBM_ERR_ARG, "clbm_ensemble_create: too many cells for the persistent step");
     EnsPersArgs& p = e->pa;
-    p.wt_split[0] = 0;
-    for (int k = 0; k < 3; ++k) p.wt_split[k + 1] = (long long)(f[k] * (double)wt);
-    p.wt_split[4] = wt;
+    p.bt_split[0] = 0;
+    for (int k = 0; k < 3; ++k) p.bt_split[k + 1] = (int)(f[k] * (double)bt);
+    p.bt_split[4] = (int)bt;
     p.mk_total = mk0[n];
     p.sw_total = sw0[n];
     p.n = n;
@@ -1282,17 +1301,14 @@ int ens_pers_setup(clbm_ensemble* e) {
         return fail(CLBM_ERR_CUDA, "clbm_ensemble_create: no resident block for the persistent step");
     CK(cudaMalloc(&e->d_pers, sizeof(long long) * h.size()));
     CK(cudaMalloc(&e->d_bar, 4 * sizeof(unsigned)));
-    CK(cudaMalloc(&e->d_nodev, sizeof(IbmDev)));
     CK(cudaMalloc(&e->d_stamps, 6 * sizeof(unsigned long long)));
     CK(cudaMemsetAsync(e->d_stamps, 0, 6 * sizeof(unsigned long long), e->st));
-    CK(cudaMemsetAsync(e->d_nodev, 0, sizeof(IbmDev), e->st));
     CK(cudaMemcpyAsync(e->d_pers, h.data(), sizeof(long long) * h.size(), cudaMemcpyHostToDevice, e->st));
     CK(cudaMemsetAsync(e->d_bar, 0, 4 * sizeof(unsigned), e->st));
     CK(cudaStreamSynchronize(e->st));
     p.mk0 = e->d_pers;
     p.sw0 = e->d_pers + n + 1;
-    p.wt0 = e->d_pers + 2 * (n + 1);
-    p.off_rows = e->d_pers + 3 * (n + 1);
+    p.off_rows = e->d_pers + 2 * (n + 1);
     p.off_new = e->d_off;
     p.off_old = e->d_off + n + 1;
     p.bar = e->d_bar;
@@ -1325,7 +1341,7 @@ int ens_step(clbm_ensemble* e) {
         p.parity = e->cur;
         p.compute_macro = !e->macro_full;
         const cudaError_t err = launch_ens_persistent(e->storage, pull, e->pers_idx32, e->d_desc, p,
-                                                      e->pers_grid, e->st);
+                                                      *e->ptab, e->pers_grid, e->st);
         if (err != cudaSuccess)
             return fail(CLBM_ERR_CUDA, "ensemble persistent step: %s", cudaGetErrorString(err));
         e->launches += 1;

@@ -402,10 +402,9 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
                           int parity, int grid, cudaStream_t st);
 // The whole ensemble step as one cooperative launch of `grid` blocks of 256 threads
 // (ensemble.cu, kb_step_persistent). Offsets per member (n + 1 entries each): mk0 virtual
-// marker blocks of 256 markers, sw0 spreading warps, wt0 bulk warp tiles (64-cell row
-// segments in the 16-bit forms, 32-cell runs in float32); the bulk tiles
-// [wt_split[k], wt_split[k + 1]) are done in phase k + 2; off_rows (written by the launch):
-// box-pass warp items of this call's boxes (16-bit forms); bar: arrivals, generation, error
+// marker blocks of 256 markers, sw0 spreading warps; off_rows (written by the launch):
+// box-pass warp items of this call's boxes (16-bit forms); the bulk pass's block tiles
+// [bt_split[k], bt_split[k + 1]) are done in phase k + 2; bar: arrivals, generation, error
 // bits of the grid barrier (arrivals zero at launch).
 struct EnsPersArgs {
     long long* off_new;
@@ -413,9 +412,8 @@ struct EnsPersArgs {
     long long* off_rows;
     const long long* mk0;
     const long long* sw0;
-    const long long* wt0;
     long long mk_total, sw_total;
-    long long wt_split[5];
+    int bt_split[5];
     unsigned* bar;
     const IbmDev* nodev;   // zeroed: an empty force band, for members without a body
     unsigned long long* stamps;   // optional phase clock: global timer at the start, after
@@ -425,10 +423,31 @@ struct EnsPersArgs {
     int compute_macro;
     int fin_blocks;
 };
+// What the bulk tiles of the persistent step read of a member, passed in the kernel's
+// parameter table (the constant bank, indexed by a block-uniform member number), so the
+// bulk bodies keep the grid and collision constants out of per-thread registers as the
+// separate launches do. A block tile is kPersTileWarps consecutive warp tiles of one member
+// (64-cell row segments in the 16-bit forms, 32-cell runs in float32); bt0: first block
+// tile of each member (n + 1 entries).
+constexpr int kPersMaxMembers = 128;
+constexpr int kPersTileWarps = 8;
+struct EnsMember {
+    Grid g;
+    Coef c;
+    void* f[2];
+    IbmDev* dev;      // the member's IBM device state, or the zeroed one (no body)
+    int cells;
+    int wtiles;       // warp tiles of the member
+};
+struct EnsPersTable {
+    EnsMember m[kPersMaxMembers];
+    int bt0[kPersMaxMembers + 1];
+};
 // Resident blocks per SM of the persistent step (0 when the query fails).
 int ens_persistent_blocks_per_sm(int storage, bool idx32);
 cudaError_t launch_ens_persistent(int storage, bool pull, bool idx32, const EnsDesc* d,
-                                  const EnsPersArgs& p, int grid, cudaStream_t st);
+                                  const EnsPersArgs& p, const EnsPersTable& t, int grid,
+                                  cudaStream_t st);
 // Cooperative launch whose barrier waits for one block more than it has: every wait runs
 // out after its bound and sets bar[2] (failure detection without a fault).
 cudaError_t launch_ens_barrier_selftest(unsigned* bar, int grid, cudaStream_t st);

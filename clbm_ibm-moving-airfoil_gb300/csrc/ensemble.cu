@@ -299,10 +299,11 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
 //   4 interpolation and spreading, two markers per warp            + bulk tiles
 //   5 force sums (virtual blocks per member) and the box pass (16-bit: by box rows, a
 //     64-cell segment per warp)                                     + the remaining bulk tiles
-// Bulk tiles are warp tiles: a 64-cell row segment (16-bit forms: the two-cell body, x
-// shifts by warp shuffles) or a run of 32 consecutive cells across row ends (float32),
-// with the member found per tile. Every per-cell and per-marker computation is the body the separate
-// launches use; data written earlier in the launch (bands, offsets, macro fields, marker
+// A warp's bulk tile is a 64-cell row segment (16-bit forms: the two-cell body, x shifts
+// by warp shuffles) or a run of 32 consecutive cells across row ends (float32); a block
+// takes kPersTileWarps consecutive warp tiles of one member at a time, whose constants it
+// reads from the kernel's parameter table (EnsPersTable). Every per-cell and per-marker
+// computation is the body the separate launches use; data written earlier in the launch (bands, offsets, macro fields, marker
 // positions and forces, force fields) is read with plain or L2 loads after a barrier,
 // never through the read-only path (the populations read are those of the previous step).
 constexpr int kPersThreads = 256;
@@ -370,53 +371,49 @@ __device__ __forceinline__ int member_of_cg(const long long* off, int n, long lo
     return lo;
 }
 
-// Warp tiles [t0, t1) of the bulk pass, one tile per warp at a time with its member found
-// by a binary search (little state stays live across the body; tile indices fit in 32
-// bits: the host checks the total).
+// Block tiles [b0, b1) of the bulk pass: a block tile is kPersTileWarps consecutive warp
+// tiles of one member, so the member number is the same in the whole block and its
+// constants come from the parameter table (constant bank) like a separate launch's.
 template <int S, bool PULL, bool IDX32>
-__device__ __forceinline__ void pers_bulk(const EnsDesc* __restrict__ d, const EnsPersArgs& p,
-                                          long long t0l, long long t1l) {
+__device__ __forceinline__ void pers_bulk(const EnsPersTable& tb, const EnsPersArgs& p, int b0, int b1) {
     using T = typename Pop<S>::T;
-    const int lane = threadIdx.x & 31;
-    const int t0 = (int)t0l, t1 = (int)t1l;
-    const int gw = (int)blockIdx.x * kPersWarps + (int)(threadIdx.x >> 5);
-    const int nw = (int)gridDim.x * kPersWarps;
-    for (int t = t0 + gw; t < t1; t += nw) {
-        {
-            const int i = member_of(p.wt0, p.n, t);
-            const int first = (int)__ldg(p.wt0 + i);
-            const EnsDesc& D = d[i];
-            const Grid& g = D.g;   // by reference: read where used, not held in registers
-            const Coef& c = D.c;
-            const unsigned local = (unsigned)(t - first);
-            const T* fin = (const T*)D.f[p.parity];
-            T* fout = (T*)D.f[p.parity ^ 1];
-            // members without a body skip the empty band of p.nodev: one body for all
-            ForceArgs fa{};
-            fa.dev = D.has_ibm ? D.a.dev : p.nodev;
-            fa.slot = (int)(fa.dev->cur & 1);
-            if constexpr (S == CLBM_STORE_F32) {
-                const unsigned k = local * 32u + (unsigned)lane;
-                if (k < (unsigned)D.cells) {
-                    const unsigned row = k / (unsigned)g.nx;
-                    const int x = (int)(k - row * (unsigned)g.nx);
-                    const int y = (int)(row % (unsigned)g.ny), z = (int)(row / (unsigned)g.ny);
-                    stream_collide_cell<S, PULL, kForceSkipBand, IDX32>(fin, fout, g, c, fa, x, y, z);
-                }
-            } else {
-                const unsigned nseg = (unsigned)(g.nx + 63) / 64u;
-                const unsigned r = local / nseg;   // row z * ny + y
-                const int x0 = (int)(local - r * nseg) * 64 + 2 * lane;
-                const int y = (int)(r % (unsigned)g.ny), z = (int)(r / (unsigned)g.ny);
-                pair_body<S, PULL, kForceSkipBand, IDX32>(fin, fout, g, c, fa, x0, y, z);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int bt = b0 + (int)blockIdx.x; bt < b1; bt += (int)gridDim.x) {
+        int lo = 0, hi = p.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tb.bt0[mid] <= bt) lo = mid;
+            else hi = mid - 1;
+        }
+        const EnsMember& M = tb.m[lo];
+        const int w = (bt - tb.bt0[lo]) * kPersTileWarps + warp;   // warp tile of member lo
+        if (w >= M.wtiles) continue;                                // warp-uniform
+        const T* fin = (const T*)M.f[p.parity];
+        T* fout = (T*)M.f[p.parity ^ 1];
+        ForceArgs fa{};
+        fa.dev = M.dev;
+        fa.slot = (int)(M.dev->cur & 1);
+        if constexpr (S == CLBM_STORE_F32) {
+            const unsigned k = (unsigned)w * 32u + (unsigned)lane;
+            if (k < (unsigned)M.cells) {
+                const unsigned row = k / (unsigned)M.g.nx;
+                const int x = (int)(k - row * (unsigned)M.g.nx);
+                const int y = (int)(row % (unsigned)M.g.ny), z = (int)(row / (unsigned)M.g.ny);
+                stream_collide_cell<S, PULL, kForceSkipBand, IDX32>(fin, fout, M.g, M.c, fa, x, y, z);
             }
+        } else {
+            const unsigned nseg = (unsigned)(M.g.nx + 63) / 64u;
+            const unsigned r = (unsigned)w / nseg;   // row z * ny + y
+            const int x0 = (int)((unsigned)w - r * nseg) * 64 + 2 * lane;
+            const int y = (int)(r % (unsigned)M.g.ny), z = (int)(r / (unsigned)M.g.ny);
+            pair_body<S, PULL, kForceSkipBand, IDX32>(fin, fout, M.g, M.c, fa, x0, y, z);
         }
     }
 }
 
 template <int S, bool PULL, bool IDX32>
 __global__ void __launch_bounds__(kPersThreads, S == CLBM_STORE_F32 ? 2 : 3)
-kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
+kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p, EnsPersTable tb) {
     using T = typename Pop<S>::T;
     const int n = p.n;
     const unsigned nb = gridDim.x;
@@ -472,7 +469,7 @@ kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
             p.off_rows[n] = sr;
         }
     }
-    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[0], p.wt_split[1]);
+    pers_bulk<S, PULL, IDX32>(tb, p, p.bt_split[0], p.bt_split[1]);
     grid_barrier(p.bar, nb);
     pers_stamp(p, 2);
     // 3: band prepare over the flat list (zero the previous box, macro on the new one)
@@ -497,7 +494,7 @@ kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
             }
         }
     }
-    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[1], p.wt_split[2]);
+    pers_bulk<S, PULL, IDX32>(tb, p, p.bt_split[1], p.bt_split[2]);
     grid_barrier(p.bar, nb);
     pers_stamp(p, 3);
     // 4: interpolation and spreading, kSpreadMarkersPerWarp markers per warp
@@ -510,7 +507,7 @@ kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
                 D.a, D.g, (int)(w - __ldg(p.sw0 + i)) * kSpreadMarkersPerWarp, lane);
         }
     }
-    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[2], p.wt_split[3]);
+    pers_bulk<S, PULL, IDX32>(tb, p, p.bt_split[2], p.bt_split[3]);
     grid_barrier(p.bar, nb);
     pers_stamp(p, 4);
     // 5: force sums (virtual blocks of kPersThreads threads per member) and the box pass
@@ -555,7 +552,7 @@ kb_step_persistent(const EnsDesc* __restrict__ d, EnsPersArgs p) {
                                                       D.c, fa, xa + seg * 64 + 2 * lane, y, z);
         }
     }
-    pers_bulk<S, PULL, IDX32>(d, p, p.wt_split[3], p.wt_split[4]);
+    pers_bulk<S, PULL, IDX32>(tb, p, p.bt_split[3], p.bt_split[4]);
     pers_stamp(p, 5);
 }
 
@@ -574,7 +571,8 @@ static int pers_occupancy() {
 }
 
 template <int S, bool PULL, bool IDX32>
-static cudaError_t pers_launch(const EnsDesc* d, const EnsPersArgs& p, int grid, cudaStream_t st) {
+static cudaError_t pers_launch(const EnsDesc* d, const EnsPersArgs& p, const EnsPersTable& t, int grid,
+                               cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -585,7 +583,7 @@ static cudaError_t pers_launch(const EnsDesc* d, const EnsPersArgs& p, int grid,
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kb_step_persistent<S, PULL, IDX32>, d, p);
+    return cudaLaunchKernelEx(&cfg, kb_step_persistent<S, PULL, IDX32>, d, p, t);
 }
 
 int ens_persistent_blocks_per_sm(int storage, bool idx32) {
@@ -601,12 +599,13 @@ int ens_persistent_blocks_per_sm(int storage, bool idx32) {
 }
 
 cudaError_t launch_ens_persistent(int storage, bool pull, bool idx32, const EnsDesc* d,
-                                  const EnsPersArgs& p, int grid, cudaStream_t st) {
+                                  const EnsPersArgs& p, const EnsPersTable& t, int grid,
+                                  cudaStream_t st) {
 #define CLBM_PERS_GO(S_)                                                                  \
-    if (pull && idx32) return pers_launch<S_, true, true>(d, p, grid, st);               \
-    if (pull) return pers_launch<S_, true, false>(d, p, grid, st);                       \
-    if (idx32) return pers_launch<S_, false, true>(d, p, grid, st);                      \
-    return pers_launch<S_, false, false>(d, p, grid, st);
+    if (pull && idx32) return pers_launch<S_, true, true>(d, p, t, grid, st);            \
+    if (pull) return pers_launch<S_, true, false>(d, p, t, grid, st);                    \
+    if (idx32) return pers_launch<S_, false, true>(d, p, t, grid, st);                   \
+    return pers_launch<S_, false, false>(d, p, t, grid, st);
     if (storage == CLBM_STORE_F32) { CLBM_PERS_GO(CLBM_STORE_F32) }
     else if (storage == CLBM_STORE_F16S) { CLBM_PERS_GO(CLBM_STORE_F16S) }
     else { CLBM_PERS_GO(CLBM_STORE_BF16S) }
