@@ -303,9 +303,10 @@ void launch_ens_bulk_rows(int storage, bool pull, int threads, int rows_per_tile
 // by warp shuffles) or a run of 32 consecutive cells across row ends (float32); a block
 // takes kPersTileWarps consecutive warp tiles of one member at a time, whose constants it
 // reads from the kernel's parameter table (EnsPersTable). Every per-cell and per-marker
-// computation is the body the separate launches use; data written earlier in the launch (bands, offsets, macro fields, marker
-// positions and forces, force fields) is read with plain or L2 loads after a barrier,
-// never through the read-only path (the populations read are those of the previous step).
+// computation is the body the separate launches use; data written earlier in the launch
+// (bands, offsets, macro fields, marker positions and forces, force fields) is read with
+// plain or L2 loads after a barrier, never through the read-only path (the populations
+// read are those of the previous step).
 constexpr int kPersThreads = 256;
 constexpr int kPersWarps = kPersThreads / 32;
 constexpr int kBarrierPolls = 1 << 20;   // with 32 ns sleeps and an L2 round trip per poll: under a second
