@@ -210,6 +210,31 @@ def measure_form(pkg, torch, device, storage, closure=None, steps=200, warmup=10
             "variant": variant["variant"], "variant_autotune_us": variant["us_per_launch"]}
 
 
+def measure_plain_step(pkg, torch, device, storage, steps=200, warmup=10):
+    """MLUPS of the LBM step alone (no IBM: clbm_moving.py:326-343 without compute_force)
+    on the same 600x200x50 lattice, one fused stream-collide launch per step; CUDA events on
+    the solver stream. The speed-up of the 16-bit storage without the IBM chain beside the
+    bulk pass."""
+    cfg = pkg.full_case(storage=storage)
+    s = pkg.Solver(cfg.nx, cfg.ny, cfg.nz, cfg.s_v, cfg.s_e, cfg.ux_in, cfg.uy_in,
+                   storage=storage, device=device)
+    stream = torch.cuda.ExternalStream(s.stream_handle(), device=torch.device("cuda", device))
+    for _ in range(warmup):
+        s.step()
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    variant = s.kernel_variant()["variant"]
+    s.close()
+    return {"value": cfg.cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
+            "steps": steps, "variant": variant}
+
+
 def measure_ensemble(pkg, torch, device, storage, n=64, steps=100, warmup=4):
     """Aggregate MLUPS of the batched ensemble: n members drawn with seeds 0..n-1 (lattices
     150x60x12, 200x80x16, 300x100x24; Re, heave, pitch, phase, k uniform), stepped together
@@ -496,6 +521,11 @@ def run_gpu(args, rank, world, local):
             if name in forms:
                 forms[name]["cl_cd_error"] = form_errors(pkg, local, st, cl)
         result["cl_cd_error"] = form_errors(pkg, local, "f32")
+        # the LBM step alone (no IBM), each storage form, and its speed-up over float32
+        plain = {st: measure_plain_step(pkg, torch, local, st) for st in ("f32", "f16", "bf16")}
+        for st in ("f16", "bf16"):
+            plain[st]["speedup_vs_f32"] = plain[st]["value"] / plain["f32"]["value"]
+        result["plain_step_no_ibm"] = plain
         result["forms"] = forms
     if result is not None and not args.no_ensemble:
         result["ensemble"] = {s: measure_ensemble(pkg, torch, local, s) for s in ("f32", "f16")}
