@@ -181,3 +181,33 @@ def test_grid_barrier_timeout_is_reported(built_pkg):
     s.step()
     s.synchronize()
     s.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("form", ["launches", "persistent"])
+def test_members_without_a_body(built_pkg, monkeypatch, storage, form):
+    """Members without markers (no IBM: the plain LBM step) stepped beside members with a
+    wing, in either step form: every member gives the bits of its case stepped alone."""
+    from dataclasses import replace
+    pkg = built_pkg
+    none = np.zeros(0, np.float32)
+    cases = _cases(pkg, storage, n=4, lattices=MIXED)
+    cases[1] = replace(cases[1], X0=none, Y0=none, Z0=none)
+    cases[3] = replace(cases[3], X0=none, Y0=none, Z0=none)
+    assert [c.n_markers > 0 for c in cases] == [True, False, True, False]
+    if form == "persistent":
+        monkeypatch.setenv("CLBM_ENS_STEP", "persistent")
+    ens = pkg.Ensemble(cases)
+    monkeypatch.delenv("CLBM_ENS_STEP", raising=False)
+    assert ens.schedule()["persistent"] == (form == "persistent")
+    ens.run(20)
+    for cfg, member in zip(cases, ens.sims):
+        alone = pkg.Simulation(cfg)
+        alone.run(20)
+        np.testing.assert_array_equal(member.solver.read_populations(),
+                                      alone.solver.read_populations())
+        if cfg.n_markers:
+            np.testing.assert_allclose(member.ibm.force_history(20), alone.ibm.force_history(20),
+                                       rtol=1e-12, atol=1e-14)
+        alone.close()
+    ens.close()
