@@ -183,7 +183,8 @@ int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* b
 /* Step form of the ensemble: *persistent = 1 when each step is one persistent cooperative
  * launch (every block resident; the IBM phases separated by a grid barrier with bounded
  * waits, the bulk pass's tiles shared out over the phases), chosen by the environment
- * variable CLBM_ENS_STEP=persistent when the ensemble is created, with *blocks its grid;
+ * variable CLBM_ENS_STEP=persistent when the ensemble is created (at most 128 members:
+ * their constants travel in the launch's parameter table), with *blocks its grid;
  * 0 and 0 for the seven launches. Both forms give the same bits. A barrier wait that ran
  * out is reported by the next clbm_ensemble_run (CLBM_ERR_STATE). Any pointer may be
  * NULL. */
