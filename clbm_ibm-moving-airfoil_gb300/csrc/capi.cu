@@ -575,6 +575,32 @@ int ibm_create(clbm_solver* s, const float* X0, const float* Y0, const float* Z0
         zmin = (m == 0 || Z0[m] < zmin) ? Z0[m] : zmin;
         zmax = (m == 0 || Z0[m] > zmax) ? Z0[m] : zmax;
     }
+    // marker order of the tiled spreading: Morton code of the body-frame cell (x, y, z
+    // interleaved bit by bit, cells offset by 2^19), ties in marker order
+    if (n > 0) {
+        std::vector<unsigned long long> key(n);
+        for (int m = 0; m < n; ++m) {
+            const float v[3] = {X0[m], Y0[m], Z0[m]};
+            unsigned long long c[3];
+            for (int d = 0; d < 3; ++d) {
+                const double f = std::floor((double)v[d]) + (double)(1 << 19);
+                c[d] = (unsigned long long)std::min(std::max(f, 0.0), (double)((1 << 20) - 1));
+            }
+            unsigned long long k = 0;
+            for (int b = 19; b >= 0; --b)
+                for (int d = 0; d < 3; ++d) k = (k << 1) | ((c[d] >> b) & 1ull);
+            key[m] = k;
+        }
+        std::vector<int> perm(n);
+        for (int m = 0; m < n; ++m) perm[m] = m;
+        std::stable_sort(perm.begin(), perm.end(), [&](int p, int q) { return key[p] < key[q]; });
+        int* dperm = nullptr;
+        if (cudaMalloc(&dperm, (size_t)n * sizeof(int)) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "ibm_create: cudaMalloc failed"));
+        a.perm = dperm;
+        if (cudaMemcpy(dperm, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(CLBM_ERR_CUDA, "ibm_create: marker order upload failed"));
+    }
     const int span = (int)std::ceil(2.0 * std::sqrt(r2)) + 6;
     a.max_bx = std::min(s->g.nx, span);
     a.max_by = std::min(s->g.ny, span);
@@ -597,7 +623,7 @@ int ibm_destroy(clbm_ibm* ibm) {
     }
     IbmArrays& a = ibm->a;
     void* ptrs[] = {(void*)a.X0, (void*)a.Y0, (void*)a.Z0, a.X, a.Y, a.Z, a.VX, a.VY, a.Uk,
-                    a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist, a.part};
+                    a.Vk, a.FXk, a.FYk, a.fx, a.fy, a.dev, a.hist, a.part, (void*)a.perm};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (ibm->ev_box) cudaEventDestroy(ibm->ev_box);

@@ -329,6 +329,10 @@ struct IbmArrays {
     float *X, *Y, *Z, *VX, *VY, *Uk, *Vk, *FXk, *FYk;
     long long *fx, *fy;   // padded full grid, fixed point (kForceScale)
     float *ux, *uy;       // padded full grid (macro of the solver)
+    const int* perm;      // marker order of the tiled spreading: the markers sorted by the
+                          // Morton code of their body-frame cell (a rigid motion keeps
+                          // nearby markers nearby), so a chunk of consecutive entries is a
+                          // compact cluster; outputs stay at the markers' own indices
     IbmDev* dev;
     double* hist;
     double* part;         // per-block partials: force-sum kernel [kFinishBlocks][4]; box pass

@@ -116,14 +116,20 @@ __device__ __forceinline__ long long spread_q(float f, float w) {
 // airfoil_moving.py:142-170) and the marker force clip (airfoil_moving.py:175-183). The
 // velocity gathers of all K markers are issued before any of their sums, so a warp has K
 // times the loads in flight; the taps are kept for spreading.
-template <int K>
+// PERM: entries m0 .. m0 + K - 1 of the marker order a.perm instead of the markers
+// themselves (every output goes to the marker's own index, so the results do not depend
+// on the order).
+template <int K, bool PERM = false>
 __device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Grid& g, int m0, int lane,
                                                    MarkerTaps (&tp)[K], bool (&has)[K]) {
     float xk[K], yk[K], zk[K], vxk[K], vyk[K], us[K], vs[K], uxv[K][2], uyv[K][2];
+    int mk[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         has[k] = m0 + k < a.n;
-        const int m = has[k] ? m0 + k : 0;   // launched only with a.n >= 1
+        const int j = has[k] ? m0 + k : 0;   // launched only with a.n >= 1
+        const int m = PERM ? a.perm[j] : j;
+        mk[k] = m;
         xk[k] = a.X[m]; yk[k] = a.Y[m]; zk[k] = a.Z[m];
         vxk[k] = a.VX[m]; vyk[k] = a.VY[m];   // with the positions: one round trip less
     }
@@ -171,7 +177,7 @@ __device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Gri
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if (!has[k]) continue;
-        const int m = m0 + k;
+        const int m = mk[k];
         tp[k].fx = fmaxf(-0.05f, fminf(0.05f, -(us[k] - vxk[k])));
         tp[k].fy = fmaxf(-0.05f, fminf(0.05f, -(vs[k] - vyk[k])));
         if (lane == 0) {
@@ -206,8 +212,8 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
 }
 
 // Spreading through a shared-memory tile: a block of 8 warps takes kTileMarkers
-// consecutive markers (a body's markers are stored in surface order, so they lie close
-// together), interpolates them (four per warp, as above), accumulates their int64
+// consecutive entries of the marker order a.perm (markers sorted by their body-frame cell,
+// so they lie close together), interpolates them (four per warp, as above), accumulates their int64
 // contributions in a tile over the box their stencils cover (y, z before the wrap) and
 // adds each touched cell to the global fields once. The sums are the same integers as with
 // one global atomic per tap. A chunk whose box exceeds the tile (or spans the lattice in
@@ -224,8 +230,8 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
     __syncthreads();
     MarkerTaps tp[kTileMarkersPerWarp];
     bool has[kTileMarkersPerWarp];
-    ibm_interp_markers<kTileMarkersPerWarp>(a, g, chunk * kTileMarkers + warp * kTileMarkersPerWarp,
-                                            lane, tp, has);
+    ibm_interp_markers<kTileMarkersPerWarp, true>(a, g, chunk * kTileMarkers + warp * kTileMarkersPerWarp,
+                                                  lane, tp, has);
 #pragma unroll
     for (int i = 0; i < kTileMarkersPerWarp; ++i) {
         if (has[i]) {
