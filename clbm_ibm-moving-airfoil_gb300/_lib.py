@@ -25,6 +25,7 @@ EXPORTED = (
     "ibm_read_markers", "ibm_read_force_history", "ibm_step_count", "clbm_run",
     "clbm_synchronize", "clbm_set_rho_floor", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant", "clbm_binary_version",
+    "clbm_state_bytes", "clbm_save_state", "clbm_load_state", "ibm_load_state",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
     "clbm_ensemble_tuning", "clbm_ensemble_schedule", "clbm_ensemble_phase_times",
@@ -113,6 +114,10 @@ def lib():
             "clbm_device_bytes": [vp, ctypes.POINTER(i64)],
             "clbm_kernel_variant": [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float)],
             "clbm_binary_version": [ctypes.POINTER(i32), ctypes.POINTER(i32)],
+            "clbm_state_bytes": [vp, ctypes.POINTER(i64)],
+            "clbm_save_state": [vp, vp, i64, ctypes.POINTER(i32)],
+            "clbm_load_state": [vp, vp, i64, i32],
+            "ibm_load_state": [vp, i64, P, i32],
             "clbm_host_alloc": [i64, pvp],
             "clbm_host_free": [vp],
             "ibm_force_sums_noalloc": [P, P, i32, i32, i32, P, P, i32, vp, P],

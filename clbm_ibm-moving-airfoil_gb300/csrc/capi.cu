@@ -13,7 +13,7 @@ thread_local std::string g_err;
 constexpr double kWd[19] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
                             1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
-constexpr int kHistCap = 1 << 16;
+constexpr int kHistCap = CLBM_HISTORY_CAPACITY;
 // kernels one graph-captured step launches: markers, band-prepare, interp/spread, bulk
 // stream-collide, box stream-collide with the force sums
 constexpr int kKernelsPerIbmStep = 5;
@@ -704,6 +704,95 @@ int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out) {
         done += run;
     }
     CK(cudaStreamSynchronize(ibm->s->st));
+    return CLBM_OK;
+}
+
+int clbm_state_bytes(const clbm_solver* s, int64_t* bytes) {
+    if (!s || !bytes) return fail(CLBM_ERR_ARG, "clbm_state_bytes: null argument");
+    *bytes = (int64_t)s->g.plane * (19 * (int64_t)store_bytes(s->cfg.storage) + 4 * (int64_t)sizeof(float));
+    return CLBM_OK;
+}
+
+// State blob: the population buffer as stored (padded layout, storage form), then rho, ux,
+// uy, uz (padded layout, float32).
+int clbm_save_state(clbm_solver* s, void* out, int64_t bytes, int32_t* flags) {
+    if (!s || !out || !flags) return fail(CLBM_ERR_ARG, "clbm_save_state: null argument");
+    int64_t need = 0;
+    clbm_state_bytes(s, &need);
+    if (bytes != need)
+        return fail(CLBM_ERR_ARG, "clbm_save_state: %lld bytes given, %lld needed", (long long)bytes,
+                    (long long)need);
+    if (int rc = join_bulk(s)) return rc;
+    const size_t fb = (size_t)s->g.plane * 19 * store_bytes(s->cfg.storage);
+    const size_t mb = (size_t)s->g.plane * sizeof(float);
+    char* o = static_cast<char*>(out);
+    CK(cudaMemcpyAsync(o, s->f[s->cur], fb, cudaMemcpyDeviceToHost, s->st));
+    const float* m[4] = {s->rho, s->ux, s->uy, s->uz};
+    for (int k = 0; k < 4; ++k)
+        CK(cudaMemcpyAsync(o + fb + k * mb, m[k], mb, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    *flags = (s->local ? 1 : 0) | (s->macro_full ? 2 : 0);
+    return CLBM_OK;
+}
+
+int clbm_load_state(clbm_solver* s, const void* in, int64_t bytes, int32_t flags) {
+    if (!s || !in) return fail(CLBM_ERR_ARG, "clbm_load_state: null argument");
+    if (flags & ~3) return fail(CLBM_ERR_ARG, "clbm_load_state: unknown flags %d", flags);
+    int64_t need = 0;
+    clbm_state_bytes(s, &need);
+    if (bytes != need)
+        return fail(CLBM_ERR_ARG, "clbm_load_state: %lld bytes given, %lld needed (another lattice or "
+                    "storage form)", (long long)bytes, (long long)need);
+    if (int rc = join_bulk(s)) return rc;
+    free_graph(s);
+    const size_t fb = (size_t)s->g.plane * 19 * store_bytes(s->cfg.storage);
+    const size_t mb = (size_t)s->g.plane * sizeof(float);
+    const char* i = static_cast<const char*>(in);
+    CK(cudaMemcpyAsync(s->f[s->cur], i, fb, cudaMemcpyHostToDevice, s->st));
+    float* m[4] = {s->rho, s->ux, s->uy, s->uz};
+    for (int k = 0; k < 4; ++k)
+        CK(cudaMemcpyAsync(m[k], i + fb + k * mb, mb, cudaMemcpyHostToDevice, s->st));
+    // a new state: the monitor's record of the old one no longer applies
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st));
+    s->local = (flags & 1) != 0;
+    s->macro_full = (flags & 2) != 0;
+    s->version += 1;
+    CK(cudaStreamSynchronize(s->st));
+    return CLBM_OK;
+}
+
+int ibm_load_state(clbm_ibm* ibm, int64_t calls, const double* hist, int32_t count) {
+    if (int rc = check_bound(ibm, "ibm_load_state")) return rc;
+    if (calls < 0 || count < 0 || count > std::min<int64_t>(calls, kHistCap) || (count > 0 && !hist))
+        return fail(CLBM_ERR_ARG, "ibm_load_state: bad argument");
+    clbm_solver* s = ibm->s;
+    if (int rc = join_bulk(s)) return rc;
+    if (s->g_ibm == ibm) free_graph(s);
+    IbmArrays& a = ibm->a;
+    // a device record after `calls` completed calls, no force box, zero force fields (the
+    // next compute_force writes them), the history ring with the given entries
+    IbmDev init{};
+    init.step = calls;
+    init.cur = calls;
+    for (int sl = 0; sl < 2; ++sl)
+        for (int e = 0; e < 6; ++e) init.box[sl][e] = kBoxEmpty;
+    CK(cudaMemcpyAsync(a.dev, &init, sizeof(init), cudaMemcpyHostToDevice, s->st));
+    const size_t pb = (size_t)s->g.plane * sizeof(long long);
+    CK(cudaMemsetAsync(a.fx, 0, pb, s->st));
+    CK(cudaMemsetAsync(a.fy, 0, pb, s->st));
+    CK(cudaMemsetAsync(a.hist, 0, (size_t)kHistCap * 4 * sizeof(double), s->st));
+    int done = 0;
+    while (done < count) {
+        const long long slot = (calls - count + done) % kHistCap;
+        const int run = (int)std::min<long long>(count - done, kHistCap - slot);
+        CK(cudaMemcpyAsync(a.hist + 4 * slot, hist + 4 * (size_t)done, (size_t)run * 4 * sizeof(double),
+                           cudaMemcpyHostToDevice, s->st));
+        done += run;
+    }
+    CK(cudaStreamSynchronize(s->st));
+    ibm->calls = calls;
+    ibm->sums_pending = false;
+    ibm->box_version = -1;
     return CLBM_OK;
 }
 

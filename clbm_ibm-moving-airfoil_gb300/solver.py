@@ -212,6 +212,21 @@ class Solver:
 
     VARIANTS = ("cell", "pair", "staged")
 
+    def save_state(self):
+        """The solver's state as stored on the device (population buffer in its storage
+        form, then the macro fields) and its flags, for a checkpoint."""
+        n = ctypes.c_int64()
+        check(lib().clbm_state_bytes(self._h, ctypes.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        flags = ctypes.c_int32()
+        check(lib().clbm_save_state(self._h, _ptr(buf), n.value, ctypes.byref(flags)))
+        return buf, flags.value
+
+    def load_state(self, buf, flags):
+        """Put back a state that save_state returned (same lattice and storage form)."""
+        buf = np.ascontiguousarray(buf, np.uint8)
+        check(lib().clbm_load_state(self._h, _ptr(buf), buf.size, int(flags)))
+
     def kernel_variant(self):
         """Full-grid kernel chosen at creation and the autotune time per launch of each
         variant in microseconds (absent: not timed)."""
@@ -283,6 +298,13 @@ class IBM:
         check(lib().ibm_step_count(self._h, ctypes.byref(v)))
         return v.value
 
+    def load_state(self, calls, history):
+        """Resume at `calls` completed compute_force calls with the given history entries
+        (the last len(history) of them); the force fields are written again by the next
+        compute_force."""
+        h = np.ascontiguousarray(history, np.float64).reshape(-1, 4)
+        check(lib().ibm_load_state(self._h, int(calls), _ptr(h), h.shape[0]))
+
 
 class Simulation:
     """A SimConfig run on the GPU: solver + IBM + the driver loop."""
@@ -304,6 +326,30 @@ class Simulation:
     def coefficients(self, count=None):
         from .config import force_coefficients
         return force_coefficients(self.ibm.force_history(count), self.cfg)
+
+    def save_checkpoint(self, path):
+        """Write the run's state to `path` (.npz): the solver's stored populations and macro
+        fields, the IBM call counter (the motion law's step) and the lift/drag history.
+        load_checkpoint on a Simulation of the same case continues bit for bit."""
+        state, flags = self.solver.save_state()
+        calls = self.ibm.step_count() if self.ibm is not None else 0
+        hist = self.ibm.force_history(min(calls, 1 << 16)) if self.ibm is not None else np.zeros((0, 4))
+        np.savez(path, format=np.int32(1), lattice=np.array([self.cfg.nx, self.cfg.ny, self.cfg.nz]),
+                 storage=np.array(self.cfg.storage), markers=np.int64(self.cfg.n_markers),
+                 state=state, flags=np.int32(flags), calls=np.int64(calls), history=hist)
+
+    def load_checkpoint(self, path):
+        """Resume from a file save_checkpoint wrote for the same case."""
+        with np.load(path) as z:
+            if int(z["format"]) != 1:
+                raise ValueError(f"{path}: unknown checkpoint format {int(z['format'])}")
+            if (tuple(int(v) for v in z["lattice"]) != (self.cfg.nx, self.cfg.ny, self.cfg.nz)
+                    or str(z["storage"]) != self.cfg.storage
+                    or int(z["markers"]) != self.cfg.n_markers):
+                raise ValueError(f"{path}: a checkpoint of another case")
+            self.solver.load_state(z["state"], int(z["flags"]))
+            if self.ibm is not None:
+                self.ibm.load_state(int(z["calls"]), z["history"])
 
     def close(self):
         if self.ibm is not None:

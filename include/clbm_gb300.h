@@ -25,6 +25,9 @@ extern "C" {
 #define CLBM_ERR_DIVERGED 3 /* non-finite or rho < threshold (clbm_check, device monitor) */
 #define CLBM_ERR_STATE 4    /* call not valid in the current state */
 
+/* Entries of an IBM's lift/drag history ring (the last this many compute_force calls). */
+#define CLBM_HISTORY_CAPACITY 65536
+
 /* Population storage forms. F32 stores f_q; the shifted forms store f_q - w_q. */
 #define CLBM_STORE_F32 0
 #define CLBM_STORE_F16S 1
@@ -123,6 +126,23 @@ int ibm_read_markers(const clbm_ibm* ibm, float* out);
 int ibm_read_force_history(const clbm_ibm* ibm, int32_t count, double* out);
 /* Number of compute_force calls made on this IBM (the device step counter). */
 int ibm_step_count(const clbm_ibm* ibm, int64_t* out);
+
+/* ---- Checkpoint / resume (no counterpart: the reference's frames hold rho and u only,
+ * main_moving.py:124-200, so its runs cannot be resumed) ----------------------------------
+ * The solver's state is its population buffer as stored (padded layout, storage form) and
+ * its macro fields: clbm_state_bytes gives the size, clbm_save_state copies it to host
+ * memory with *flags (bit 0: the buffer holds a post-stream state, bit 1: the macro fields
+ * are those of that state), clbm_load_state puts it back into a solver of the same lattice
+ * and storage form. An IBM's state is its call counter and its history:
+ * ibm_load_state(ibm, calls, hist, count) sets the counter to `calls` (the motion law's
+ * step), writes the last `count` history entries (4 doubles each, as
+ * ibm_read_force_history returns them; count <= min(calls, CLBM_HISTORY_CAPACITY)) and
+ * clears the force fields, which the next compute_force writes again. A run resumed from
+ * a saved step continues bit for bit as the run that was saved. */
+int clbm_state_bytes(const clbm_solver* s, int64_t* bytes);
+int clbm_save_state(clbm_solver* s, void* out, int64_t bytes, int32_t* flags);
+int clbm_load_state(clbm_solver* s, const void* in, int64_t bytes, int32_t flags);
+int ibm_load_state(clbm_ibm* ibm, int64_t calls, const double* hist, int32_t count);
 
 /* No counterpart in the reference. Allocation-free force sums for callers that cannot call
  * cudaMalloc when they need lift/drag: real-time loops whose device memory budget is fixed

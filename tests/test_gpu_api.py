@@ -377,3 +377,38 @@ def test_loaded_device_code_is_sm_103a(gpkg):
     b, p = ctypes.c_int32(), ctypes.c_int32()
     assert gpkg.lib().clbm_binary_version(ctypes.byref(b), ctypes.byref(p)) == 0
     assert b.value == 103, (b.value, p.value)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_checkpoint_resume_is_bit_exact(gpkg, tmp_path, storage, graph):
+    """A run saved after 25 steps and resumed in a new Simulation continues bit for bit as
+    the run that was saved (populations, macro fields through the next IBM call, lift/drag
+    history, motion phase), also from a checkpoint of the initial state."""
+    cfg = gpkg.small_case(storage=storage)
+    for first in (25, 0):
+        a = gpkg.Simulation(cfg)
+        a.run(first, graph=graph)
+        path = str(tmp_path / f"ck_{storage}_{first}.npz")
+        a.save_checkpoint(path)
+        a.run(20, graph=graph)
+        b = gpkg.Simulation(cfg)
+        b.load_checkpoint(path)
+        assert b.ibm.step_count() == first
+        b.run(20, graph=graph)
+        np.testing.assert_array_equal(b.solver.read_populations(), a.solver.read_populations())
+        assert b.ibm.step_count() == a.ibm.step_count() == first + 20
+        np.testing.assert_array_equal(b.ibm.force_history(first + 20), a.ibm.force_history(first + 20))
+        a.close()
+        b.close()
+
+
+def test_checkpoint_of_another_case_is_refused(gpkg, tmp_path):
+    a = gpkg.Simulation(gpkg.small_case())
+    path = str(tmp_path / "ck.npz")
+    a.save_checkpoint(path)
+    a.close()
+    b = gpkg.Simulation(gpkg.small_case(storage="f16"))
+    with pytest.raises(ValueError):
+        b.load_checkpoint(path)
+    b.close()
