@@ -26,6 +26,7 @@ EXPORTED = (
     "clbm_synchronize", "clbm_set_rho_floor", "clbm_selftest_wait_timeout", "clbm_stream", "clbm_profile_enable", "clbm_profile_read",
     "clbm_profile_read_split", "clbm_device_bytes", "clbm_kernel_variant", "clbm_binary_version",
     "clbm_state_bytes", "clbm_save_state", "clbm_load_state", "ibm_load_state",
+    "clbm_bounds_checked", "clbm_selftest_bounds",
     "clbm_host_alloc", "clbm_host_free", "clbm_last_error", "ibm_force_sums_noalloc",
     "clbm_ensemble_create", "clbm_ensemble_run", "clbm_ensemble_stream",
     "clbm_ensemble_tuning", "clbm_ensemble_schedule", "clbm_ensemble_phase_times",
@@ -66,14 +67,15 @@ _LIB = None
 
 
 def lib_path():
-    return _build.LIB
+    """The library the package loads: the bounds-checked build when CLBM_CHECK_BUILD=1."""
+    return _build.LIB_CHECK if os.environ.get("CLBM_CHECK_BUILD") == "1" else _build.LIB
 
 
 def lib():
     """Load the CUDA library (raises if it has not been built)."""
     global _LIB
     if _LIB is None:
-        path = _build.LIB
+        path = lib_path()
         if not os.path.exists(path):
             raise RuntimeError(
                 f"CUDA library {path} is not built; run __graft_entry__.build() or "
@@ -115,6 +117,8 @@ def lib():
             "clbm_kernel_variant": [vp, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float)],
             "clbm_binary_version": [ctypes.POINTER(i32), ctypes.POINTER(i32)],
             "clbm_state_bytes": [vp, ctypes.POINTER(i64)],
+            "clbm_bounds_checked": [ctypes.POINTER(i32)],
+            "clbm_selftest_bounds": [vp],
             "clbm_save_state": [vp, vp, i64, ctypes.POINTER(i32)],
             "clbm_load_state": [vp, vp, i64, i32],
             "ibm_load_state": [vp, i64, P, i32],

@@ -17,6 +17,11 @@ LIB = os.path.join(BUILD, "libclbm_gb300.so")
 # record of the nvcc command lines that produced LIB (the target architecture is checked
 # from it on machines without a GPU)
 INFO = os.path.join(BUILD, "build_info.json")
+# the bounds-checked library (-DCLBM_CHECK): the same entry points, every population,
+# field and stencil access tested against its array first (a debug build; selected by
+# CLBM_CHECK_BUILD=1 when the package loads the library)
+BUILD_CHECK = os.path.join(HERE, "_build_check")
+LIB_CHECK = os.path.join(BUILD_CHECK, "libclbm_gb300.so")
 SOURCES = ["lbm_kernels.cu", "ibm_kernels.cu", "ensemble.cu", "closure.cu", "capi.cu", "closure_api.cu",
            "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,23 +40,27 @@ def _deps():
     return files
 
 
-def up_to_date():
-    if not os.path.exists(LIB):
+def up_to_date(lib=LIB):
+    if not os.path.exists(lib):
         return False
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force=False, verbose_ptxas=False):
-    """Compile the library unless it is newer than every source. Returns the .so path."""
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose_ptxas=False, check=False):
+    """Compile the library unless it is newer than every source. Returns the .so path.
+    check: the bounds-checked library (LIB_CHECK) instead."""
+    out_dir, lib_file = (BUILD_CHECK, LIB_CHECK) if check else (BUILD, LIB)
+    if not force and up_to_date(lib_file):
+        return lib_file
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    if check:
+        extra = extra + ["-DCLBM_CHECK"]
     procs = []
     for src in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(out_dir, src.replace(".cu", ".o"))
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), src, obj))
     objs, errors, cmds = [], [], []
@@ -65,15 +74,15 @@ def build(force=False, verbose_ptxas=False):
         objs.append(obj)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    tmp = LIB + ".tmp"
+    tmp = lib_file + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     subprocess.run(cmd, check=True)
     cmds.append(cmd)
-    with open(INFO, "w") as fh:
+    with open(os.path.join(out_dir, "build_info.json"), "w") as fh:
         json.dump({"arch": ARCH, "commands": cmds}, fh, indent=1)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_file)
+    return lib_file
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv, check="--check" in sys.argv))

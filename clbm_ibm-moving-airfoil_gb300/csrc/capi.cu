@@ -895,12 +895,15 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
             if (replays >= kReplaysInFlight) {
                 CK(cudaEventSynchronize(s->ev_replay[replays % kReplaysInFlight]));
                 const unsigned int st_word = *(volatile unsigned int*)s->h_status;
-                if (st_word & (kStatusDiverged | kStatusWaitTimeout)) {
+                if (st_word & (kStatusDiverged | kStatusWaitTimeout | kStatusBounds)) {
                     s->local = false;
                     s->macro_full = false;
                     if (st_word & kStatusWaitTimeout)
                         return fail(CLBM_ERR_STATE, "clbm_run: a device wait gave up (status %u)",
                                     st_word);
+                    if (st_word & kStatusBounds)
+                        return fail(CLBM_ERR_STATE, "clbm_run: an access outside its array was "
+                                    "caught and skipped (bounds-checked build, status %u)", st_word);
                     return fail(CLBM_ERR_DIVERGED, "clbm_run: diverged: a collision met a "
                                 "density below %g or not finite; stopped after %d of %d steps",
                                 (double)s->c.rho_floor, done, nsteps);
@@ -933,10 +936,37 @@ int clbm_synchronize(clbm_solver* s) {
     CK(cudaStreamSynchronize(s->st));
     if (status & kStatusWaitTimeout)
         return fail(CLBM_ERR_STATE, "clbm_synchronize: a device wait gave up (status %u)", status);
+    if (status & kStatusBounds)
+        return fail(CLBM_ERR_STATE, "clbm_synchronize: an access outside its array was caught and "
+                    "skipped (bounds-checked build, status %u)", status);
     if (status & kStatusDiverged)
         return fail(CLBM_ERR_DIVERGED, "clbm_synchronize: diverged: a collision met a density "
                     "below %g or not finite", (double)s->c.rho_floor);
     return CLBM_OK;
+}
+
+int clbm_bounds_checked(int32_t* on) {
+    if (!on) return fail(CLBM_ERR_ARG, "clbm_bounds_checked: null argument");
+    *on = kBoundsChecked ? 1 : 0;
+    return CLBM_OK;
+}
+
+int clbm_selftest_bounds(clbm_solver* s) {
+    if (!s) return fail(CLBM_ERR_ARG, "clbm_selftest_bounds: null solver");
+    if (!kBoundsChecked) return fail(CLBM_ERR_STATE, "clbm_selftest_bounds: not the bounds-checked build");
+    if (int rc = join_bulk(s)) return rc;
+    CK(cudaStreamSynchronize(s->st));
+    launch_bounds_selftest(s->g, s->st);
+    CK_LAUNCH();
+    s->launches += 1;
+    unsigned int status = 0;
+    CK(cudaMemcpyAsync(&status, s->status, sizeof(status), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (status & kStatusBounds)
+        return fail(CLBM_ERR_STATE, "clbm_selftest_bounds: the index test past the end was reported "
+                    "as intended (status %u)", status);
+    return fail(CLBM_ERR_CUDA, "clbm_selftest_bounds: the index test was not reported");
 }
 
 int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit) {

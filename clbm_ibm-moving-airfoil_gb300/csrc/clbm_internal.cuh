@@ -55,6 +55,26 @@ struct Grid {
 constexpr unsigned int kStatusWaitTimeout = 1u;
 // status bit: some collision met a density below the floor or a non-finite density
 constexpr unsigned int kStatusDiverged = 2u;
+// status bit of the bounds-checked build: some access tested an element index outside its
+// array
+constexpr unsigned int kStatusBounds = 4u;
+
+// Bounds-checked build (-DCLBM_CHECK, a separate library): the population, force-field,
+// macro-field and stencil accesses of the stream-collide, band and IBM bodies test their
+// element index against the array's extent first; an index outside it sets kStatusBounds
+// in the solver's status word and the access is skipped (a load gives 0) instead of
+// touching memory. In the normal build the test is the constant true and compiles away.
+#ifdef CLBM_CHECK
+constexpr bool kBoundsChecked = true;
+__device__ __forceinline__ bool in_bounds(long long i, long long n, unsigned int* status) {
+    if (i >= 0 && i < n) return true;
+    if (status) atomicOr(status, kStatusBounds);
+    return false;
+}
+#else
+constexpr bool kBoundsChecked = false;
+__device__ __forceinline__ constexpr bool in_bounds(long long, long long, unsigned int*) { return true; }
+#endif
 
 // Collision and boundary constants, rounded to float once on the host.
 struct Coef {
@@ -271,6 +291,9 @@ struct ForceArgs {
 int knob(const char* name, int def);  // integer tuning parameter from the environment
 bool spread_tiled();                  // IBM spreading through shared-memory tiles (CLBM_SPREAD)
 void launch_init(int storage, void* f, const Grid& g, const Coef& c, cudaStream_t st);
+// One index test past the end of the populations, no access (kStatusBounds in the
+// bounds-checked build).
+void launch_bounds_selftest(const Grid& g, cudaStream_t st);
 // binaryVersion / ptxVersion of the float32 bulk stream-collide kernel (cudaFuncGetAttributes).
 cudaError_t stream_collide_binary_version(int* binary, int* ptx);
 // Stream-collide kernel variants for the full-grid pass:

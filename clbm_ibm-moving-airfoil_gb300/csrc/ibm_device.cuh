@@ -150,8 +150,9 @@ __device__ __forceinline__ void ibm_interp_markers(const IbmArrays& a, const Gri
             tp[k].ii[h] = ii;
             tp[k].jr[h] = jb + dj;
             tp[k].kr[h] = kb + dk;
-            uxv[k][h] = (w != 0.0f) ? a.ux[c] : 0.0f;
-            uyv[k][h] = (w != 0.0f) ? a.uy[c] : 0.0f;
+            const bool ok = w != 0.0f && in_bounds(c, g.plane, g.status);
+            uxv[k][h] = ok ? a.ux[c] : 0.0f;
+            uyv[k][h] = ok ? a.uy[c] : 0.0f;
         }
     }
 #pragma unroll
@@ -204,6 +205,7 @@ __device__ __forceinline__ void ibm_interp_spread_body(const IbmArrays& a, const
         for (int h = 0; h < 2; ++h) {
             if (tp[k].wt[h] != 0.0f) {
                 const long long c = ((long long)pmod(tp[k].kr[h], g.nz) * g.ny + pmod(tp[k].jr[h], g.ny)) * g.pitch + tp[k].ii[h];
+                if (!in_bounds(c, g.plane, g.status)) continue;
                 red_add(a.fx + c, spread_q(tp[k].fx, tp[k].wt[h]));
                 red_add(a.fy + c, spread_q(tp[k].fy, tp[k].wt[h]));
             }
@@ -260,6 +262,7 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
             for (int h = 0; h < 2; ++h) {
                 if (tp[i].wt[h] != 0.0f) {
                     const long long c = ((long long)pmod(tp[i].kr[h], g.nz) * g.ny + pmod(tp[i].jr[h], g.ny)) * g.pitch + tp[i].ii[h];
+                    if (!in_bounds(c, g.plane, g.status)) continue;
                     red_add(a.fx + c, spread_q(tp[i].fx, tp[i].wt[h]));
                     red_add(a.fy + c, spread_q(tp[i].fy, tp[i].wt[h]));
                 }
@@ -293,6 +296,7 @@ __device__ __forceinline__ void ibm_interp_spread_tiled_body(const IbmArrays& a,
         const int r = t / li;
         const int y = pmod(j0 + r % lj, g.ny), z = pmod(k0 + r / lj, g.nz);
         const long long c = ((long long)z * g.ny + y) * g.pitch + x;
+        if (!in_bounds(c, g.plane, g.status)) continue;
         if (vx) red_add(a.fx + c, vx);
         if (vy) red_add(a.fy + c, vy);
     }

@@ -55,8 +55,11 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
     if (!PULL) {
         const I cell = ((I)z * (I)g.ny + (I)y) * (I)g.pitch + (I)x;
 #pragma unroll
-        for (int q = 0; q < 19; ++q)
-            v[q] = kRaw ? P::ld_raw(f + ((I)q * plane + cell)) : P::ld(f + ((I)q * plane + cell), q);
+        for (int q = 0; q < 19; ++q) {
+            const I e = (I)q * plane + cell;
+            v[q] = !in_bounds((long long)e, 19LL * g.plane, g.status) ? 0.0f
+                   : kRaw ? P::ld_raw(f + e) : P::ld(f + e, q);
+        }
         return;
     }
     const int xe = (x == g.nx - 1) ? g.nx - 2 : x;  // outlet: copy of column Nx-2
@@ -72,8 +75,9 @@ __device__ __forceinline__ void gather(const typename Pop<S>::T* __restrict__ f,
         if (ex(q) == 1 && xe == 0) {
             v[q] = 0.0f;  // inlet unknown, rebuilt by Zou-He below
         } else {
-            const typename P::T* p = f + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)sx);
-            v[q] = kRaw ? P::ld_raw(p) : P::ld(p, q);
+            const I e = (I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)sx;
+            v[q] = !in_bounds((long long)e, 19LL * g.plane, g.status) ? 0.0f
+                   : kRaw ? P::ld_raw(f + e) : P::ld(f + e, q);
         }
     }
     if (xe == 0) {
@@ -95,7 +99,10 @@ __device__ __forceinline__ void store_raw(typename Pop<S>::T* __restrict__ f, co
                                           long long cell, const float (&v)[19]) {
     using I = typename std::conditional<IDX32, unsigned, long long>::type;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Pop<S>::st_raw(f + ((I)q * (I)g.plane + (I)cell), v[q]);
+    for (int q = 0; q < 19; ++q) {
+        const I e = (I)q * (I)g.plane + (I)cell;
+        if (in_bounds((long long)e, 19LL * g.plane, g.status)) Pop<S>::st_raw(f + e, v[q]);
+    }
 }
 
 // Zeroth, first and second raw moments of a population vector.
@@ -717,7 +724,8 @@ __device__ __forceinline__ void pair_boundaries(const typename Pair<S>::T* __res
         for (int q = 0; q < 19; ++q) {
             const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
             const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-            h0[q] = P::ld1(fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)(xe - ex(q))));
+            const I e = (I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch + (I)(xe - ex(q));
+            h0[q] = in_bounds((long long)e, 19LL * g.plane, g.status) ? P::ld1(fin + e) : 0.0f;
         }
     }
 }
@@ -756,11 +764,11 @@ __device__ __forceinline__ void pair_finish(typename Pair<S>::T* __restrict__ fo
     if (FMODE == kForceBand || FMODE == kForceOnlyBand) {
         frc0 = in0;
         frc1 = in1;
-        if (in0) {
+        if (in0 && in_bounds((long long)(row + x0), g.plane, g.status)) {
             F0x = fminf(fmaxf(qforce(fa.qx[row + x0]), -0.05f), 0.05f);
             F0y = fminf(fmaxf(qforce(fa.qy[row + x0]), -0.05f), 0.05f);
         }
-        if (in1) {
+        if (in1 && in_bounds((long long)(row + x0 + 1), g.plane, g.status)) {
             F1x = fminf(fmaxf(qforce(fa.qx[row + x0 + 1]), -0.05f), 0.05f);
             F1y = fminf(fmaxf(qforce(fa.qy[row + x0 + 1]), -0.05f), 0.05f);
         }
@@ -780,17 +788,27 @@ __device__ __forceinline__ void pair_finish(typename Pair<S>::T* __restrict__ fo
         }
     }
     collide_pair<true>(h0, h1, c, use0, use1, frc0, frc1, F0x, F0y, F0z, F1x, F1y, F1z);
+    const long long nel = 19LL * g.plane;
     if (use0 && use1) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) P::st2(fout + ((I)q * plane + row + (I)x0), h0[q], h1[q]);
+        for (int q = 0; q < 19; ++q) {
+            const I e = (I)q * plane + row + (I)x0;
+            if (in_bounds((long long)e + 1, nel, g.status)) P::st2(fout + e, h0[q], h1[q]);
+        }
     } else {
         if (use0) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) P::st1(fout + ((I)q * plane + row + (I)x0), h0[q]);
+            for (int q = 0; q < 19; ++q) {
+                const I e = (I)q * plane + row + (I)x0;
+                if (in_bounds((long long)e, nel, g.status)) P::st1(fout + e, h0[q]);
+            }
         }
         if (use1) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) P::st1(fout + ((I)q * plane + row + (I)x0 + 1), h1[q]);
+            for (int q = 0; q < 19; ++q) {
+                const I e = (I)q * plane + row + (I)x0 + 1;
+                if (in_bounds((long long)e, nel, g.status)) P::st1(fout + e, h1[q]);
+            }
         }
     }
 }
@@ -818,7 +836,9 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
     if (!PULL) {
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
-            const float2 p = P::ld2(fin + ((I)q * plane + row + (I)x0c));
+            const I e = (I)q * plane + row + (I)x0c;
+            const float2 p = in_bounds((long long)e + 1, 19LL * g.plane, g.status) ? P::ld2(fin + e)
+                                                                                  : make_float2(0.f, 0.f);
             h0[q] = p.x;
             h1[q] = p.y;
         }
@@ -831,19 +851,25 @@ __device__ __forceinline__ void pair_body(const typename Pair<S>::T* __restrict_
         for (int q = 0; q < 19; ++q) {
             const int sy = ey(q) == 1 ? ym : (ey(q) == -1 ? yp : y);
             const int sz = ez(q) == 1 ? zm : (ez(q) == -1 ? zp : z);
-            const typename P::T* rp = fin + ((I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch);
-            const float2 p = P::ld2(rp + x0c);
+            const I rb = (I)q * plane + ((I)sz * (I)g.ny + (I)sy) * (I)g.pitch;
+            const typename P::T* rp = fin + rb;
+            const float2 p = in_bounds((long long)(rb + (I)x0c) + 1, 19LL * g.plane, g.status)
+                                 ? P::ld2(rp + x0c) : make_float2(0.f, 0.f);
             if (ex(q) == 0) {
                 h0[q] = p.x;
                 h1[q] = p.y;
             } else if (ex(q) == 1) {  // pull from x - 1
                 float up = __shfl_up_sync(kFull, p.y, 1);
-                if (lane == 0) up = (x0 >= 1 && x0 - 1 < g.nx) ? P::ld1(rp + (x0 - 1)) : 0.0f;
+                if (lane == 0)
+                    up = (x0 >= 1 && x0 - 1 < g.nx && in_bounds((long long)(rb + (I)(x0 - 1)), 19LL * g.plane, g.status))
+                             ? P::ld1(rp + (x0 - 1)) : 0.0f;
                 h0[q] = up;   // at x0 = 0 an inlet unknown, rebuilt by Zou-He below
                 h1[q] = p.x;
             } else {                  // pull from x + 1
                 float dn = __shfl_down_sync(kFull, p.x, 1);
-                if (lane == 31) dn = (x0 + 2 < g.nx) ? P::ld1(rp + (x0 + 2)) : 0.0f;
+                if (lane == 31)
+                    dn = (x0 + 2 < g.nx && in_bounds((long long)(rb + (I)(x0 + 2)), 19LL * g.plane, g.status))
+                             ? P::ld1(rp + (x0 + 2)) : 0.0f;
                 h0[q] = p.y;
                 h1[q] = dn;
             }
@@ -878,15 +904,17 @@ __device__ __forceinline__ void stream_collide_cell(const typename Pop<S>::T* __
     if (FMODE == kForceNone || FMODE == kForceSkipBand) {
         collide<false, DEV>(f, c, 0.f, 0.f, 0.f);
     } else if (FMODE == kForceDense) {
-        const float Fz = fa.fz ? fa.fz[cell] : 0.0f;
-        collide<true, DEV>(f, c, fa.fx[cell], fa.fy[cell], Fz);
+        const bool ok = in_bounds(cell, g.plane, g.status);
+        const float Fz = (fa.fz && ok) ? fa.fz[cell] : 0.0f;
+        collide<true, DEV>(f, c, ok ? fa.fx[cell] : 0.0f, ok ? fa.fy[cell] : 0.0f, Fz);
     } else {
         const Band b = load_band(fa.dev, fa.slot);
         if (in_band(b, x, y, z, g.ny, g.nz)) {
             // Eulerian clip of _clip_forces (airfoil_moving.py:219-225) applied on read;
             // fz is always zero there.
-            const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
-            const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+            const bool ok = in_bounds(cell, g.plane, g.status);
+            const float Fx = ok ? fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f) : 0.0f;
+            const float Fy = ok ? fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f) : 0.0f;
             if (FMODE == kForceOnlyBand && ks) {
                 ks[0] += (long long)(Fx * kForceScale);
                 ks[1] += (long long)(Fy * kForceScale);
@@ -915,8 +943,9 @@ __device__ __forceinline__ void box_pass_cell(const typename Pop<S>::T* __restri
     float f[19];
     gather<S, PULL, true>(fin, g, c, x, y, z, f);
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
-    const float Fx = fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f);
-    const float Fy = fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f);
+    const bool ok = in_bounds(cell, g.plane, g.status);
+    const float Fx = ok ? fminf(fmaxf(qforce(fa.qx[cell]), -0.05f), 0.05f) : 0.0f;
+    const float Fy = ok ? fminf(fmaxf(qforce(fa.qy[cell]), -0.05f), 0.05f) : 0.0f;
     if (SUMS) {
         *kx += (long long)(Fx * kForceScale);
         *ky += (long long)(Fy * kForceScale);
@@ -945,6 +974,7 @@ __device__ __forceinline__ void band_zero_cell(const Grid& g, long long* fx, lon
     int x, y, z;
     box_cell(ob, g.ny, g.nz, t, x, y, z);
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    if (!in_bounds(cell, g.plane, g.status)) return;
     fx[cell] = 0;
     fy[cell] = 0;
 }
@@ -966,6 +996,7 @@ __device__ __forceinline__ void band_macro_cell(const typename Pop<S>::T* __rest
         mz += (float)ez(q) * f[q];
     }
     const long long cell = ((long long)z * g.ny + y) * g.pitch + x;
+    if (!in_bounds(cell, g.plane, g.status)) return;
     rho[cell] = r;
     ux[cell] = mx / r;
     uy[cell] = my / r;

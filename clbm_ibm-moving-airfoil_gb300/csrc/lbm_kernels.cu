@@ -554,6 +554,14 @@ static int macro_full_blocks() {
         default: { constexpr int S_ = CLBM_STORE_BF16S; __VA_ARGS__; } break;             \
     }
 
+// Bounds-check self test: one index test just past the end of the populations (no access),
+// which in the bounds-checked build sets kStatusBounds.
+__global__ void k_bounds_selftest(Grid g) {
+    if (threadIdx.x == 0) (void)in_bounds(19LL * g.plane, 19LL * g.plane, g.status);
+}
+
+void launch_bounds_selftest(const Grid& g, cudaStream_t st) { k_bounds_selftest<<<1, 32, 0, st>>>(g); }
+
 // Architecture the bulk stream-collide kernel was compiled for, as the CUDA runtime reports
 // it (major * 10 + minor of the SASS it loaded), and its PTX version.
 cudaError_t stream_collide_binary_version(int* binary, int* ptx) {

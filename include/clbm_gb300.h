@@ -238,6 +238,17 @@ int clbm_set_rho_floor(clbm_solver* s, double rho_floor);
  * unchanged (no block writes results) and clears the status word. */
 int clbm_selftest_wait_timeout(clbm_solver* s, int32_t spin_limit);
 
+/* Bounds-checked build (the same library compiled with -DCLBM_CHECK, a debug build for
+ * finding out-of-range accesses without a sanitizer): the population, force-field,
+ * macro-field and stencil accesses of the stream-collide, band and IBM kernels test their
+ * index first; one outside its array is skipped and reported by clbm_synchronize
+ * (CLBM_ERR_STATE). clbm_bounds_checked tells which build is loaded (*on = 1: checked);
+ * clbm_selftest_bounds makes one index test past the end (no access) and returns
+ * CLBM_ERR_STATE when it was reported (the expected outcome; CLBM_ERR_STATE also in the
+ * normal build, where there is nothing to test). */
+int clbm_bounds_checked(int32_t* on);
+int clbm_selftest_bounds(clbm_solver* s);
+
 /* Failure-detection self test of the persistent ensemble step's grid barrier: a
  * cooperative launch of `blocks` (1..16) blocks whose barrier waits for one block more than
  * the launch has, so every block's bounded wait gives up (well under a second) and sets the

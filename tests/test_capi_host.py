@@ -61,3 +61,17 @@ def test_invalid_configuration_is_rejected(built_pkg):
     assert ei.value.code == 2
     with pytest.raises(ValueError):
         built_pkg.Solver(16, 8, 4, 1.5, storage="fp8")
+
+
+def test_normal_build_is_not_the_bounds_checked_one(built_pkg, monkeypatch):
+    """The library the package loads by default has no index tests on its hot paths (they
+    are in the separate -DCLBM_CHECK library, selected by CLBM_CHECK_BUILD=1)."""
+    monkeypatch.delenv("CLBM_CHECK_BUILD", raising=False)
+    import importlib
+    b = importlib.import_module(built_pkg.__name__ + ".build")
+    assert built_pkg.lib_path() == b.LIB
+    v = ctypes.c_int32(-1)
+    assert built_pkg.lib().clbm_bounds_checked(ctypes.byref(v)) == 0
+    assert v.value == 0
+    monkeypatch.setenv("CLBM_CHECK_BUILD", "1")
+    assert built_pkg.lib_path().endswith(os.path.join("_build_check", "libclbm_gb300.so"))
