@@ -339,6 +339,75 @@ def fish_case(storage="f32"):
                      X0=X, Y0=Y, Z0=Z)
 
 
+# D3Q19 velocities in the reference's population order (clbm_moving.py:21-30) and the raw
+# moments e_x^p e_y^q e_z^r of M_raw in its row order (config_moving.py:62-68): the same
+# tables as csrc/clbm_internal.cuh (ex, ey, ez) and csrc/closure_device.cuh (pqr_code).
+D3Q19_E = np.array([(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1),
+                    (0, 0, -1), (1, 1, 0), (-1, 1, 0), (1, -1, 0), (-1, -1, 0), (1, 0, 1),
+                    (-1, 0, 1), (1, 0, -1), (-1, 0, -1), (0, 1, 1), (0, -1, 1), (0, 1, -1),
+                    (0, -1, -1)], np.int64)
+MOMENT_PQR = ((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (1, 1, 0), (1, 0, 1), (0, 1, 1),
+              (2, 0, 0), (0, 2, 0), (0, 0, 2), (2, 1, 0), (1, 2, 0), (2, 0, 1), (0, 2, 1),
+              (1, 0, 2), (0, 1, 2), (2, 2, 0), (2, 0, 2), (0, 2, 2))
+
+
+def raw_moment_matrices():
+    """M_raw (19 x 19, rows the moments of MOMENT_PQR, columns the populations) and its
+    inverse as float32; every entry of the inverse is 0, +-1/4, +-1/2 or +-1, so the float32
+    values are exact."""
+    e = D3Q19_E
+    m = np.array([[float(e[q, 0] ** p * e[q, 1] ** r1 * e[q, 2] ** r2) for q in range(19)]
+                  for (p, r1, r2) in MOMENT_PQR])
+    inv = np.round(np.linalg.inv(m) * 4.0) / 4.0
+    assert np.allclose(inv @ m, np.eye(19), atol=1e-12)
+    return m, inv.astype(np.float32)
+
+
+def to_config_module(cfg, n_steps=1000, vis_interval=100, data_dir="data_moving",
+                     name="config_moving"):
+    """A ``config_moving``-style module for `cfg`: every name the reference's
+    clbm_moving.py (:15-16), airfoil_moving.py (:17-19) and main_moving.py (:42-54) import,
+    so the reference's driver runs this case through the drop-in modules
+    (``sys.modules["config_moving"] = to_config_module(cfg)``, as main_highRe.py:26-27 selects
+    its configuration). Body dimensions and templates the case does not have are zeros and
+    empty arrays (they only go into meta.npz)."""
+    import types
+    mod = types.ModuleType(name)
+    mod.Nx, mod.Ny, mod.Nz = int(cfg.nx), int(cfg.ny), int(cfg.nz)
+    mod.c = float(cfg.chord)
+    mod.U_inf, mod.Re = float(cfg.u_inf), float(cfg.re)
+    mod.cs2 = 1.0 / 3.0
+    mod.nu, mod.tau = cfg.nu, cfg.tau
+    mod.s_v, mod.s_e, mod.s_q, mod.s_pi = cfg.s_v, float(cfg.s_e), 1.0, 1.0
+    mod.AoA0_deg = float(cfg.inflow_deg)
+    mod.M_raw_np, mod.M_raw_inv_np = raw_moment_matrices()
+    mod.x0, mod.y0, mod.z0 = float(cfg.x0), float(cfg.y0), float(cfg.nz) / 2.0
+    mod.f_motion = cfg.f_motion
+    mod.omega = cfg.omega_motion
+    mod.k_reduced = float(cfg.k_reduced)
+    mod.A_heave, mod.A_pitch = float(cfg.a_heave), float(cfg.a_pitch)
+    mod.phi_pitch, mod.AoA0_rad = float(cfg.phi_pitch), float(cfg.aoa0)
+    geo = dict(fuse_ax=0.0, fuse_ay=0.0, fuse_az=0.0, b_half=0.0, z_wing_start=0.0,
+               z_wing_end=float(cfg.nz), x_tail_arm=0.0, c_htail=0.0, b_half_htail=0.0,
+               z_htail_start=0.0, z_htail_end=0.0, c_vtail=0.0, h_vtail=0.0)
+    geo.update(cfg.geometry or {})
+    for k, v in geo.items():
+        setattr(mod, k, v)
+    empty = np.zeros(0, np.float32)
+    tmpl = dict(X_template=empty, Y_template=empty, X_htail_tmpl=empty, Y_htail_tmpl=empty)
+    tmpl.update(cfg.templates or {})
+    for k, v in tmpl.items():
+        setattr(mod, k, np.asarray(v, np.float32))
+    X0 = cfg.X0 if cfg.X0 is not None else empty
+    mod.X_marker_np = np.asarray(X0, np.float32)
+    mod.Y_marker_np = np.asarray(cfg.Y0 if cfg.Y0 is not None else empty, np.float32)
+    mod.Z_marker_np = np.asarray(cfg.Z0 if cfg.Z0 is not None else empty, np.float32)
+    mod.N_MARKERS = int(len(X0))
+    mod.N_MARKERS_2D = int(len(mod.X_template)) if len(mod.X_template) else mod.N_MARKERS
+    mod.N_steps, mod.vis_interval, mod.DATA_DIR = int(n_steps), int(vis_interval), str(data_dir)
+    return mod
+
+
 def from_config_module(mod, storage="f32"):
     """Build a SimConfig from a ``config_moving``-style module (the names the reference's
     clbm_moving.py, airfoil_moving.py and main_moving.py import)."""

@@ -181,3 +181,28 @@ def test_fish_dropin_modules_against_oracle(built_pkg, oracle_mod, dropin_env):
     assert rel_l2(np.stack([got["ux"], got["uy"], got["uz"]]), np.stack([ux, uy, uz])) < 1e-5
     assert ibm.X_marker.to_numpy().shape == (cfg_mod.N_MARKERS,)
     lbm._solver.close()
+
+
+def test_dropin_modules_under_a_generated_configuration(built_pkg, dropin_env):
+    """config.to_config_module makes any case of this package a ``config_moving``: the
+    drop-in CLBMSolver / DroneMovingIBM loaded under the module generated for a small wing,
+    called as main_moving.py calls them (compute_force with the host motion law, then step),
+    give the bits of Simulation.step_host_motion on the same case."""
+    cfg = built_pkg.wing_case(96, 40, 6, 16, name="wing-96x40x6")
+    sys.modules["config_moving"] = built_pkg.config.to_config_module(cfg)
+    clbm_moving = importlib.import_module("clbm_moving")
+    airfoil_moving = importlib.import_module("airfoil_moving")
+    assert clbm_moving.__file__.startswith(COMPAT)
+    lbm = clbm_moving.CLBMSolver()
+    ibm = airfoil_moving.DroneMovingIBM()
+    sim = built_pkg.Simulation(cfg)
+    for step in range(1, 16):
+        fx, fy, fz = ibm.compute_force(lbm.ux, lbm.uy, *cfg.motion_state(step))
+        lbm.step(fx, fy, fz)
+        sim.step_host_motion(step)
+    got = {k: getattr(lbm, k).to_numpy() for k in FIELDS}
+    want = sim.solver.read_macro()
+    for k in FIELDS:
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    np.testing.assert_array_equal(lbm.f.to_numpy(), sim.solver.read_populations())
+    sim.close()
