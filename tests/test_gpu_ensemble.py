@@ -211,3 +211,25 @@ def test_members_without_a_body(built_pkg, monkeypatch, storage, form):
                                        rtol=1e-12, atol=1e-14)
         alone.close()
     ens.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_member_checkpoint_resumes_alone(built_pkg, tmp_path, storage):
+    """A member checkpointed after ensemble steps and resumed as a single Simulation
+    continues with the bits of the same member stepped on in the ensemble."""
+    pkg = built_pkg
+    cases = _cases(pkg, storage, n=3)
+    ens = pkg.Ensemble(cases)
+    ens.run(16)
+    path = str(tmp_path / "member1.npz")
+    ens.sims[1].save_checkpoint(path)
+    ens.run(12)
+    alone = pkg.Simulation(cases[1])
+    alone.load_checkpoint(path)
+    assert alone.ibm.step_count() == 16
+    alone.run(12)
+    np.testing.assert_array_equal(alone.solver.read_populations(), ens.sims[1].solver.read_populations())
+    np.testing.assert_allclose(alone.ibm.force_history(28), ens.sims[1].ibm.force_history(28),
+                               rtol=1e-12, atol=1e-14)
+    alone.close()
+    ens.close()
