@@ -233,3 +233,30 @@ def test_member_checkpoint_resumes_alone(built_pkg, tmp_path, storage):
                                rtol=1e-12, atol=1e-14)
     alone.close()
     ens.close()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_ensemble_at_the_stated_horizon(built_pkg, storage):
+    """The 64-member ensemble (lattices 150x60x12, 200x80x16, 300x100x24) for the 5,000
+    steps its configuration states, graph-replayed: no member's divergence monitor fires,
+    and the first member of each lattice still has the bits of its case stepped alone."""
+    pkg = built_pkg
+    cases = [pkg.config.ensemble_case(seed, storage=storage) for seed in range(64)]
+    steps = 5000
+    ens = pkg.Ensemble(cases)
+    ens.run(steps)
+    ens.synchronize()   # raises if a member's monitor saw a non-finite or too low density
+    firsts = {}
+    for i, c in enumerate(cases):
+        firsts.setdefault((c.nx, c.ny, c.nz), i)
+    for i in sorted(firsts.values()):
+        alone = pkg.Simulation(cases[i])
+        alone.run(steps)
+        np.testing.assert_array_equal(ens.sims[i].solver.read_populations(),
+                                      alone.solver.read_populations(), err_msg=f"member {i}")
+        assert ens.sims[i].ibm.step_count() == steps
+        alone.close()
+    for m in ens.sims:
+        cl = m.coefficients(100)
+        assert np.all(np.isfinite(cl["cl"])) and np.all(np.isfinite(cl["cd"]))
+    ens.close()
