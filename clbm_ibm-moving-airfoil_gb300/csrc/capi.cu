@@ -1152,6 +1152,13 @@ struct clbm_ensemble {
     // the short launches of the small groups fill each other's ramp-up and tail)
     std::vector<cudaStream_t> gst;
     std::vector<cudaEvent_t> gev;   // [0]: fork; [1 + k]: end of group k + 1
+    // bulk pass as one single-lattice stream-collide launch per member (members = true when
+    // the autotuner chose it): members in order of size, round-robin over kMemberStreams
+    // concurrent streams
+    bool members = false;
+    std::vector<int> morder;
+    std::vector<cudaStream_t> mst;
+    std::vector<cudaEvent_t> mev;   // [0]: fork; [1 + k]: end of stream k
     float bulk_ms = 0.f;     // time of one bulk pass of the chosen schedule at creation
     int max_marker_blocks = 0, max_spread_blocks = 0;
     int cur = 0;
@@ -1278,6 +1285,62 @@ int ens_bulk_rows(clbm_ensemble* e, bool pull, cudaStream_t st) {
     return CLBM_OK;
 }
 
+constexpr int kMemberStreams = 8;
+
+// Streams and order of the per-member bulk launches.
+int ens_members_setup(clbm_ensemble* e) {
+    if (!e->mst.empty()) return CLBM_OK;
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    const int k = std::min(kMemberStreams, e->n);
+    for (int i = 0; i < k; ++i) {
+        cudaStream_t st;
+        CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lo));
+        e->mst.push_back(st);
+    }
+    for (int i = 0; i <= k; ++i) {
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        e->mev.push_back(ev);
+    }
+    e->morder.resize(e->n);
+    for (int i = 0; i < e->n; ++i) e->morder[i] = i;
+    std::stable_sort(e->morder.begin(), e->morder.end(), [&](int a, int b) {
+        return (long long)e->s[a]->g.nx * e->s[a]->g.ny * e->s[a]->g.nz >
+               (long long)e->s[b]->g.nx * e->s[b]->g.ny * e->s[b]->g.nz;
+    });
+    return CLBM_OK;
+}
+
+// The bulk pass as one launch of the single-lattice stream-collide kernel per member (the
+// one-cell kernel in float32, the two-cell kernel in the 16-bit forms), skipping the
+// member's force box, forked from st over the member streams and joined back into it.
+int ens_bulk_members(clbm_ensemble* e, bool pull, cudaStream_t st) {
+    const int k = (int)e->mst.size();
+    CK(cudaEventRecord(e->mev[0], st));
+    for (int j = 0; j < k; ++j) CK(cudaStreamWaitEvent(e->mst[j], e->mev[0], 0));
+    const int variant = e->storage == CLBM_STORE_F32 ? kVariantCell : kVariantPair;
+    for (int r = 0; r < e->n; ++r) {
+        const int i = e->morder[r];
+        const clbm_solver* s = e->s[i];
+        const clbm_ibm* b = e->ibm[i];
+        ForceArgs fa{};
+        int fmode = kForceNone;
+        if (b) {
+            fa.dev = b->a.dev;
+            fa.slot = -1;   // the member's current call, read on the device
+            fmode = kForceSkipBand;
+        }
+        launch_stream_collide(e->storage, pull, fmode, variant, s->f[e->cur], s->f[e->cur ^ 1], s->g,
+                              s->c, fa, e->mst[r % k]);
+    }
+    for (int j = 0; j < k; ++j) {
+        CK(cudaEventRecord(e->mev[1 + j], e->mst[j]));
+        CK(cudaStreamWaitEvent(st, e->mev[1 + j], 0));
+    }
+    return CLBM_OK;
+}
+
 // Device descriptors for tile width bx; returns the number of bulk tiles.
 int ens_upload(clbm_ensemble* e, int bx) {
     std::vector<EnsDesc> h(e->n);
@@ -1373,6 +1436,27 @@ int ens_tune(clbm_ensemble* e) {
         if (int rc = ens_groups(e, best_r)) return rc;
         e->rows = true;
         e->bulk_ms = best_rows / 3.0f;
+    }
+    // one single-lattice launch per member over concurrent streams; CLBM_ENS_MEMBERS=1 / 0
+    // forces / forbids it (tests), otherwise kept when faster than the schedule above
+    const int force_m = knob("CLBM_ENS_MEMBERS", -1);
+    if (force_m != 0 && force != 1) {
+        if (int rc = ens_members_setup(e)) return rc;
+        if (int rc = ens_bulk_members(e, true, e->st)) return rc;
+        CK(cudaEventRecord(e0, e->st));
+        for (int k = 0; k < 3; ++k)
+            if (int rc = ens_bulk_members(e, true, e->st)) return rc;
+        CK(cudaEventRecord(e1, e->st));
+        CK(cudaEventSynchronize(e1));
+        CK_LAUNCH();
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        e->launches += 4LL * e->n;
+        if (force_m == 1 || ms / 3.0f < e->bulk_ms) {
+            e->members = true;
+            e->rows = false;
+            e->bulk_ms = ms / 3.0f;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1479,6 +1563,13 @@ int ens_pers_check(clbm_ensemble* e, const char* who) {
                 "(bits %u); the members' state is not valid", who, err);
 }
 
+// Kernel launches of one ensemble step: the six of the IBM chain and the box pass, and the
+// bulk pass's (one, one per row-width group, or one per member); one for the persistent step.
+long long ens_step_launches(const clbm_ensemble* e) {
+    if (e->pers) return 1;
+    return 6 + (e->members ? e->n : e->rows ? (long long)e->groups.size() : 1);
+}
+
 int ens_step(clbm_ensemble* e) {
     const bool pull = !e->local;
     if (e->pers) {
@@ -1505,7 +1596,9 @@ int ens_step(clbm_ensemble* e) {
     launch_ens_interp_spread(e->d_desc, e->n, e->max_spread_blocks, e->st);
     launch_ens_finish(e->d_desc, e->n, e->st);
     CK(cudaStreamWaitEvent(e->st2, e->ev_box, 0));
-    if (e->rows) {
+    if (e->members) {
+        if (int rc = ens_bulk_members(e, pull, e->st2)) return rc;
+    } else if (e->rows) {
         if (int rc = ens_bulk_rows(e, pull, e->st2)) return rc;
     } else launch_ens_bulk(e->storage, pull, e->bx, e->d_desc, e->d_tile0, e->n, e->ntiles, e->cur,
                          e->grid, e->st2);
@@ -1513,7 +1606,7 @@ int ens_step(clbm_ensemble* e) {
     launch_ens_box_flat(e->storage, pull, e->d_desc, e->n, off_new, e->cur, e->flat_grid, e->st);
     CK(cudaStreamWaitEvent(e->st, e->ev_bulk, 0));
     CK_LAUNCH();
-    e->launches += 7;
+    e->launches += ens_step_launches(e);
     e->cur ^= 1;
     e->local = false;
     e->macro_full = false;
@@ -1651,7 +1744,7 @@ int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph) {
         while (nsteps - done >= 2) {
             CK(cudaGraphLaunch(e->gexec, e->st));
             done += 2;
-            e->launches += e->pers ? 2 : 12;
+            e->launches += 2 * ens_step_launches(e);
         }
     }
     while (done < nsteps) {
@@ -1686,6 +1779,13 @@ int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* b
     if (rows_per_block) *rows_per_block = e->rows ? e->rows_per_tile : 0;
     long long rows = 0;
     for (const auto& G : e->groups) rows += G.ntiles;
+    if (e->members) {   // one launch per member
+        if (tile_width) *tile_width = -1;
+        if (blocks) *blocks = e->n;
+        if (tiles) *tiles = e->n;
+        if (bulk_ms) *bulk_ms = e->bulk_ms;
+        return CLBM_OK;
+    }
     if (tile_width) *tile_width = e->rows ? 0 : e->bx;
     if (blocks) *blocks = e->rows ? (int)std::min<long long>(rows, 1LL << 30) : e->grid;
     if (tiles) *tiles = e->rows ? rows : e->ntiles;
@@ -1742,6 +1842,8 @@ int clbm_ensemble_destroy(clbm_ensemble* e) {
     ens_free_groups(e);
     for (cudaStream_t st : e->gst) cudaStreamDestroy(st);
     for (cudaEvent_t ev : e->gev) cudaEventDestroy(ev);
+    for (cudaStream_t st : e->mst) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : e->mev) cudaEventDestroy(ev);
     if (e->d_tile0) cudaFree(e->d_tile0);
     if (e->d_off) cudaFree(e->d_off);
     if (e->d_pers) cudaFree(e->d_pers);

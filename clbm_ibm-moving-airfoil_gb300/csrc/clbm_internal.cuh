@@ -185,7 +185,11 @@ __device__ inline bool in_band(const Band& b, int x, int y, int z, int ny, int n
     return (unsigned)(x - b.i0) < (unsigned)b.ilen && oy < b.jlen && oz < b.klen;
 }
 
+// slot < 0: the slot of the call the device record names current (dev->cur & 1), for
+// launches whose call index the host does not track (one ensemble member per launch; the
+// ensemble orders the next call's marker kernel after the step).
 __device__ __forceinline__ Band load_band(const IbmDev* dev, int slot) {
+    if (slot < 0) slot = (int)(dev->cur & 1);
     const int4 a = *reinterpret_cast<const int4*>(dev->band[slot]);
     const int2 b = *reinterpret_cast<const int2*>(dev->band[slot] + 4);
     return Band{a.x, a.y, a.z, a.w, b.x, b.y};
@@ -285,7 +289,8 @@ struct ForceArgs {
     const IbmDev* dev;     // band mode: boxes of the compute_force calls
     int slot;              // band mode: box slot of the call this step applies (call index & 1),
                            // passed by the host so the next call's marker kernel may run
-                           // while this step's bulk pass still reads it
+                           // while this step's bulk pass still reads it; -1: read on the
+                           // device (load_band)
 };
 
 int knob(const char* name, int def);  // integer tuning parameter from the environment

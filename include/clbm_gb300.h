@@ -195,7 +195,8 @@ int clbm_ensemble_create(clbm_solver* const* solvers, clbm_ibm* const* ibms,
 int clbm_ensemble_run(clbm_ensemble* e, int32_t nsteps, int32_t use_graph);
 int clbm_ensemble_stream(const clbm_ensemble* e, void** out);
 /* The bulk-pass schedule chosen at creation: tile width (cells; 0: whole rows per block,
- * members grouped by row width, one launch per group), blocks, tiles, the time of one
+ * members grouped by row width, one launch per group; -1: one single-lattice launch per
+ * member over concurrent streams, blocks = tiles = members), blocks, tiles, the time of one
  * bulk pass of all members with it, alone, in milliseconds, and in the row mode the rows
  * one block computes per tile (0 otherwise). Any pointer may be NULL. */
 int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* blocks,

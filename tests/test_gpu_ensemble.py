@@ -1,6 +1,8 @@
 """Batched ensemble: members stepped together give the same results as each case stepped
 alone (same per-cell arithmetic, fixed-point spreading), in float32 and 16-bit storage."""
 
+import os
+
 import numpy as np
 import pytest
 
@@ -22,15 +24,21 @@ def _cases(pkg, storage, n=5, lattices=SMALL):
 @pytest.mark.parametrize("graph", [True, False])
 @pytest.mark.parametrize("variant", ["cell", "pair"])
 @pytest.mark.parametrize("lattices", [SMALL, MIXED], ids=["even", "mixed"])
-@pytest.mark.parametrize("rows", ["1", "1:3", "0"])
+@pytest.mark.parametrize("rows", ["1", "1:3", "0", "m"])
 def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, graph, variant, lattices,
                                             rows):
     """The single runs use either full-grid kernel; all variants give the same bits; the
     ensemble bulk pass with whole rows per block (rows = 1: the autotuner's rows per tile;
-    1:3: three rows per tile, which does not divide the members' row counts) or with row
-    segments / runs (0)."""
+    1:3: three rows per tile, which does not divide the members' row counts), with row
+    segments / runs or whatever else the autotuner picks (0), or as one single-lattice
+    launch per member over concurrent streams (m)."""
     pkg = built_pkg
     monkeypatch.setenv("CLBM_KERNEL", variant)
+    if rows == "m":
+        monkeypatch.setenv("CLBM_ENS_MEMBERS", "1")
+        rows = "0"
+    else:
+        monkeypatch.setenv("CLBM_ENS_MEMBERS", "0" if rows != "0" else "-1")
     mode, _, per_tile = rows.partition(":")
     monkeypatch.setenv("CLBM_ENS_ROWS", mode)
     monkeypatch.setenv("CLBM_ENS_ROWS_R", per_tile or "0")
@@ -38,9 +46,11 @@ def test_ensemble_members_equal_single_runs(built_pkg, monkeypatch, storage, gra
     ens = pkg.Ensemble(cases)
     ens.run(24, graph=graph)
     t = ens.tuning()
-    assert t["tile_width"] in (0, 128, 256) and t["blocks"] > 0 and t["tiles"] > 0
+    assert t["tile_width"] in (-1, 0, 128, 256) and t["blocks"] > 0 and t["tiles"] > 0
     if mode == "1":
         assert t["tile_width"] == 0 and t["rows_per_block"] == int(per_tile or t["rows_per_block"]) > 0
+    if os.environ.get("CLBM_ENS_MEMBERS") == "1":
+        assert t["tile_width"] == -1 and t["blocks"] == len(cases)
     for cfg, member in zip(cases, ens.sims):
         alone = pkg.Simulation(cfg)
         alone.run(24, graph=graph)
