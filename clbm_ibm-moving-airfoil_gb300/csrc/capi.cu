@@ -1292,7 +1292,7 @@ int ens_members_setup(clbm_ensemble* e) {
     if (!e->mst.empty()) return CLBM_OK;
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    const int k = std::min(kMemberStreams, e->n);
+    const int k = std::max(1, std::min(knob("CLBM_ENS_MEMBER_STREAMS", kMemberStreams), e->n));
     for (int i = 0; i < k; ++i) {
         cudaStream_t st;
         CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, lo));
