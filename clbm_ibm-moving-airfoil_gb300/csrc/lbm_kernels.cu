@@ -84,8 +84,8 @@ __global__ void __launch_bounds__(kBoxBlock, 8) k_box_rows_cell(const typename P
 
 // ------------------------------------------------------------------ 16-bit pair kernel
 // Two cells per thread (Pair, pair_body in lbm_device.cuh).
-// PX threads per block (2 PX cells along x): 64 or 128, whichever leaves fewer idle lanes
-// at the row ends (pair_threads).
+// PX threads per block (2 PX cells along x): 32, 64 or 128, whichever leaves fewer idle
+// lanes at the row ends (pair_threads; 64 on a tie with 32).
 template <int S, bool PULL, int FMODE, int PX, bool IDX32>
 __global__ void __launch_bounds__(PX, 1024 / PX) k_stream_collide_pair(const typename Pair<S>::T* __restrict__ fin,
                                                                     typename Pair<S>::T* __restrict__ fout,
@@ -95,7 +95,9 @@ __global__ void __launch_bounds__(PX, 1024 / PX) k_stream_collide_pair(const typ
 }
 
 static int pair_threads(int nx) {
-    const int w64 = (nx + 127) / 128 * 128 - nx, w128 = (nx + 255) / 256 * 256 - nx;
+    const int w32 = (nx + 63) / 64 * 64 - nx, w64 = (nx + 127) / 128 * 128 - nx,
+              w128 = (nx + 255) / 256 * 256 - nx;
+    if (w32 < w64) return 32;   // narrow rows (150, 300 cells): 64 cells per block
     return w64 < w128 ? 64 : 128;
 }
 
@@ -612,7 +614,9 @@ static void sc_launch(int fmode, int variant, const void* fin, void* fout, const
         return;
     }
     if constexpr (S != CLBM_STORE_F32) if (variant == kVariantPair) {
-        if (pair_threads(g.nx) == 64) pair_launch<S, PULL, 64>(fmode, fin, fout, g, c, fa, st);
+        const int px = pair_threads(g.nx);
+        if (px == 64) pair_launch<S, PULL, 64>(fmode, fin, fout, g, c, fa, st);
+        else if (px == 32) pair_launch<S, PULL, 32>(fmode, fin, fout, g, c, fa, st);
         else pair_launch<S, PULL, 128>(fmode, fin, fout, g, c, fa, st);
         return;
     }
