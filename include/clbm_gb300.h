@@ -178,10 +178,11 @@ int clbm_run(clbm_solver* s, clbm_ibm* ibm, const clbm_motion* m, int32_t nsteps
 
 /* Batched ensemble (no counterpart in the reference, which runs one case per process):
  * many independent solvers, each with its own IBM (or NULL) and motion law, stepped
- * together -- each step is seven launches over all members (markers, force-box offsets,
- * band macro, interpolation/spreading, force sums, force-box pass, and the bulk
- * stream-collide over every member's cells: one launch over a flat tile list, or one
- * launch per row width, run concurrently), or one persistent launch when the ensemble is
+ * together -- each step is six batched launches over all members (markers, force-box
+ * offsets, band macro, interpolation/spreading, force sums, force-box pass) and the bulk
+ * stream-collide over every member's cells (one launch over a flat tile list, one launch
+ * per row width, or one single-lattice launch per member, run concurrently; timed at
+ * creation), or one persistent launch when the ensemble is
  * created with CLBM_ENS_STEP=persistent (clbm_ensemble_schedule). Members keep their buffers and
  * all per-member reads (clbm_read_macro, ibm_read_force_history, ...) keep working; the
  * members must be fresh or at the same step, share storage form and device, and outlive
@@ -206,14 +207,14 @@ int clbm_ensemble_tuning(const clbm_ensemble* e, int32_t* tile_width, int32_t* b
  * waits, the bulk pass's tiles shared out over the phases), chosen by the environment
  * variable CLBM_ENS_STEP=persistent when the ensemble is created (at most 128 members:
  * their constants travel in the launch's parameter table), with *blocks its grid;
- * 0 and 0 for the seven launches. Both forms give the same bits. A barrier wait that ran
+ * 0 and 0 for separate launches. Both forms give the same bits. A barrier wait that ran
  * out is reported by the next clbm_ensemble_run (CLBM_ERR_STATE). Any pointer may be
  * NULL. */
 int clbm_ensemble_schedule(const clbm_ensemble* e, int32_t* persistent, int32_t* blocks);
 /* Phase clock of the last persistent step, in microseconds (5 entries): markers; box
  * offsets + bulk share; band prepare + bulk share; interpolation/spreading + bulk share; and
  * force sums, box pass and the rest of the bulk pass as seen by block 0 (the launch ends
- * when its last block does). Waits for the ensemble's stream. CLBM_ERR_STATE for the seven
+ * when its last block does). Waits for the ensemble's stream. CLBM_ERR_STATE for separate
  * launches. */
 int clbm_ensemble_phase_times(clbm_ensemble* e, double* us);
 int clbm_ensemble_destroy(clbm_ensemble* e);
