@@ -170,7 +170,14 @@ def test_persistent_step_equals_separate_launches(built_pkg, monkeypatch, storag
             monkeypatch.delenv("CLBM_ENS_STEP", raising=False)
         ens = pkg.Ensemble(cases)
         assert ens.schedule()["persistent"] == (form == "persistent")
+        if form == "launches":
+            assert ens.schedule()["blocks"] == 0
+            with pytest.raises(pkg.CLBMError):
+                ens.phase_times()   # the phase clock belongs to the persistent step
         ens.run(24, graph=graph)
+        if form == "persistent":
+            ph = ens.phase_times()
+            assert all(v >= 0 for v in ph.values()) and ph["spreading"] > 0
         out[form] = [(m.solver.read_populations(), m.ibm.force_history(24), m.ibm.step_count())
                      for m in ens.sims]
         ens.close()
